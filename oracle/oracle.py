@@ -1,0 +1,194 @@
+"""ctypes binding of the CPU oracle (liboracle.so) and of the reference-header build (_ref/libref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()`` as the checker and by bench.py's
+CPU-baseline leg.  Nothing on the product path imports this module.
+"""
+import ctypes as C
+import os
+import subprocess
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REFLIB = os.path.join(HERE, "_ref", "libref.so")
+
+
+class Tex(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("ncomp", C.c_int), ("data", C.c_void_p)]
+
+
+class Geom(C.Structure):
+    _fields_ = [("node", C.c_void_p), ("prim", C.c_void_p), ("solid", C.c_void_p), ("num_solid", C.c_int),
+                ("inst", C.c_void_p), ("inst_inv", C.c_void_p), ("num_inst", C.c_int),
+                ("itra", C.c_void_p), ("plan", C.c_void_p)]
+
+
+class Sim(C.Structure):
+    _fields_ = [("geom", Geom), ("bnd", Tex), ("bnd_nm0", C.c_float), ("bnd_nms", C.c_float),
+                ("optical", C.c_void_p), ("icdf", Tex), ("hd_factor", C.c_int), ("max_bounce", C.c_int),
+                ("max_time", C.c_float), ("tmin", C.c_float), ("tmin0", C.c_float), ("tmax", C.c_float),
+                ("eps0_mask", C.c_uint32), ("seed", C.c_uint64), ("offset", C.c_uint64),
+                ("skipahead_event_offset", C.c_uint64), ("debug_tag", C.c_int)]
+
+
+def build(ref=False):
+    subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
+    if ref:
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref"])
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# flags after which the smaller epsilon applies: TO,CK,SI,SC,RE (sysrap/SEventConfig.cc:104)
+EPS0_MASK = (1 << 2) | (1 << 0) | (1 << 1) | (1 << 5) | (1 << 4)
+
+
+class SimConfig:
+    """Owns the arrays a Sim struct points at (so they outlive the ctypes struct)."""
+
+    def __init__(self, arrays, max_bounce=31, max_time=1e27, tmin=0.05, tmin0=0.05, tmax=1e6, seed=0, offset=0,
+                 skipahead=100000, debug_tag=1):
+        from_geom = arrays
+        self.node = np.ascontiguousarray(from_geom["node"], dtype=np.float32)
+        self.prim = np.ascontiguousarray(from_geom["prim"], dtype=np.float32)
+        self.solid = np.ascontiguousarray(from_geom["solid"])
+        self.inst = np.ascontiguousarray(from_geom["inst"], dtype=np.float32)
+        self.inst_inv = np.ascontiguousarray(invert_instances(self.inst))
+        self.itra = np.ascontiguousarray(from_geom["itra"], dtype=np.float32)
+        if self.itra.size == 0:
+            self.itra = np.zeros((1, 4, 4), dtype=np.float32)
+        self.plan = np.ascontiguousarray(from_geom["plan"], dtype=np.float32)
+        if self.plan.size == 0:
+            self.plan = np.zeros((1, 4), dtype=np.float32)
+        bnd = np.ascontiguousarray(from_geom["bnd"], dtype=np.float32)
+        self.bnd_tex = bnd.reshape(-1, bnd.shape[-2], 4)          # (num_bnd*4*2, 761, 4)
+        self.optical = np.ascontiguousarray(from_geom["optical"], dtype=np.uint32)
+        self.icdf = np.ascontiguousarray(from_geom["icdf"], dtype=np.float32)
+        nm0, nms = from_geom["domain"]
+        s = Sim()
+        s.geom = Geom(_ptr(self.node), _ptr(self.prim), _ptr(self.solid), len(self.solid), _ptr(self.inst),
+                      _ptr(self.inst_inv), len(self.inst), _ptr(self.itra), _ptr(self.plan))
+        s.bnd = Tex(self.bnd_tex.shape[1], self.bnd_tex.shape[0], 4, _ptr(self.bnd_tex))
+        s.bnd_nm0 = nm0
+        s.bnd_nms = nms
+        s.optical = _ptr(self.optical)
+        s.icdf = Tex(self.icdf.shape[1], self.icdf.shape[0], 1, _ptr(self.icdf))
+        s.hd_factor = int(from_geom["hd_factor"])
+        s.max_bounce = max_bounce
+        s.max_time = max_time
+        s.tmin = tmin
+        s.tmin0 = tmin0
+        s.tmax = tmax
+        s.eps0_mask = EPS0_MASK
+        s.seed = seed
+        s.offset = offset
+        s.skipahead_event_offset = skipahead
+        s.debug_tag = debug_tag
+        self.sim = s
+
+
+def invert_instances(inst):
+    m = inst.astype(np.float64).copy()
+    m[:, :, 3] = (0, 0, 0, 1)
+    inv = np.linalg.inv(m)
+    inv[:, :, 3] = (0, 0, 0, 1)
+    return inv.astype(np.float32)
+
+
+class _Lib:
+    def __init__(self, path, prefix):
+        self.lib = C.CDLL(path)
+        self.prefix = prefix
+
+
+_oracle = None
+_ref = None
+
+
+def lib():
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(LIB):
+            build()
+        _oracle = C.CDLL(LIB)
+        _oracle.orc_fill_seed.restype = C.c_int64
+        _oracle.orc_select_hits.restype = C.c_int64
+        _oracle.orc_intersect_prim_c.restype = C.c_int
+    return _oracle
+
+
+def reflib():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REFLIB):
+            return None
+        _ref = C.CDLL(REFLIB)
+        _ref.ref_intersect_prim.restype = C.c_int
+    return _ref
+
+
+def simulate(cfg, gs, input_photon=None, event_index=0, photon_offset=0, nthreads=1, seq=True, use_ref=False):
+    """Run the oracle (or the reference-header build) over every photon of ``gs``. Returns (photons, seq)."""
+    from importlib import import_module
+    L = import_module("eic_opticks_gb300.layout")
+    gs = np.ascontiguousarray(gs, dtype=np.float32)
+    counts = gs.view(np.uint32)[:, 0, 3].astype(np.int64)
+    seed = np.ascontiguousarray(np.repeat(np.arange(len(gs), dtype=np.int32), counts))
+    n = len(seed)
+    out = np.zeros(n, dtype=L.PHOTON)
+    sq = np.zeros(n, dtype=L.SEQ) if seq else None
+    inp = np.ascontiguousarray(input_photon) if input_photon is not None else np.zeros(1, dtype=L.PHOTON)
+    if use_ref:
+        r = reflib()
+        if r is None:
+            raise RuntimeError("reference build oracle/_ref/libref.so not present")
+        r.ref_simulate(C.byref(cfg.sim), _ptr(gs), _ptr(seed), _ptr(inp), C.c_uint64(photon_offset),
+                       C.c_uint32(event_index), C.c_int64(n), _ptr(out), _ptr(sq) if sq is not None else None)
+    else:
+        lib().orc_simulate(C.byref(cfg.sim), _ptr(gs), _ptr(seed), _ptr(inp), C.c_uint64(photon_offset),
+                           C.c_uint32(event_index), C.c_int64(n), _ptr(out),
+                           _ptr(sq) if sq is not None else None, C.c_int(nthreads))
+    return out, sq
+
+
+def philox_uniforms(seed, subsequence, offset, skip, n, use_ref=False):
+    out = np.zeros(n, dtype=np.float32)
+    if use_ref:
+        reflib().ref_curand_uniforms(C.c_uint64(seed), C.c_uint64(subsequence), C.c_uint64(offset),
+                                     C.c_uint64(skip), C.c_int(n), _ptr(out))
+    else:
+        lib().orc_philox_uniforms(C.c_uint64(seed), C.c_uint64(subsequence), C.c_uint64(offset),
+                                  C.c_uint64(skip), C.c_int(n), _ptr(out))
+    return out
+
+
+def intersect_prim(node, plan, itra, t_min, o, d, use_ref=False):
+    node = np.ascontiguousarray(node, dtype=np.float32)
+    plan = np.ascontiguousarray(plan if plan is not None and len(plan) else np.zeros((1, 4)), dtype=np.float32)
+    itra = np.ascontiguousarray(itra if itra is not None and len(itra) else np.zeros((1, 4, 4)), dtype=np.float32)
+    o = np.ascontiguousarray(o, dtype=np.float32)
+    d = np.ascontiguousarray(d, dtype=np.float32)
+    out = np.zeros(4, dtype=np.float32)
+    if use_ref:
+        v = reflib().ref_intersect_prim(_ptr(node), _ptr(plan), _ptr(itra), C.c_float(t_min), _ptr(o), _ptr(d), _ptr(out))
+    else:
+        v = lib().orc_intersect_prim_c(_ptr(node), _ptr(plan), _ptr(itra), C.c_float(t_min), _ptr(o), _ptr(d), _ptr(out))
+    return bool(v), out
+
+
+def tex_lookup(tex, xy):
+    """CUDA linear-filter emulation: tex is (ny, nx) float or (ny, nx, 4) float4; xy (n, 2) normalized coords."""
+    tex = np.ascontiguousarray(tex, dtype=np.float32)
+    xy = np.ascontiguousarray(xy, dtype=np.float32)
+    n = len(xy)
+    if tex.ndim == 3:
+        t = Tex(tex.shape[1], tex.shape[0], 4, _ptr(tex))
+        out = np.zeros((n, 4), dtype=np.float32)
+        lib().orc_tex_lookup4(C.byref(t), _ptr(xy), C.c_int(n), _ptr(out))
+    else:
+        t = Tex(tex.shape[1], tex.shape[0], 1, _ptr(tex))
+        out = np.zeros(n, dtype=np.float32)
+        lib().orc_tex_lookup1(C.byref(t), _ptr(xy), C.c_int(n), _ptr(out))
+    return out
