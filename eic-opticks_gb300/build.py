@@ -1,0 +1,70 @@
+"""Compile recipe for libgbopticks.so (sm_103a) : explicit nvcc / g++ invocations, no cmake.
+
+The library is built in-tree at ``eic-opticks_gb300/libgbopticks.so`` so that a process loading it shows the
+in-tree path.  Host C++ is compiled with -ffp-contract=off so that the inverse instance transforms are the same
+binary32 values on x86-64 and aarch64 hosts.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libgbopticks.so")
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+CU_SOURCES = ["gbo_engine.cu"]
+CPP_SOURCES = ["gbo_accel.cpp"]
+HEADERS = ["gbo_device.cuh", "gbo_csg.cuh", "gbo_physics.cuh", "gbo_trace.cuh", "gbo_accel.h"]
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose=False, force=False, ptxas_verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    deps = [os.path.join(CSRC, f) for f in CU_SOURCES + CPP_SOURCES + HEADERS]
+    deps += [os.path.join(inc, f) for f in ("gbopticks.h", "gbo_types.h")]
+    if not force and not _newer(LIB, deps):
+        return LIB
+    procs, objs = [], []
+    for f in CU_SOURCES:
+        o = os.path.join(BUILD, f + ".o")
+        cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", inc, "-c",
+               os.path.join(CSRC, f), "-o", o]
+        if ptxas_verbose:
+            cmd[1:1] = ["-Xptxas", "-v"]
+        procs.append(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT))
+        objs.append(o)
+    for f in CPP_SOURCES:
+        o = os.path.join(BUILD, f + ".o")
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", inc, "-c", os.path.join(CSRC, f), "-o", o]
+        procs.append(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT))
+        objs.append(o)
+    logs = []
+    for p in procs:
+        out, _ = p.communicate()
+        logs.append(out.decode(errors="replace"))
+        if p.returncode != 0:
+            sys.stderr.write(out.decode(errors="replace"))
+            raise RuntimeError("compile failed: %s" % " ".join(p.args))
+    tmp = LIB + ".tmp"
+    link = [NVCC, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs]
+    subprocess.check_call(link)
+    os.replace(tmp, LIB)
+    if verbose or ptxas_verbose:
+        for lg in logs:
+            if lg.strip():
+                print(lg)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, force="--force" in sys.argv, ptxas_verbose="-v" in sys.argv)

@@ -1,0 +1,230 @@
+// gbo_accel.cpp : host builder of the two-level acceleration structure (see gbo_accel.h).
+#include "gbo_accel.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+namespace gbo {
+
+namespace {
+
+struct Box {
+    double lo[3] = {1e300, 1e300, 1e300};
+    double hi[3] = {-1e300, -1e300, -1e300};
+    void grow(const double* p) { for (int k = 0; k < 3; k++) { lo[k] = std::min(lo[k], p[k]); hi[k] = std::max(hi[k], p[k]); } }
+    void grow(const Box& b) { grow(b.lo); grow(b.hi); }
+    bool empty() const { return lo[0] > hi[0]; }
+    double area() const
+    {
+        if (empty()) return 0.0;
+        double d0 = hi[0] - lo[0], d1 = hi[1] - lo[1], d2 = hi[2] - lo[2];
+        return 2.0 * (d0 * d1 + d1 * d2 + d2 * d0);
+    }
+    double centroid(int k) const { return 0.5 * (lo[k] + hi[k]); }
+};
+
+// AABBs are padded so that float round-off in the slab test never culls a hit on the surface itself
+void pad(Box& b)
+{
+    double ext = 0.0;
+    for (int k = 0; k < 3; k++) ext = std::max(ext, std::max(std::fabs(b.lo[k]), std::fabs(b.hi[k])));
+    const double e = 1e-5 * ext + 1e-3;
+    for (int k = 0; k < 3; k++) { b.lo[k] -= e; b.hi[k] += e; }
+}
+
+void invert_affine(const double m[3][3], const double t[3], double r[3][3], double it[3])
+{
+    double det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                 m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    r[0][0] = (m[1][1] * m[2][2] - m[1][2] * m[2][1]) / det;
+    r[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) / det;
+    r[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) / det;
+    r[1][0] = (m[1][2] * m[2][0] - m[1][0] * m[2][2]) / det;
+    r[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) / det;
+    r[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) / det;
+    r[2][0] = (m[1][0] * m[2][1] - m[1][1] * m[2][0]) / det;
+    r[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) / det;
+    r[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) / det;
+    for (int j = 0; j < 3; j++) it[j] = -(t[0] * r[0][j] + t[1] * r[1][j] + t[2] * r[2][j]);
+}
+
+struct Builder {
+    std::vector<Box> boxes;
+    std::vector<int32_t>& index;
+    std::vector<BvhNode>& nodes;
+    int max_depth = 0;
+
+    Builder(std::vector<int32_t>& idx, std::vector<BvhNode>& n) : index(idx), nodes(n) {}
+
+    int build(int begin, int end, int depth)
+    {
+        max_depth = std::max(max_depth, depth);
+        Box bb, cb;
+        for (int i = begin; i < end; i++) {
+            bb.grow(boxes[index[i]]);
+            double c[3] = {boxes[index[i]].centroid(0), boxes[index[i]].centroid(1), boxes[index[i]].centroid(2)};
+            cb.grow(c);
+        }
+        int self = (int)nodes.size();
+        nodes.push_back(BvhNode{});
+        for (int k = 0; k < 3; k++) { nodes[self].bmin[k] = (float)bb.lo[k]; nodes[self].bmax[k] = (float)bb.hi[k]; }
+        const int n = end - begin;
+        if (n <= 2 || depth >= 48) {
+            nodes[self].left_first = begin;
+            nodes[self].count = n;
+            return self;
+        }
+        // binned SAH over the widest centroid axis, 16 bins
+        int axis = 0;
+        for (int k = 1; k < 3; k++) if (cb.hi[k] - cb.lo[k] > cb.hi[axis] - cb.lo[axis]) axis = k;
+        int mid = begin + n / 2;
+        const double span = cb.hi[axis] - cb.lo[axis];
+        if (span > 0.0) {
+            const int NB = 16;
+            Box bin[NB];
+            int cnt[NB] = {0};
+            for (int i = begin; i < end; i++) {
+                int b = (int)((boxes[index[i]].centroid(axis) - cb.lo[axis]) / span * NB);
+                b = std::min(NB - 1, std::max(0, b));
+                cnt[b]++;
+                bin[b].grow(boxes[index[i]]);
+            }
+            double best = 1e300;
+            int best_split = -1;
+            for (int s = 1; s < NB; s++) {
+                Box l, r;
+                int nl = 0, nr = 0;
+                for (int b = 0; b < s; b++) { if (cnt[b]) { l.grow(bin[b]); nl += cnt[b]; } }
+                for (int b = s; b < NB; b++) { if (cnt[b]) { r.grow(bin[b]); nr += cnt[b]; } }
+                if (nl == 0 || nr == 0) continue;
+                double cost = l.area() * nl + r.area() * nr;
+                if (cost < best) { best = cost; best_split = s; }
+            }
+            if (best_split > 0) {
+                auto it = std::partition(index.begin() + begin, index.begin() + end, [&](int32_t id) {
+                    int b = (int)((boxes[id].centroid(axis) - cb.lo[axis]) / span * NB);
+                    b = std::min(NB - 1, std::max(0, b));
+                    return b < best_split;
+                });
+                mid = (int)(it - index.begin());
+            }
+            if (mid == begin || mid == end) {
+                std::nth_element(index.begin() + begin, index.begin() + begin + n / 2, index.begin() + end,
+                                 [&](int32_t a, int32_t b) { return boxes[a].centroid(axis) < boxes[b].centroid(axis); });
+                mid = begin + n / 2;
+            }
+        }
+        const int l = build(begin, mid, depth + 1);
+        const int r = build(mid, end, depth + 1);
+        (void)l;
+        nodes[self].left_first = r;     // left child is always self+1
+        nodes[self].count = 0;
+        return self;
+    }
+};
+
+}  // namespace
+
+int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, int num_prim,
+                const gbo_csgsolid* solid, int num_solid, const gbo_qat4* inst, int num_inst, AccelHost& out,
+                char* err, int errlen)
+{
+    out = AccelHost{};
+    if (num_inst <= 0 || num_solid <= 0 || num_prim <= 0 || num_node <= 0) {
+        std::snprintf(err, errlen, "empty geometry (nodes %d prims %d solids %d instances %d)", num_node, num_prim,
+                      num_solid, num_inst);
+        return 1;
+    }
+    if (num_inst > 0x10000) {
+        std::snprintf(err, errlen, "%d instances exceed the 16-bit instance index of the photon record", num_inst);
+        return 1;
+    }
+    out.solid.resize(num_solid);
+    std::vector<Box> solid_box(num_solid);
+    out.prim.resize(num_prim);
+    for (int s = 0; s < num_solid; s++) {
+        const gbo_csgsolid& so = solid[s];
+        if (so.primOffset < 0 || so.numPrim < 0 || so.primOffset + so.numPrim > num_prim) {
+            std::snprintf(err, errlen, "solid %d prim range [%d,+%d) outside %d prims", s, so.primOffset, so.numPrim, num_prim);
+            return 1;
+        }
+        out.solid[s] = SolidDev{so.primOffset, so.numPrim};
+        for (int k = 0; k < so.numPrim; k++) {
+            const int pi = so.primOffset + k;
+            const gbo_csgprim& pr = prim[pi];
+            const int noff = pr.q0.i[1];
+            const int nn = pr.q0.i[0];
+            if (noff < 0 || nn <= 0 || noff + nn > num_node) {
+                std::snprintf(err, errlen, "prim %d node range [%d,+%d) outside %d nodes", pi, noff, nn, num_node);
+                return 1;
+            }
+            Box b;
+            double lo[3] = {pr.q2.f[0], pr.q2.f[1], pr.q2.f[2]};
+            double hi[3] = {pr.q2.f[3], pr.q3.f[0], pr.q3.f[1]};
+            b.grow(lo);
+            b.grow(hi);
+            pad(b);
+            PrimDev& pd = out.prim[pi];
+            for (int j = 0; j < 3; j++) { pd.bmin[j] = (float)b.lo[j]; pd.bmax[j] = (float)b.hi[j]; }
+            pd.node_offset = noff;
+            const unsigned boundary = node[noff].q1.u[2];
+            const unsigned gpi = pr.q3.u[3];
+            pd.prim_boundary = ((gpi & 0xffffu) << 16) | (boundary & 0xffffu);
+            solid_box[s].grow(b);
+        }
+    }
+    out.inst.resize(num_inst);
+    std::vector<Box> inst_box(num_inst);
+    for (int i = 0; i < num_inst; i++) {
+        const gbo_qat4& q = inst[i];
+        const int s = q.q1.i[3];
+        if (s < 0 || s >= num_solid) {
+            std::snprintf(err, errlen, "instance %d refers to solid %d of %d", i, s, num_solid);
+            return 1;
+        }
+        double m[3][3] = {{q.q0.f[0], q.q0.f[1], q.q0.f[2]}, {q.q1.f[0], q.q1.f[1], q.q1.f[2]}, {q.q2.f[0], q.q2.f[1], q.q2.f[2]}};
+        double t[3] = {q.q3.f[0], q.q3.f[1], q.q3.f[2]};
+        double r[3][3], it[3];
+        invert_affine(m, t, r, it);
+        InstDev& d = out.inst[i];
+        const bool ident = q.q0.f[0] == 1.f && q.q0.f[1] == 0.f && q.q0.f[2] == 0.f && q.q1.f[0] == 0.f &&
+                           q.q1.f[1] == 1.f && q.q1.f[2] == 0.f && q.q2.f[0] == 0.f && q.q2.f[1] == 0.f &&
+                           q.q2.f[2] == 1.f && q.q3.f[0] == 0.f && q.q3.f[1] == 0.f && q.q3.f[2] == 0.f;
+        // columns of the inverse in the row-vector convention of sqat4::right_multiply
+        for (int j = 0; j < 3; j++) {
+            float* c = j == 0 ? d.c0 : (j == 1 ? d.c1 : d.c2);
+            c[0] = (float)r[0][j];
+            c[1] = (float)r[1][j];
+            c[2] = (float)r[2][j];
+            c[3] = (float)it[j];
+        }
+        d.solid = s;
+        d.identity = (uint32_t)q.q2.i[3];
+        d.is_identity = ident ? 1 : 0;
+        d.iindex = (uint32_t)i;
+        const Box& sb = solid_box[s];
+        Box wb;
+        for (int cx = 0; cx < 2; cx++)
+            for (int cy = 0; cy < 2; cy++)
+                for (int cz = 0; cz < 2; cz++) {
+                    double p[3] = {cx ? sb.hi[0] : sb.lo[0], cy ? sb.hi[1] : sb.lo[1], cz ? sb.hi[2] : sb.lo[2]};
+                    double w[3];
+                    for (int k = 0; k < 3; k++) w[k] = p[0] * m[0][k] + p[1] * m[1][k] + p[2] * m[2][k] + t[k];
+                    wb.grow(w);
+                }
+        pad(wb);
+        inst_box[i] = wb;
+    }
+    out.tlas_index.resize(num_inst);
+    for (int i = 0; i < num_inst; i++) out.tlas_index[i] = i;
+    Builder b(out.tlas_index, out.tlas);
+    b.boxes = inst_box;
+    out.tlas.reserve(2 * num_inst);
+    b.build(0, num_inst, 0);
+    out.max_depth = b.max_depth;
+    return 0;
+}
+
+}  // namespace gbo

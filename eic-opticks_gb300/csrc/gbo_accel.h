@@ -1,0 +1,63 @@
+// gbo_accel.h : two-level acceleration structure replacing the reference's OptiX IAS/GAS.
+//
+// The reference builds one GAS per CSGSolid from CSGPrim AABBs and one IAS over the instance transforms
+// (CSGOptiX/SBT.cc:247-495, GAS_Builder.cc, IAS_Builder.cc), then lets OptiX traverse them.  Here:
+//   * level 1 (TLAS): a binned-SAH BVH over the world-space AABBs of all instances, built on the host;
+//   * level 2: the prims of the instance's solid, each with an object-space AABB test before intersect_prim
+//     (solids in these geometries hold a handful of prims).
+// Device layouts (all 16-byte aligned, read as float4/int4):
+//   BvhNode  32 B : bmin.xyz, left-child-or-first-index ; bmax.xyz, count (0 for inner nodes)
+//   InstDev  64 B : inverse transform as three float4 columns + (solid, identity, is_identity, iindex)
+//   PrimDev  32 B : object AABB min.xyz + node offset ; AABB max.xyz + (globalPrimIdx<<16 | boundary)
+#pragma once
+#include <cstdint>
+#include <vector>
+#include "../../include/gbo_types.h"
+
+namespace gbo {
+
+struct BvhNode {
+    float bmin[3];
+    int32_t left_first;
+    float bmax[3];
+    int32_t count;
+};
+static_assert(sizeof(BvhNode) == 32, "BvhNode is 32 bytes");
+
+struct InstDev {
+    float c0[4], c1[4], c2[4];     // columns of the inverse (object <- world) 3x4 transform: xyz rows + translation
+    int32_t solid;
+    uint32_t identity;             // sensor_identifier + 1, 0 : not a sensor
+    int32_t is_identity;
+    uint32_t iindex;
+};
+static_assert(sizeof(InstDev) == 64, "InstDev is 64 bytes");
+
+struct PrimDev {
+    float bmin[3];
+    int32_t node_offset;
+    float bmax[3];
+    uint32_t prim_boundary;
+};
+static_assert(sizeof(PrimDev) == 32, "PrimDev is 32 bytes");
+
+struct SolidDev {
+    int32_t prim_offset;
+    int32_t num_prim;
+};
+
+struct AccelHost {
+    std::vector<BvhNode> tlas;
+    std::vector<int32_t> tlas_index;     // leaf ranges index into this permutation of instances
+    std::vector<InstDev> inst;
+    std::vector<PrimDev> prim;
+    std::vector<SolidDev> solid;
+    int max_depth = 0;
+};
+
+// Builds the host-side structure from CSGFoundry-layout arrays. Returns 0 on success.
+int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, int num_prim,
+                const gbo_csgsolid* solid, int num_solid, const gbo_qat4* inst, int num_inst, AccelHost& out,
+                char* err, int errlen);
+
+}  // namespace gbo

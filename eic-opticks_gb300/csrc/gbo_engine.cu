@@ -1,0 +1,824 @@
+// gbo_engine.cu : simulate kernel, hit compaction kernels and the C ABI of libgbopticks.so.
+//
+// One event = one pass of the photon program of CSGOptiX/CSGOptiX7.cu:405-503 over every photon its gensteps
+// describe, then hit selection (sysrap/SU.cu:89-92,155-160 via qudarap/QEvt.cc:934-967,1113-1131).
+//
+// Device-side flow of an event:
+//   k_genstep_prefix   inclusive prefix of genstep numphoton (replaces the seed array of QEvt.cu:181-237: a
+//                      photon finds its genstep by binary search, so no per-photon seed buffer is written)
+//   k_simulate<TREE>   one thread per photon: Philox stream, generate, bounce loop of trace + propagate, final
+//                      record; a warp ballot writes one 32-bit hit-bitmap word per 32 photons and hit photons are
+//                      appended (warp-aggregated atomics) to an unordered buffer unless the full photon array is kept
+//   k_word_prefix      per-word popcount prefix inside 256-word blocks + block totals
+//   k_block_offsets    exclusive scan of the block totals (one block) -> number of hits
+//   k_gather_*         hits written in photon order (the order thrust::copy_if gives the reference)
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gbopticks.h"
+#include "gbo_accel.h"
+#include "gbo_trace.cuh"
+
+namespace gbo {
+
+constexpr int SIM_BLOCK = 128;
+constexpr int SCAN_WORDS = 256;     // words per block in k_word_prefix
+
+struct Params {
+    Accel acc;
+    Tables tab;
+    int max_bounce;
+    float max_time, tmin, tmin0, tmax;
+    uint32_t eps0_mask, hitmask;
+    uint64_t seed, position0;
+    const float4* gs;
+    const unsigned long long* gs_end;     // inclusive prefix of numphoton
+    int num_gs;
+    long long num_photon;
+    unsigned long long photon_offset;
+    const gbo_sphoton* input_photon;
+    gbo_sphoton* photon_out;
+    gbo_seq* seq_out;
+    gbo_sphoton* hit_unordered;
+    unsigned long long* hit_count;
+    uint32_t* bitmap;
+};
+
+template <bool TREE>
+__global__ void __launch_bounds__(SIM_BLOCK) k_simulate(const __grid_constant__ Params P)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = idx < P.num_photon;
+    Photon p;
+    bool is_hit = false;
+    if (active) {
+        int lo = 0, hi = P.num_gs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(P.gs_end + mid) > (unsigned long long)idx) hi = mid; else lo = mid + 1;
+        }
+        const float4* g = P.gs + 6 * (size_t)lo;
+        float4 gq[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) gq[k] = __ldg(g + k);
+        const unsigned long long photon_idx = P.photon_offset + (unsigned long long)idx;
+
+        Rng rng;
+        rng_init(rng, P.seed, photon_idx, P.position0);
+
+        p.pos = f3(0.f, 0.f, 0.f); p.time = 0.f; p.mom = f3(0.f, 0.f, 0.f); p.hitcount_iindex = 0u;
+        p.pol = f3(0.f, 0.f, 0.f); p.wavelength = 0.f;
+        p.orient_boundary_flag = 0u; p.identity = 0u; p.index = 0u; p.flagmask = 0u;
+        const int gencode = __float_as_int(gq[0].x);
+        switch (gencode) {
+            case GBO_GS_TORCH: gen_torch(p, rng, gq, photon_idx); break;
+            case GBO_GS_CERENKOV:
+            case GBO_GS_G4Cerenkov_modified: gen_cerenkov(P.tab, p, rng, gq); break;
+            case GBO_GS_SCINTILLATION:
+            case GBO_GS_DsG4Scintillation_r4695: gen_scint(P.tab, p, rng, gq); break;
+            case GBO_GS_INPUT_PHOTON: load_photon(p, P.input_photon + idx); set_flag(p, GBO_TORCH); break;
+            default: break;
+        }
+        set_index(p, photon_idx);
+
+        Seq seq;
+        seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
+        int bounce = 0;
+        if (P.seq_out) seq_add(seq, 0u, flag_of(p), boundary_of(p));
+        while (bounce < P.max_bounce && p.time < P.max_time) {
+            const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
+            Hit h;
+            trace<TREE>(P.acc, p.pos, p.mom, tmin, P.tmax, h);
+            if ((h.prim_boundary & 0xffffu) == 0xffffu) break;
+            h.normal = normalize(h.normal);
+            const int command = propagate(P.tab, p, h, rng);
+            bounce++;
+            if (P.seq_out) seq_add(seq, (unsigned)bounce, flag_of(p), boundary_of(p));
+            if (command == CMD_BREAK) break;
+        }
+        is_hit = (p.flagmask & P.hitmask) == P.hitmask;
+        if (P.photon_out) store_photon(P.photon_out + idx, p);
+        if (P.seq_out) {
+            ulonglong2* s = reinterpret_cast<ulonglong2*>(P.seq_out + idx);
+            s[0] = make_ulonglong2(seq.his[0], seq.his[1]);
+            s[1] = make_ulonglong2(seq.bnd[0], seq.bnd[1]);
+        }
+    }
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned mask = __ballot_sync(0xffffffffu, is_hit);
+    const long long word = idx >> 5;
+    if (lane == 0 && word * 32 < P.num_photon) P.bitmap[word] = mask;
+    if (P.hit_unordered && mask) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(P.hit_count, (unsigned long long)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (is_hit) store_photon(P.hit_unordered + base + __popc(mask & ((1u << lane) - 1u)), p);
+    }
+}
+
+__global__ void k_genstep_prefix(const gbo_quad6* gs, int num_gs, unsigned long long* gs_end)
+{
+    // single block: chunked inclusive scan of numphoton
+    __shared__ unsigned long long buf[1024];
+    __shared__ unsigned long long carry;
+    if (threadIdx.x == 0) carry = 0ull;
+    __syncthreads();
+    for (int base = 0; base < num_gs; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        unsigned long long v = i < num_gs ? (unsigned long long)gs[i].q[0].u[3] : 0ull;
+        buf[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+            unsigned long long add = threadIdx.x >= (unsigned)off ? buf[threadIdx.x - off] : 0ull;
+            __syncthreads();
+            buf[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (i < num_gs) gs_end[i] = carry + buf[threadIdx.x];
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += buf[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+__global__ void k_word_prefix(const uint32_t* bitmap, long long words, uint32_t* word_prefix, uint32_t* block_sum)
+{
+    __shared__ uint32_t buf[SCAN_WORDS];
+    const long long w = (long long)blockIdx.x * SCAN_WORDS + threadIdx.x;
+    const uint32_t c = w < words ? (uint32_t)__popc(bitmap[w]) : 0u;
+    buf[threadIdx.x] = c;
+    __syncthreads();
+    for (int off = 1; off < SCAN_WORDS; off <<= 1) {
+        uint32_t add = threadIdx.x >= (unsigned)off ? buf[threadIdx.x - off] : 0u;
+        __syncthreads();
+        buf[threadIdx.x] += add;
+        __syncthreads();
+    }
+    if (w < words) word_prefix[w] = buf[threadIdx.x] - c;       // exclusive within block
+    if (threadIdx.x == SCAN_WORDS - 1) block_sum[blockIdx.x] = buf[threadIdx.x];
+}
+
+__global__ void k_block_offsets(uint32_t* block_sum, long long nblocks, unsigned long long* block_offset,
+                                unsigned long long* total)
+{
+    __shared__ unsigned long long buf[1024];
+    __shared__ unsigned long long carry;
+    if (threadIdx.x == 0) carry = 0ull;
+    __syncthreads();
+    for (long long base = 0; base < nblocks; base += blockDim.x) {
+        const long long i = base + threadIdx.x;
+        const unsigned long long v = i < nblocks ? (unsigned long long)block_sum[i] : 0ull;
+        buf[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+            unsigned long long add = threadIdx.x >= (unsigned)off ? buf[threadIdx.x - off] : 0ull;
+            __syncthreads();
+            buf[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (i < nblocks) block_offset[i] = carry + buf[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += buf[threadIdx.x];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__device__ __forceinline__ void copy_photon(gbo_sphoton* dst, const gbo_sphoton* src)
+{
+    const float4* s = reinterpret_cast<const float4*>(src);
+    float4* d = reinterpret_cast<float4*>(dst);
+    const float4 a = __ldg(s), b = __ldg(s + 1), c = __ldg(s + 2), e = __ldg(s + 3);
+    d[0] = a; d[1] = b; d[2] = c; d[3] = e;
+}
+
+// warp per bitmap word: lane j copies photon 32w+j when its bit is set
+__global__ void k_gather_photons(const gbo_sphoton* photons, const uint32_t* bitmap, const uint32_t* word_prefix,
+                                 const unsigned long long* block_offset, long long words, gbo_sphoton* hits)
+{
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31u;
+    if (w >= words) return;
+    const uint32_t m = bitmap[w];
+    if (!(m & (1u << lane))) return;
+    const unsigned long long rank = block_offset[w / SCAN_WORDS] + word_prefix[w] + __popc(m & ((1u << lane) - 1u));
+    copy_photon(hits + rank, photons + w * 32 + lane);
+}
+
+// thread per unordered hit: its photon index gives the bitmap rank, i.e. its place in photon order
+__global__ void k_gather_unordered(const gbo_sphoton* unordered, const unsigned long long* count,
+                                   unsigned long long photon_offset, const uint32_t* bitmap, const uint32_t* word_prefix,
+                                   const unsigned long long* block_offset, gbo_sphoton* hits)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((unsigned long long)i >= *count) return;
+    const gbo_sphoton* src = unordered + i;
+    const unsigned long long full = ((unsigned long long)(__ldg(&src->identity) >> 24) << 32) | __ldg(&src->index);
+    const unsigned long long rel = full - photon_offset;
+    const long long w = (long long)(rel >> 5);
+    const unsigned j = (unsigned)(rel & 31u);
+    const uint32_t m = bitmap[w];
+    const unsigned long long rank = block_offset[w / SCAN_WORDS] + word_prefix[w] + __popc(m & ((1u << j) - 1u));
+    copy_photon(hits + rank, src);
+}
+
+// ---- known-answer kernels (the reference keeps equivalents in qudarap/QSim.cu for QSimTest) -----------------
+
+__global__ void k_rng_sequence(uint64_t seed, uint64_t subsequence0, uint64_t position, int num_seq, int per_seq,
+                               float* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num_seq) return;
+    Rng r;
+    rng_init(r, seed, subsequence0 + (uint64_t)i, position);
+    for (int k = 0; k < per_seq; k++) out[(size_t)i * per_seq + k] = uniform(r);
+}
+
+__global__ void k_tex_lookup(Tables t, const float2* xy, int n, int which, float4* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 c = xy[i];
+    if (which == 0) out[i] = tex2D<float4>(t.bnd_tex, c.x, c.y);
+    else out[i] = make_float4(tex2D<float>(t.icdf_tex, c.x, c.y), 0.f, 0.f, 0.f);
+}
+
+__global__ void k_scint_wavelength(Tables t, const float* u, int n, float* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = scint_wavelength(t, u[i]);
+}
+
+}  // namespace gbo
+
+// ================================================================================================================
+// host side
+
+using namespace gbo;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CU(call)                                                                                           \
+    do {                                                                                                   \
+        cudaError_t err_ = (call);                                                                         \
+        if (err_ != cudaSuccess) return fail(GBO_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(err_)); \
+    } while (0)
+
+template <typename T>
+struct DBuf {
+    T* ptr = nullptr;
+    size_t cap = 0;     // elements
+    int ensure(size_t n)
+    {
+        if (n <= cap && ptr) return 0;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+        size_t want = n < 1 ? 1 : n;
+        if (cudaMalloc(&ptr, want * sizeof(T)) != cudaSuccess) {
+            ptr = nullptr;
+            return fail(GBO_ERR_CUDA, "cudaMalloc of %zu bytes failed", want * sizeof(T));
+        }
+        cap = want;
+        return 0;
+    }
+    void release() { if (ptr) cudaFree(ptr); ptr = nullptr; cap = 0; }
+};
+
+template <typename T>
+int upload(DBuf<T>& b, const void* src, size_t n, cudaStream_t s)
+{
+    int rc = b.ensure(n);
+    if (rc) return rc;
+    if (n) CU(cudaMemcpyAsync(b.ptr, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
+    return 0;
+}
+
+bool env_float(const char* k, float& v) { const char* s = std::getenv(k); if (!s || !*s) return false; v = std::strtof(s, nullptr); return true; }
+bool env_int(const char* k, long long& v) { const char* s = std::getenv(k); if (!s || !*s) return false; v = std::strtoll(s, nullptr, 10); return true; }
+
+uint32_t parse_flag_mask(const char* spec)
+{
+    static const struct { const char* abbrev; uint32_t flag; } T[] = {
+        {"CK", GBO_CERENKOV}, {"SI", GBO_SCINTILLATION}, {"TO", GBO_TORCH}, {"AB", GBO_BULK_ABSORB},
+        {"RE", GBO_BULK_REEMIT}, {"SC", GBO_BULK_SCATTER}, {"SD", GBO_SURFACE_DETECT}, {"SA", GBO_SURFACE_ABSORB},
+        {"DR", GBO_SURFACE_DREFLECT}, {"SR", GBO_SURFACE_SREFLECT}, {"BR", GBO_BOUNDARY_REFLECT},
+        {"BT", GBO_BOUNDARY_TRANSMIT}, {"NA", GBO_NAN_ABORT}, {"EC", GBO_EFFICIENCY_COLLECT},
+        {"EX", GBO_EFFICIENCY_CULL}, {"MI", GBO_MISS}};
+    uint32_t m = 0;
+    std::string s(spec);
+    size_t pos = 0;
+    while (pos <= s.size()) {
+        size_t c = s.find(',', pos);
+        std::string tok = s.substr(pos, c == std::string::npos ? std::string::npos : c - pos);
+        for (auto& e : T) if (tok == e.abbrev) m |= e.flag;
+        if (c == std::string::npos) break;
+        pos = c + 1;
+    }
+    return m;
+}
+
+}  // namespace
+
+struct gbo_engine {
+    int device = 0;
+    gbo_config cfg{};
+    cudaStream_t stream = nullptr;
+    // geometry
+    DBuf<BvhNode> tlas;
+    DBuf<int32_t> tlas_index;
+    DBuf<InstDev> inst;
+    DBuf<PrimDev> prim;
+    DBuf<SolidDev> solid;
+    DBuf<gbo_csgnode> node;
+    DBuf<float4> plan;
+    DBuf<gbo_qat4> itra;
+    DBuf<uint4> optical;
+    cudaArray_t bnd_array = nullptr, icdf_array = nullptr;
+    cudaTextureObject_t bnd_tex = 0, icdf_tex = 0;
+    int bnd_nx = 0, bnd_ny = 0, hd_factor = 0;
+    float nm0 = 60.f, nms = 1.f;
+    bool has_tree = false;
+    // event
+    DBuf<gbo_quad6> gs;
+    DBuf<unsigned long long> gs_end;
+    DBuf<gbo_sphoton> input;
+    DBuf<gbo_sphoton> photon;
+    DBuf<gbo_seq> seq;
+    DBuf<gbo_sphoton> hits_unordered;
+    DBuf<gbo_sphoton> hits;
+    DBuf<uint32_t> bitmap, word_prefix, block_sum;
+    DBuf<unsigned long long> block_offset;
+    DBuf<unsigned long long> counters;      // [0] unordered hit count, [1] total hits, [2] photons
+    unsigned long long* host_counters = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    long long num_photon = -1, num_hit = 0;
+    int32_t event_id = -1;
+    gbo_stats stats{};
+};
+
+extern "C" {
+
+const char* gbo_last_error(void) { return g_last_error.c_str(); }
+
+int gbo_config_default(gbo_config* c)
+{
+    if (!c) return fail(GBO_ERR_ARG, "gbo_config_default: null config");
+    std::memset(c, 0, sizeof(*c));
+    c->max_bounce = 31;
+    c->max_time = 1.e27f;
+    c->propagate_epsilon = 0.05f;
+    c->propagate_epsilon0 = 0.05f;
+    c->epsilon0_mask = GBO_TORCH | GBO_CERENKOV | GBO_SCINTILLATION | GBO_BULK_SCATTER | GBO_BULK_REEMIT;
+    c->hit_mask = GBO_SURFACE_DETECT;
+    c->rng_seed = 0;
+    c->rng_offset = 0;
+    c->event_skipahead = 100000;
+    c->tmax = 1000000.f;
+    c->debug_tag = 1;
+    c->record_photon = 0;
+    c->record_seq = 0;
+    c->max_photon = 0;
+    long long iv;
+    float fv;
+    if (env_int("OPTICKS_MAX_BOUNCE", iv)) c->max_bounce = (int32_t)iv;
+    if (env_float("OPTICKS_MAX_TIME", fv)) c->max_time = fv;
+    if (env_float("OPTICKS_PROPAGATE_EPSILON", fv)) c->propagate_epsilon = fv;
+    if (env_float("OPTICKS_PROPAGATE_EPSILON0", fv)) c->propagate_epsilon0 = fv;
+    if (const char* s = std::getenv("OPTICKS_PROPAGATE_EPSILON0_MASK")) c->epsilon0_mask = parse_flag_mask(s);
+    if (const char* s = std::getenv("OPTICKS_HIT_MASK")) c->hit_mask = parse_flag_mask(s);
+    if (env_int("OPTICKS_EVENT_SKIPAHEAD", iv)) c->event_skipahead = (uint64_t)iv;
+    if (const char* s = std::getenv("QRng__SEED_OFFSET")) {
+        char* end = nullptr;
+        c->rng_seed = std::strtoull(s, &end, 10);
+        if (end && *end == ':') c->rng_offset = std::strtoull(end + 1, nullptr, 10);
+    }
+    return GBO_OK;
+}
+
+static int make_texture(cudaArray_t* arr, cudaTextureObject_t* tex, const void* data, int nx, int ny, bool f4)
+{
+    cudaChannelFormatDesc ch = f4 ? cudaCreateChannelDesc<float4>() : cudaCreateChannelDesc<float>();
+    CU(cudaMallocArray(arr, &ch, (size_t)nx, (size_t)ny));
+    const size_t row = (size_t)nx * (f4 ? 16 : 4);
+    CU(cudaMemcpy2DToArray(*arr, 0, 0, data, row, row, (size_t)ny, cudaMemcpyHostToDevice));
+    cudaResourceDesc res;
+    std::memset(&res, 0, sizeof(res));
+    res.resType = cudaResourceTypeArray;
+    res.res.array.array = *arr;
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof(td));
+    td.addressMode[0] = cudaAddressModeWrap;
+    td.addressMode[1] = cudaAddressModeWrap;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    CU(cudaCreateTextureObject(tex, &res, &td, nullptr));
+    return 0;
+}
+
+void gbo_engine_destroy(gbo_engine* e)
+{
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->bnd_tex) cudaDestroyTextureObject(e->bnd_tex);
+    if (e->icdf_tex) cudaDestroyTextureObject(e->icdf_tex);
+    if (e->bnd_array) cudaFreeArray(e->bnd_array);
+    if (e->icdf_array) cudaFreeArray(e->icdf_array);
+    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->prim.release(); e->solid.release();
+    e->node.release(); e->plan.release(); e->itra.release(); e->optical.release();
+    e->gs.release(); e->gs_end.release(); e->input.release(); e->photon.release(); e->seq.release();
+    e->hits_unordered.release(); e->hits.release(); e->bitmap.release(); e->word_prefix.release();
+    e->block_sum.release(); e->block_offset.release(); e->counters.release();
+    if (e->host_counters) cudaFreeHost(e->host_counters);
+    for (auto& v : e->ev) if (v) cudaEventDestroy(v);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int device, gbo_engine** out)
+{
+    if (!g || !out) return fail(GBO_ERR_ARG, "gbo_engine_create: null argument");
+    *out = nullptr;
+    if (!g->node || !g->prim || !g->solid || !g->inst || !g->bnd || !g->optical || !g->icdf)
+        return fail(GBO_ERR_ARG, "gbo_engine_create: geometry array missing");
+    if (g->num_bnd <= 0 || g->bnd_nx <= 1 || g->icdf_nx <= 1 || (g->icdf_ny != 1 && g->icdf_ny != 3))
+        return fail(GBO_ERR_ARG, "gbo_engine_create: bad table shape (num_bnd %d bnd_nx %d icdf %dx%d)", g->num_bnd,
+                    g->bnd_nx, g->icdf_ny, g->icdf_nx);
+    if (g->hd_factor != 0 && g->hd_factor != 10 && g->hd_factor != 20)
+        return fail(GBO_ERR_ARG, "gbo_engine_create: hd_factor %d not in {0,10,20}", g->hd_factor);
+    if (g->bnd_domain_step <= 0.f) return fail(GBO_ERR_ARG, "gbo_engine_create: bnd_domain_step must be positive");
+    int ndev = 0;
+    CU(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(GBO_ERR_ARG, "gbo_engine_create: device %d of %d", device, ndev);
+    CU(cudaSetDevice(device));
+
+    AccelHost acc;
+    char err[512] = {0};
+    if (build_accel(g->node, g->num_node, g->prim, g->num_prim, g->solid, g->num_solid, g->inst, g->num_inst, acc, err,
+                    sizeof(err)))
+        return fail(GBO_ERR_ARG, "gbo_engine_create: %s", err);
+    for (int n = 0; n < g->num_node; n++) {
+        const unsigned tc = g->node[n].q3.u[2];
+        const unsigned gt = g->node[n].q3.u[3] & 0x7fffffffu;
+        if (tc >= GBO_CSG_UNION && tc <= GBO_CSG_DIFFERENCE) {}
+        if (gt > (unsigned)g->num_itra) return fail(GBO_ERR_ARG, "node %d transform %u beyond %d itra", n, gt, g->num_itra);
+        if (tc >= GBO_CSG_NODE && tc < GBO_CSG_LEAF) return fail(GBO_ERR_ARG, "node %d: CSG list nodes are not supported", n);
+    }
+
+    gbo_engine* e = new gbo_engine();
+    e->device = device;
+    if (cfg) e->cfg = *cfg; else gbo_config_default(&e->cfg);
+    int rc = 0;
+#define TRY(x) do { rc = (x); if (rc) { gbo_engine_destroy(e); return rc; } } while (0)
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        gbo_engine_destroy(e);
+        return fail(GBO_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    for (auto& v : e->ev) if (cudaEventCreate(&v) != cudaSuccess) { gbo_engine_destroy(e); return fail(GBO_ERR_CUDA, "cudaEventCreate failed"); }
+    if (cudaMallocHost(&e->host_counters, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+        gbo_engine_destroy(e);
+        return fail(GBO_ERR_CUDA, "cudaMallocHost failed");
+    }
+    for (int p = 0; p < g->num_prim; p++) {
+        const int noff = g->prim[p].q0.i[1];
+        const unsigned tc = g->node[noff].q3.u[2];
+        if (tc < GBO_CSG_NODE) e->has_tree = true;
+    }
+    TRY(upload(e->tlas, acc.tlas.data(), acc.tlas.size(), e->stream));
+    TRY(upload(e->tlas_index, acc.tlas_index.data(), acc.tlas_index.size(), e->stream));
+    TRY(upload(e->inst, acc.inst.data(), acc.inst.size(), e->stream));
+    TRY(upload(e->prim, acc.prim.data(), acc.prim.size(), e->stream));
+    TRY(upload(e->solid, acc.solid.data(), acc.solid.size(), e->stream));
+    TRY(upload(e->node, g->node, (size_t)g->num_node, e->stream));
+    std::vector<float4> plan(g->num_plan > 0 ? g->num_plan : 1, make_float4(0, 0, 0, 0));
+    if (g->num_plan > 0 && g->plan) std::memcpy(plan.data(), g->plan, sizeof(float4) * g->num_plan);
+    TRY(upload(e->plan, plan.data(), plan.size(), e->stream));
+    std::vector<gbo_qat4> itra(g->num_itra > 0 ? g->num_itra : 1);
+    if (g->num_itra > 0 && g->itra) std::memcpy(itra.data(), g->itra, sizeof(gbo_qat4) * g->num_itra);
+    TRY(upload(e->itra, itra.data(), itra.size(), e->stream));
+    TRY(upload(e->optical, g->optical, (size_t)g->num_bnd * 4, e->stream));
+    e->bnd_nx = g->bnd_nx;
+    e->bnd_ny = g->num_bnd * 8;
+    e->nm0 = g->bnd_domain_low;
+    e->nms = g->bnd_domain_step;
+    e->hd_factor = g->hd_factor;
+    TRY(make_texture(&e->bnd_array, &e->bnd_tex, g->bnd, e->bnd_nx, e->bnd_ny, true));
+    TRY(make_texture(&e->icdf_array, &e->icdf_tex, g->icdf, g->icdf_nx, g->icdf_ny, false));
+    TRY(e->counters.ensure(4));
+    if (cudaStreamSynchronize(e->stream) != cudaSuccess) {
+        gbo_engine_destroy(e);
+        return fail(GBO_ERR_CUDA, "geometry upload failed");
+    }
+#undef TRY
+    *out = e;
+    return GBO_OK;
+}
+
+static Params make_params(gbo_engine* e)
+{
+    Params P;
+    std::memset(&P, 0, sizeof(P));
+    P.acc.tlas = e->tlas.ptr;
+    P.acc.tlas_index = e->tlas_index.ptr;
+    P.acc.inst = e->inst.ptr;
+    P.acc.prim = e->prim.ptr;
+    P.acc.solid = e->solid.ptr;
+    P.acc.node = e->node.ptr;
+    P.acc.plan = e->plan.ptr;
+    P.acc.itra = e->itra.ptr;
+    P.tab.bnd_tex = e->bnd_tex;
+    P.tab.bnd_nx = (float)e->bnd_nx;
+    P.tab.bnd_ny = (float)e->bnd_ny;
+    P.tab.nm0 = e->nm0;
+    P.tab.nms = e->nms;
+    P.tab.optical = e->optical.ptr;
+    P.tab.icdf_tex = e->icdf_tex;
+    P.tab.hd_factor = e->hd_factor;
+    P.tab.debug_tag = e->cfg.debug_tag;
+    P.max_bounce = e->cfg.max_bounce;
+    P.max_time = e->cfg.max_time;
+    P.tmin = e->cfg.propagate_epsilon;
+    P.tmin0 = e->cfg.propagate_epsilon0;
+    P.tmax = e->cfg.tmax;
+    P.eps0_mask = e->cfg.epsilon0_mask;
+    P.hitmask = e->cfg.hit_mask;
+    P.seed = e->cfg.rng_seed;
+    return P;
+}
+
+// runs one event whose gensteps (and input photons) are already in e->gs / e->input on the device
+static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int64_t num_gs,
+                     const gbo_sphoton* d_input, int64_t num_input, long long num_photon, cudaStream_t s)
+{
+    const bool keep_photon = e->cfg.record_photon != 0;
+    const bool keep_seq = e->cfg.record_seq != 0;
+    int rc;
+    if (e->cfg.max_photon > 0 && num_photon > e->cfg.max_photon)
+        return fail(GBO_ERR_CAPACITY, "event of %lld photons above max_photon %lld", num_photon, (long long)e->cfg.max_photon);
+    if (num_input > 0 && num_input < num_photon)
+        return fail(GBO_ERR_ARG, "%lld input photons for %lld photon slots", (long long)num_input, num_photon);
+    const long long words = (num_photon + 31) / 32;
+    const long long nblk = (words + SCAN_WORDS - 1) / SCAN_WORDS;
+    if ((rc = e->bitmap.ensure(words))) return rc;
+    if ((rc = e->word_prefix.ensure(words))) return rc;
+    if ((rc = e->block_sum.ensure(nblk))) return rc;
+    if ((rc = e->block_offset.ensure(nblk))) return rc;
+    if ((rc = e->hits.ensure(num_photon))) return rc;
+    if (keep_photon) { if ((rc = e->photon.ensure(num_photon))) return rc; }
+    else { if ((rc = e->hits_unordered.ensure(num_photon))) return rc; }
+    if (keep_seq) { if ((rc = e->seq.ensure(num_photon))) return rc; }
+
+    Params P = make_params(e);
+    const uint64_t skip = e->cfg.event_skipahead * (uint64_t)(event_id < 0 ? 0 : event_id);
+    P.position0 = e->cfg.rng_offset + skip;
+    P.gs = reinterpret_cast<const float4*>(d_gs);
+    P.gs_end = e->gs_end.ptr;
+    P.num_gs = (int)num_gs;
+    P.num_photon = num_photon;
+    P.photon_offset = 0;
+    P.input_photon = d_input;
+    P.photon_out = keep_photon ? e->photon.ptr : nullptr;
+    P.seq_out = keep_seq ? e->seq.ptr : nullptr;
+    P.hit_unordered = keep_photon ? nullptr : e->hits_unordered.ptr;
+    P.hit_count = e->counters.ptr;
+    P.bitmap = e->bitmap.ptr;
+
+    CU(cudaMemsetAsync(e->counters.ptr, 0, 4 * sizeof(unsigned long long), s));
+    int launches = 1;
+    CU(cudaEventRecord(e->ev[1], s));
+    if (num_photon > 0) {
+        const long long blocks = (num_photon + SIM_BLOCK - 1) / SIM_BLOCK;
+        if (e->has_tree) k_simulate<true><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
+        else k_simulate<false><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
+        CU(cudaGetLastError());
+        launches++;
+    }
+    CU(cudaEventRecord(e->ev[2], s));
+    if (num_photon > 0) {
+        k_word_prefix<<<(unsigned)nblk, SCAN_WORDS, 0, s>>>(e->bitmap.ptr, words, e->word_prefix.ptr, e->block_sum.ptr);
+        k_block_offsets<<<1, 1024, 0, s>>>(e->block_sum.ptr, nblk, e->block_offset.ptr, e->counters.ptr + 1);
+        launches += 2;
+        if (keep_photon) {
+            const long long threads = words * 32;
+            k_gather_photons<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(e->photon.ptr, e->bitmap.ptr, e->word_prefix.ptr,
+                                                                                e->block_offset.ptr, words, e->hits.ptr);
+        } else {
+            // the unordered count is only known on the device: launch for the worst case and let threads exit
+            k_gather_unordered<<<(unsigned)((num_photon + 255) / 256), 256, 0, s>>>(
+                e->hits_unordered.ptr, e->counters.ptr, 0ull, e->bitmap.ptr, e->word_prefix.ptr, e->block_offset.ptr, e->hits.ptr);
+        }
+        launches++;
+        CU(cudaGetLastError());
+    }
+    CU(cudaEventRecord(e->ev[3], s));
+    CU(cudaMemcpyAsync(e->host_counters, e->counters.ptr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    e->num_photon = num_photon;
+    e->num_hit = (long long)e->host_counters[1];
+    e->event_id = event_id;
+    e->stats.num_photon = num_photon;
+    e->stats.num_hit = e->num_hit;
+    e->stats.simulate_launches = num_photon > 0 ? 1 : 0;
+    e->stats.kernel_launches = launches;
+    cudaEventElapsedTime(&e->stats.ms_upload, e->ev[0], e->ev[1]);
+    cudaEventElapsedTime(&e->stats.ms_simulate, e->ev[1], e->ev[2]);
+    cudaEventElapsedTime(&e->stats.ms_compact, e->ev[2], e->ev[3]);
+    return GBO_OK;
+}
+
+int gbo_simulate(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs, const gbo_sphoton* input_photon,
+                 int64_t num_input_photon)
+{
+    if (!e) return fail(GBO_ERR_ARG, "gbo_simulate: null engine");
+    if (num_gs < 0 || (num_gs > 0 && !gs)) return fail(GBO_ERR_ARG, "gbo_simulate: bad gensteps");
+    if (num_gs > 0x7fffffff) return fail(GBO_ERR_CAPACITY, "gbo_simulate: %lld gensteps", (long long)num_gs);
+    if (num_input_photon < 0 || (num_input_photon > 0 && !input_photon)) return fail(GBO_ERR_ARG, "gbo_simulate: bad input photons");
+    CU(cudaSetDevice(e->device));
+    std::vector<unsigned long long> end((size_t)num_gs);
+    unsigned long long total = 0;
+    bool has_input_gs = false;
+    for (int64_t i = 0; i < num_gs; i++) {
+        total += gs[i].q[0].u[3];
+        end[(size_t)i] = total;
+        if (gs[i].q[0].i[0] == GBO_GS_INPUT_PHOTON) has_input_gs = true;
+    }
+    if (has_input_gs && (long long)num_input_photon < (long long)total)
+        return fail(GBO_ERR_ARG, "gbo_simulate: INPUT_PHOTON gensteps need %llu photons, %lld given", total,
+                    (long long)num_input_photon);
+    cudaStream_t s = e->stream;
+    CU(cudaEventRecord(e->ev[0], s));
+    int rc;
+    if ((rc = upload(e->gs, gs, (size_t)num_gs, s))) return rc;
+    if ((rc = upload(e->gs_end, end.data(), end.size(), s))) return rc;
+    if (num_input_photon > 0) { if ((rc = upload(e->input, input_photon, (size_t)num_input_photon, s))) return rc; }
+    return run_event(e, event_id, e->gs.ptr, num_gs, num_input_photon > 0 ? e->input.ptr : nullptr, num_input_photon,
+                     (long long)total, s);
+}
+
+int gbo_simulate_device(gbo_engine* e, int32_t event_id, const void* d_gs, int64_t num_gs, const void* d_input,
+                        int64_t num_input, void* stream)
+{
+    if (!e) return fail(GBO_ERR_ARG, "gbo_simulate_device: null engine");
+    if (num_gs < 0 || (num_gs > 0 && !d_gs)) return fail(GBO_ERR_ARG, "gbo_simulate_device: bad gensteps");
+    if (num_gs > 0x7fffffff) return fail(GBO_ERR_CAPACITY, "gbo_simulate_device: %lld gensteps", (long long)num_gs);
+    CU(cudaSetDevice(e->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+    int rc;
+    if ((rc = e->gs_end.ensure((size_t)(num_gs > 0 ? num_gs : 1)))) return rc;
+    CU(cudaEventRecord(e->ev[0], s));
+    unsigned long long total = 0;
+    if (num_gs > 0) {
+        k_genstep_prefix<<<1, 1024, 0, s>>>((const gbo_quad6*)d_gs, (int)num_gs, e->gs_end.ptr);
+        CU(cudaGetLastError());
+        CU(cudaMemcpyAsync(e->host_counters + 3, e->gs_end.ptr + (num_gs - 1), sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        total = e->host_counters[3];
+    }
+    return run_event(e, event_id, (const gbo_quad6*)d_gs, num_gs, (const gbo_sphoton*)d_input, num_input,
+                     (long long)total, s);
+}
+
+int64_t gbo_num_hit(const gbo_engine* e) { return e && e->num_photon >= 0 ? e->num_hit : -1; }
+int64_t gbo_num_photon(const gbo_engine* e) { return e ? e->num_photon : -1; }
+const void* gbo_device_hits(const gbo_engine* e) { return e ? e->hits.ptr : nullptr; }
+
+int gbo_copy_hits(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64_t count)
+{
+    if (!e || (!dst && count > 0)) return fail(GBO_ERR_ARG, "gbo_copy_hits: null argument");
+    if (e->num_photon < 0) return fail(GBO_ERR_STATE, "gbo_copy_hits: no event simulated");
+    if (offset < 0 || count < 0 || offset + count > e->num_hit)
+        return fail(GBO_ERR_ARG, "gbo_copy_hits: range [%lld,+%lld) outside %lld hits", (long long)offset, (long long)count, e->num_hit);
+    if (count == 0) return GBO_OK;
+    CU(cudaSetDevice(e->device));
+    CU(cudaMemcpyAsync(dst, e->hits.ptr + offset, (size_t)count * sizeof(gbo_sphoton), cudaMemcpyDeviceToHost, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+    return GBO_OK;
+}
+
+int gbo_copy_photons(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64_t count)
+{
+    if (!e || (!dst && count > 0)) return fail(GBO_ERR_ARG, "gbo_copy_photons: null argument");
+    if (!e->cfg.record_photon) return fail(GBO_ERR_STATE, "gbo_copy_photons: record_photon is off");
+    if (e->num_photon < 0) return fail(GBO_ERR_STATE, "gbo_copy_photons: no event simulated");
+    if (offset < 0 || count < 0 || offset + count > e->num_photon) return fail(GBO_ERR_ARG, "gbo_copy_photons: range outside event");
+    if (count == 0) return GBO_OK;
+    CU(cudaSetDevice(e->device));
+    CU(cudaMemcpyAsync(dst, e->photon.ptr + offset, (size_t)count * sizeof(gbo_sphoton), cudaMemcpyDeviceToHost, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+    return GBO_OK;
+}
+
+int gbo_copy_seq(gbo_engine* e, gbo_seq* dst, int64_t offset, int64_t count)
+{
+    if (!e || (!dst && count > 0)) return fail(GBO_ERR_ARG, "gbo_copy_seq: null argument");
+    if (!e->cfg.record_seq) return fail(GBO_ERR_STATE, "gbo_copy_seq: record_seq is off");
+    if (e->num_photon < 0) return fail(GBO_ERR_STATE, "gbo_copy_seq: no event simulated");
+    if (offset < 0 || count < 0 || offset + count > e->num_photon) return fail(GBO_ERR_ARG, "gbo_copy_seq: range outside event");
+    if (count == 0) return GBO_OK;
+    CU(cudaSetDevice(e->device));
+    CU(cudaMemcpyAsync(dst, e->seq.ptr + offset, (size_t)count * sizeof(gbo_seq), cudaMemcpyDeviceToHost, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+    return GBO_OK;
+}
+
+int gbo_reset(gbo_engine* e, int32_t event_id)
+{
+    if (!e) return fail(GBO_ERR_ARG, "gbo_reset: null engine");
+    (void)event_id;
+    e->num_photon = -1;
+    e->num_hit = 0;
+    e->event_id = -1;
+    return GBO_OK;
+}
+
+int gbo_get_stats(const gbo_engine* e, gbo_stats* out)
+{
+    if (!e || !out) return fail(GBO_ERR_ARG, "gbo_get_stats: null argument");
+    *out = e->stats;
+    return GBO_OK;
+}
+
+}  // extern "C"
+
+// ---- known-answer entry points ---------------------------------------------------------------------------------
+
+namespace {
+template <typename F>
+int with_scratch(size_t in_bytes, const void* in, size_t out_bytes, void* out, F launch)
+{
+    void* d_in = nullptr;
+    void* d_out = nullptr;
+    if (in_bytes && cudaMalloc(&d_in, in_bytes) != cudaSuccess) return fail(GBO_ERR_CUDA, "cudaMalloc failed");
+    if (cudaMalloc(&d_out, out_bytes) != cudaSuccess) { cudaFree(d_in); return fail(GBO_ERR_CUDA, "cudaMalloc failed"); }
+    int rc = GBO_OK;
+    if (in_bytes && cudaMemcpy(d_in, in, in_bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(GBO_ERR_CUDA, "upload failed");
+    if (!rc) {
+        launch(d_in, d_out);
+        cudaError_t err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaDeviceSynchronize();
+        if (err != cudaSuccess) rc = fail(GBO_ERR_CUDA, "kernel failed: %s", cudaGetErrorString(err));
+    }
+    if (!rc && cudaMemcpy(out, d_out, out_bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = fail(GBO_ERR_CUDA, "download failed");
+    cudaFree(d_in);
+    cudaFree(d_out);
+    return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int gbo_rng_sequence(int device, uint64_t seed, uint64_t subsequence0, uint64_t position, int32_t num_seq,
+                     int32_t per_seq, float* out)
+{
+    if (!out || num_seq <= 0 || per_seq <= 0) return fail(GBO_ERR_ARG, "gbo_rng_sequence: bad arguments");
+    CU(cudaSetDevice(device));
+    return with_scratch(0, nullptr, (size_t)num_seq * per_seq * sizeof(float), out, [&](void*, void* d_out) {
+        k_rng_sequence<<<(num_seq + 127) / 128, 128>>>(seed, subsequence0, position, num_seq, per_seq, (float*)d_out);
+    });
+}
+
+int gbo_texture_lookup(gbo_engine* e, int32_t which, const float* xy, int32_t n, float* out)
+{
+    if (!e || !xy || !out || n <= 0 || (which != 0 && which != 1)) return fail(GBO_ERR_ARG, "gbo_texture_lookup: bad arguments");
+    CU(cudaSetDevice(e->device));
+    Params P = make_params(e);
+    return with_scratch((size_t)n * sizeof(float2), xy, (size_t)n * sizeof(float4), out, [&](void* d_in, void* d_out) {
+        k_tex_lookup<<<(n + 127) / 128, 128>>>(P.tab, (const float2*)d_in, n, which, (float4*)d_out);
+    });
+}
+
+int gbo_scint_wavelength(gbo_engine* e, const float* u, int32_t n, float* out)
+{
+    if (!e || !u || !out || n <= 0) return fail(GBO_ERR_ARG, "gbo_scint_wavelength: bad arguments");
+    CU(cudaSetDevice(e->device));
+    Params P = make_params(e);
+    return with_scratch((size_t)n * sizeof(float), u, (size_t)n * sizeof(float), out, [&](void* d_in, void* d_out) {
+        k_scint_wavelength<<<(n + 127) / 128, 128>>>(P.tab, (const float*)d_in, n, (float*)d_out);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+/*
+ * gbopticks.h : C ABI of the GB300 optical-photon engine (libgbopticks.so).
+ *
+ * Plain pointers and sizes only.  Every entry point returns GBO_OK (0) or an error code; the message of the
+ * calling thread's last error is available from gbo_last_error().  Array layouts are those of gbo_types.h,
+ * i.e. the reference's own genstep / photon / CSGFoundry layouts.
+ *
+ * Reference interface each entry point stands in for:
+ *
+ *   gbo_config_default   SEventConfig defaults + OPTICKS_* environment (sysrap/SEventConfig.cc:37-115,
+ *                        keys sysrap/SEventConfig.hh:218-283)
+ *   gbo_engine_create    G4CXOpticks::SetGeometry(const G4VPhysicalVolume*) (g4cx/G4CXOpticks.hh:49,
+ *                        g4cx/G4CXOpticks.cc:79-84, 315-346): geometry + optical tables uploaded once; the caller
+ *                        has already translated the Geant4 tree into CSGFoundry arrays (CSG/CSGFoundry.cc:2782-2788)
+ *   gbo_simulate         G4CXOpticks::simulate(int eventID, bool reset=false) (g4cx/G4CXOpticks.hh:95,
+ *                        .cc:466-486) with gensteps that SEvt::AddGenstep collected (sysrap/SEvt.hh:487) and the
+ *                        input photons of SEvt::SetInputPhoton; synchronous, hits gathered when it returns
+ *   gbo_num_hit          SEvt::GetNumHit(0) (sysrap/SEvt.cc:2050)
+ *   gbo_copy_hits        SEvt::getHit(sphoton&, unsigned idx) (sysrap/SEvt.cc:4991), in bulk
+ *   gbo_reset            G4CXOpticks::reset(int eventID) (g4cx/G4CXOpticks.hh:96, .cc:499-518)
+ *   gbo_copy_photons     the full photon array of a debug event mode (QEvt::gatherPhoton)
+ *   gbo_copy_seq         the seqhis/seqbnd arrays of a debug event mode (sysrap/sseq.h)
+ *   gbo_simulate_device  QSim::simulate on gensteps already resident in device memory (qudarap/QSim.cc:428-631)
+ *   gbo_engine_destroy   G4CXOpticks::Finalize
+ */
+#ifndef GBOPTICKS_H
+#define GBOPTICKS_H
+
+#include <stdint.h>
+#include "gbo_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    GBO_OK = 0,
+    GBO_ERR_ARG = 1,        /* bad argument (null pointer, size out of range, malformed geometry) */
+    GBO_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+    GBO_ERR_STATE = 3,      /* call out of order (e.g. hits requested before any simulate) */
+    GBO_ERR_CAPACITY = 4,   /* request above a configured or fixed limit */
+    GBO_ERR_DEVICE = 5      /* a kernel reported an error through its status word */
+};
+
+typedef struct gbo_engine gbo_engine;
+
+typedef struct gbo_geometry_desc {
+    const gbo_csgnode*  node;    int32_t num_node;
+    const gbo_csgprim*  prim;    int32_t num_prim;
+    const gbo_csgsolid* solid;   int32_t num_solid;
+    const gbo_qat4*     inst;    int32_t num_inst;     /* forward transforms, identity ints in .w column */
+    const gbo_qat4*     itra;    int32_t num_itra;     /* inverse node transforms (1-based gtransformIdx) */
+    const float*        plan;    int32_t num_plan;     /* float4 planes */
+    const float*        bnd;     int32_t num_bnd;      /* (num_bnd, 4, 2, bnd_nx, 4) boundary payload */
+    int32_t             bnd_nx;                        /* wavelength samples (761) */
+    float               bnd_domain_low;                /* nm (60) */
+    float               bnd_domain_step;               /* nm (1) */
+    const uint32_t*     optical;                       /* (num_bnd*4, 4) */
+    const float*        icdf;                          /* (icdf_ny, icdf_nx) scintillation inverse CDF */
+    int32_t             icdf_ny, icdf_nx, hd_factor;
+} gbo_geometry_desc;
+
+typedef struct gbo_config {
+    int32_t  max_bounce;            /* OPTICKS_MAX_BOUNCE        31    */
+    float    max_time;              /* OPTICKS_MAX_TIME          1e27 ns */
+    float    propagate_epsilon;     /* OPTICKS_PROPAGATE_EPSILON 0.05 mm */
+    float    propagate_epsilon0;    /* OPTICKS_PROPAGATE_EPSILON0 0.05 mm */
+    uint32_t epsilon0_mask;         /* OPTICKS_PROPAGATE_EPSILON0_MASK TO,CK,SI,SC,RE */
+    uint32_t hit_mask;              /* OPTICKS_HIT_MASK          SD    */
+    uint64_t rng_seed;              /* QRng__SEED_OFFSET seed    0     */
+    uint64_t rng_offset;            /* QRng__SEED_OFFSET offset  0     */
+    uint64_t event_skipahead;       /* OPTICKS_EVENT_SKIPAHEAD   100000 */
+    float    tmax;                  /* trace limit               1e6 mm */
+    int32_t  debug_tag;             /* 1: draw order of the reference's OptiX build (alignment burns), 0: PRODUCTION */
+    int32_t  record_photon;         /* keep the full photon array of each event */
+    int32_t  record_seq;            /* keep seqhis/seqbnd of each event */
+    int64_t  max_photon;            /* capacity limit per event (0: no limit beyond device memory) */
+} gbo_config;
+
+typedef struct gbo_stats {
+    int64_t num_photon;
+    int64_t num_hit;
+    float   ms_upload;              /* host->device copies of gensteps / input photons */
+    float   ms_simulate;            /* simulate kernel */
+    float   ms_compact;             /* hit scan + gather */
+    int32_t simulate_launches;
+    int32_t kernel_launches;        /* all engine kernels of the last event */
+} gbo_stats;
+
+int         gbo_config_default(gbo_config* cfg);
+int         gbo_engine_create(const gbo_geometry_desc* geom, const gbo_config* cfg, int device, gbo_engine** out);
+void        gbo_engine_destroy(gbo_engine* e);
+int         gbo_simulate(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs,
+                         const gbo_sphoton* input_photon, int64_t num_input_photon);
+int         gbo_simulate_device(gbo_engine* e, int32_t event_id, const void* d_gs, int64_t num_gs,
+                                const void* d_input_photon, int64_t num_input_photon, void* cuda_stream);
+int64_t     gbo_num_hit(const gbo_engine* e);
+int64_t     gbo_num_photon(const gbo_engine* e);
+int         gbo_copy_hits(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64_t count);
+int         gbo_copy_photons(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64_t count);
+int         gbo_copy_seq(gbo_engine* e, gbo_seq* dst, int64_t offset, int64_t count);
+const void* gbo_device_hits(const gbo_engine* e);
+int         gbo_reset(gbo_engine* e, int32_t event_id);
+int         gbo_get_stats(const gbo_engine* e, gbo_stats* out);
+const char* gbo_last_error(void);
+
+/* Known-answer entry points; the reference drives equivalent test kernels from QSimTest (qudarap/QSim.cu,
+ * qudarap/tests/QSimTest.cc:700-770):
+ *   gbo_rng_sequence      QSim::rng_sequence : num_seq consecutive subsequences from subsequence0, per_seq
+ *                         uniforms each, starting at stream position (offset + skipahead) `position`
+ *   gbo_texture_lookup    QBnd / QScint texture lookups at normalized (x,y) pairs; which 0: boundary texture
+ *                         (float4 out), 1: scintillation ICDF (value in .x of each float4 out)
+ *   gbo_scint_wavelength  qscint::wavelength (hd_factor layers) for each uniform u */
+int         gbo_rng_sequence(int device, uint64_t seed, uint64_t subsequence0, uint64_t position, int32_t num_seq,
+                             int32_t per_seq, float* out);
+int         gbo_texture_lookup(gbo_engine* e, int32_t which, const float* xy, int32_t n, float* out);
+int         gbo_scint_wavelength(gbo_engine* e, const float* u, int32_t n, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBOPTICKS_H */

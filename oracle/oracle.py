@@ -90,11 +90,11 @@ class SimConfig:
 
 
 def invert_instances(inst):
-    m = inst.astype(np.float64).copy()
-    m[:, :, 3] = (0, 0, 0, 1)
-    inv = np.linalg.inv(m)
-    inv[:, :, 3] = (0, 0, 0, 1)
-    return inv.astype(np.float32)
+    """Inverse instance transforms with the same double-precision adjugate formula the engine uses."""
+    inst = np.ascontiguousarray(inst, dtype=np.float32)
+    out = np.zeros_like(inst)
+    lib().orc_invert_transforms(_ptr(inst), _ptr(out), C.c_int(len(inst)))
+    return out
 
 
 class _Lib:

@@ -1,0 +1,60 @@
+"""The C-ABI library loads without a GPU and exports every entry point include/*.h declares."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(gbo_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__ as ge
+    ge.load_package()
+    from eic_opticks_gb300 import build
+    path = build.build()
+    return ctypes.CDLL(path)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for must in ("gbo_engine_create", "gbo_simulate", "gbo_num_hit", "gbo_copy_hits", "gbo_reset"):
+        assert must in syms
+
+
+def test_library_exports_declared_symbols(lib):
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_config_default_without_gpu(lib, monkeypatch):
+    from eic_opticks_gb300 import engine as E
+    monkeypatch.setenv("OPTICKS_MAX_BOUNCE", "9")
+    monkeypatch.setenv("OPTICKS_HIT_MASK", "SD,EC")
+    c = E.Config()
+    assert lib.gbo_config_default(ctypes.byref(c)) == 0
+    assert c.max_bounce == 9
+    assert c.hit_mask == (1 << 6) | (1 << 13)
+    assert abs(c.propagate_epsilon - 0.05) < 1e-9 and c.event_skipahead == 100000 and c.debug_tag == 1
+
+
+def test_engine_create_rejects_bad_geometry(lib):
+    from eic_opticks_gb300 import engine as E
+    d = E.GeometryDesc()
+    h = ctypes.c_void_p()
+    lib.gbo_last_error.restype = ctypes.c_char_p
+    rc = lib.gbo_engine_create(ctypes.byref(d), None, 0, ctypes.byref(h))
+    assert rc == 1 and b"missing" in lib.gbo_last_error()
