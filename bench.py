@@ -1,0 +1,295 @@
+"""Benchmark: propagated photons/s of the GB300 engine on the scintillating crystal-array workload.
+
+Workload (one step = one event): the 8x8 CsI crystal array, 2,000 scintillation gensteps with Poisson(5000)
+photons each (~10M photons), Gaussian 550+-50 nm emission through the 3x4096 hd_factor-20 inverse CDF,
+1000 ns decay, reference physics defaults (max_bounce 31, epsilon 0.05 mm, hit mask SD), synthetic gensteps
+from seeded numpy generators (Geant4 is not part of the path).
+
+* ``value``  photons/s with the gensteps already resident in device memory (gbo_simulate_device), timed with
+  CUDA events around each event; L2 is flushed (256 MB write) between timed events.
+* ``e2e``    photons/s through the reference-facing C ABI (gbo_simulate with host gensteps, then gbo_copy_hits
+  into pinned host memory), host<->device copies inside the timed region.
+* ``roofline`` the simulate kernel's algorithmic HBM bytes per photon (genstep share + 4 B seed + 64 B photon
+  write + 64 B compaction read + 64 B x hit fraction, the reference's traffic for the same event) over its
+  CUDA-event time, against the measured copy bandwidth.
+* ``cpu_baseline`` the CPU oracle (the reference's algorithm restated in C, pthreads over all host cores) on a
+  bounded sample of the same event.
+
+``--impl reference`` times the reference's CPU implementation of the path instead (oracle/_ref when it was
+built from the reference's own headers on this host, else the oracle port), on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as ge  # noqa: E402
+
+METRIC = "propagated photons/s, batched vs plain per-event launch on 1 GB300; p99 latency"
+UNIT = "photons/s"
+WORKLOAD = "crystal_array_8x8_CsI_scint_2000gs_poisson5000"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return float(m["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def workload(seed=1, num_gs=2000):
+    ge.load_package()
+    from eic_opticks_gb300 import geometry as G, gensteps as GS
+    geom = G.crystal_array().arrays()
+    gs = GS.crystal_scint_gensteps(num_gs, 5000, seed=seed)
+    return geom, gs
+
+
+def cpu_baseline(geom, gs, target_s=12.0, threads=None):
+    """The oracle on a bounded sample (first gensteps of the event) using all host cores."""
+    O = ge.load_oracle()
+    O.build()
+    cfg = O.SimConfig(geom)
+    threads = threads or os.cpu_count() or 1
+    n_gs = 4
+    while True:
+        sample = gs[:n_gs]
+        t0 = time.perf_counter()
+        out, _ = O.simulate(cfg, sample, nthreads=threads, seq=False)
+        dt = time.perf_counter() - t0
+        if dt > target_s / 4 or n_gs >= len(gs):
+            break
+        n_gs = min(len(gs), max(n_gs + 1, int(n_gs * target_s / 4 / max(dt, 1e-3))))
+    n = len(out)
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of %d gensteps (%d photons), %.1f s" % (n_gs, len(gs), n, dt)}
+
+
+def reference_arm(args):
+    """--impl reference : the reference's CPU implementation of the path on the host cores."""
+    geom, gs = workload()
+    O = ge.load_oracle()
+    O.build()
+    use_ref = O.reflib() is not None
+    kind = "reference" if use_ref else "port"
+    cfg = O.SimConfig(geom)
+    threads = os.cpu_count() or 1
+    sample_gs = 2
+    times, photons = [], 0
+    for step in range(args.warmup + args.steps):
+        sample = gs[step * sample_gs % len(gs):][:sample_gs]
+        t0 = time.perf_counter()
+        if use_ref:
+            out, _ = O.simulate(cfg, sample, seq=False, use_ref=True)          # single-threaded driver
+        else:
+            out, _ = O.simulate(cfg, sample, nthreads=threads, seq=False)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+            photons += len(out)
+    total = sum(times)
+    value = photons / total
+    cores = 1 if use_ref else threads
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / max(1, len(times)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample_gensteps_per_step": sample_gs},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": "%d gensteps per step (~%d photons)" % (sample_gs, photons // max(1, len(times)))},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    return dist, dist.get_rank(), ws
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--gensteps", type=int, default=2000, help="gensteps per event (2000 is the benchmark workload)")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        if rank == 0:
+            reference_arm(args)
+        return
+
+    dist, rank, world = dist_init(args)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    torch.cuda.set_device(local)
+    if rank == 0:
+        ge.build()
+    if dist:
+        dist.barrier()
+    ge.load_package()
+    from eic_opticks_gb300 import engine as E
+    geom, gs = workload(seed=1 + rank, num_gs=args.gensteps)
+    n_photon = int(gs.view(np.uint32)[:, 0, 3].astype(np.int64).sum())
+    eng = E.Engine(geom, device=local)
+
+    d_gs = torch.from_numpy(gs.copy()).to(f"cuda:{local}")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    # ---- device-resident throughput (value) ----
+    for w in range(args.warmup):
+        eng.simulate_device(w, d_gs.data_ptr(), len(gs))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms, sim_ms, launches, hits = [], [], 0, 0
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            start.record()
+            hits = eng.simulate_device(1000 + k, d_gs.data_ptr(), len(gs))
+            end.record()
+            end.synchronize()
+            ms.append(start.elapsed_time(end))
+            st = eng.stats()
+            sim_ms.append(st["ms_simulate"])
+            launches += st["kernel_launches"]
+    torch.cuda.synchronize()
+    total_ms = sum(ms)
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t[0])
+    value = world * n_photon * args.steps / (total_ms * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers (e2e) ----
+    hits_host = None
+    e2e_ms = []
+    h2d = gs.nbytes
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nh = eng.simulate(2000 + k, gs)
+        if hits_host is None or len(hits_host) < nh:
+            hits_host = np.zeros(max(nh, 1) * 2, dtype=E.L.PHOTON)
+        eng.hits(out=hits_host[:nh])
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            e2e_ms.append(dt * 1e3)
+    d2h = nh * 64 + 32      # ordered hits + the counters read that sizes them
+    e2e_total = sum(e2e_ms)
+    if dist:
+        t = torch.tensor([e2e_total], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t[0])
+    e2e_value = world * n_photon * args.steps / (e2e_total * 1e-3)
+
+    if rank != 0:
+        if dist:
+            dist.barrier()
+        return
+
+    hbm, peak_kind = peaks()
+    f_hit = hits / n_photon
+    b_alg = 96.0 / (n_photon / len(gs)) + 4 + 64 + 64 + 64 * f_hit
+    sim_mean = float(np.mean(sim_ms))
+    achieved = b_alg * n_photon / (sim_mean * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded numpy gensteps with the reference genstep layout)",
+        "config": {"workload": WORKLOAD if args.gensteps == 2000 else WORKLOAD + "_%dgs" % args.gensteps, "photons_per_step": n_photon, "gensteps_per_step": len(gs),
+                   "hits_per_step": hits, "path": "plain: one event per launch", "l2": "flushed (256 MB write) between timed steps",
+                   "max_bounce": 31, "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "kernel": "k_simulate", "bytes_per_photon": b_alg,
+                     "kernel_ms": sim_mean, "peak_source": peak_kind},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(geom, gs)
+    print(json.dumps(line))
+    if dist:
+        dist.barrier()
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -571,7 +571,8 @@ static Params make_params(gbo_engine* e)
 
 // runs one event whose gensteps (and input photons) are already in e->gs / e->input on the device
 static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int64_t num_gs,
-                     const gbo_sphoton* d_input, int64_t num_input, long long num_photon, cudaStream_t s)
+                     const gbo_sphoton* d_input, int64_t num_input, long long num_photon, cudaStream_t s,
+                     int prior_launches)
 {
     const bool keep_photon = e->cfg.record_photon != 0;
     const bool keep_seq = e->cfg.record_seq != 0;
@@ -607,7 +608,7 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     P.bitmap = e->bitmap.ptr;
 
     CU(cudaMemsetAsync(e->counters.ptr, 0, 4 * sizeof(unsigned long long), s));
-    int launches = 1;
+    int launches = prior_launches;
     CU(cudaEventRecord(e->ev[1], s));
     if (num_photon > 0) {
         const long long blocks = (num_photon + SIM_BLOCK - 1) / SIM_BLOCK;
@@ -675,7 +676,7 @@ int gbo_simulate(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
     if ((rc = upload(e->gs_end, end.data(), end.size(), s))) return rc;
     if (num_input_photon > 0) { if ((rc = upload(e->input, input_photon, (size_t)num_input_photon, s))) return rc; }
     return run_event(e, event_id, e->gs.ptr, num_gs, num_input_photon > 0 ? e->input.ptr : nullptr, num_input_photon,
-                     (long long)total, s);
+                     (long long)total, s, 0);
 }
 
 int gbo_simulate_device(gbo_engine* e, int32_t event_id, const void* d_gs, int64_t num_gs, const void* d_input,
@@ -699,7 +700,7 @@ int gbo_simulate_device(gbo_engine* e, int32_t event_id, const void* d_gs, int64
         total = e->host_counters[3];
     }
     return run_event(e, event_id, (const gbo_quad6*)d_gs, num_gs, (const gbo_sphoton*)d_input, num_input,
-                     (long long)total, s);
+                     (long long)total, s, num_gs > 0 ? 1 : 0);
 }
 
 int64_t gbo_num_hit(const gbo_engine* e) { return e && e->num_photon >= 0 ? e->num_hit : -1; }

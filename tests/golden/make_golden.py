@@ -105,7 +105,7 @@ def sims():
     gst = np.concatenate([GS.torch_gensteps(1, 60, torch_type=t, pos=(0, 0, 0), radius=30.0)
                           for t in (L.T_DISC, L.T_SPHERE, L.T_SPHERE_MARSAGLIA, L.T_POINT, L.T_CIRCLE, L.T_RECTANGLE)])
     sim_case("torch", G.nested_boxes(), gst)
-    ls = G.large_sphere(num_sensors=2000, sphere_radius=1770.0, sensor_radius=1940.0, shell=12.0)
+    ls = G.large_sphere(num_sensors=150, sphere_radius=1770.0, sensor_radius=1940.0, shell=12.0)
     sim_case("large_sphere_small", ls, GS.sphere_scint_gensteps(10, 100, seed=11, radius=1700.0))
 
 

