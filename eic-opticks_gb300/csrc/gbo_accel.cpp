@@ -224,6 +224,33 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
     out.tlas.reserve(2 * num_inst);
     b.build(0, num_inst, 0);
     out.max_depth = b.max_depth;
+
+    // two-child-box form: node k of tlas2 corresponds to inner node map[k] of tlas
+    const std::vector<BvhNode>& t = out.tlas;
+    std::vector<int> inner_id(t.size(), -1);
+    std::vector<int> order;
+    for (size_t i = 0; i < t.size(); i++)
+        if (t[i].count == 0) { inner_id[i] = (int)order.size(); order.push_back((int)i); }
+    auto child = [&](int ci, float* lo, float* hi, int32_t& first, int32_t& count) {
+        for (int k = 0; k < 3; k++) { lo[k] = t[ci].bmin[k]; hi[k] = t[ci].bmax[k]; }
+        if (t[ci].count > 0) { first = t[ci].left_first; count = t[ci].count; }
+        else { first = inner_id[ci]; count = 0; }
+    };
+    if (order.empty()) {            // root is a leaf: one node whose second child is empty
+        BvhNode2 n{};
+        child(0, n.lo0, n.hi0, n.first0, n.count0);
+        for (int k = 0; k < 3; k++) { n.lo1[k] = 1.f; n.hi1[k] = -1.f; }
+        n.first1 = 0;
+        n.count1 = 0x7fffffff;      // never visited: empty box
+        out.tlas2.push_back(n);
+    } else {
+        for (int id : order) {
+            BvhNode2 n{};
+            child(id + 1, n.lo0, n.hi0, n.first0, n.count0);
+            child(t[id].left_first, n.lo1, n.hi1, n.first1, n.count1);
+            out.tlas2.push_back(n);
+        }
+    }
     return 0;
 }
 

@@ -24,6 +24,17 @@ struct BvhNode {
 };
 static_assert(sizeof(BvhNode) == 32, "BvhNode is 32 bytes");
 
+// Traversal node: the boxes of both children, so one 64 B load decides which children to visit and in which
+// order.  For child c, count_c > 0 marks a leaf holding tlas_index[first_c .. first_c+count_c), else first_c
+// is the inner node to visit.
+struct BvhNode2 {
+    float lo0[3]; int32_t first0;
+    float hi0[3]; int32_t count0;
+    float lo1[3]; int32_t first1;
+    float hi1[3]; int32_t count1;
+};
+static_assert(sizeof(BvhNode2) == 64, "BvhNode2 is 64 bytes");
+
 struct InstDev {
     float c0[4], c1[4], c2[4];     // columns of the inverse (object <- world) 3x4 transform: xyz rows + translation
     int32_t solid;
@@ -48,6 +59,7 @@ struct SolidDev {
 
 struct AccelHost {
     std::vector<BvhNode> tlas;
+    std::vector<BvhNode2> tlas2;         // traversal form of tlas (root is node 0; a single-leaf tree has one node)
     std::vector<int32_t> tlas_index;     // leaf ranges index into this permutation of instances
     std::vector<InstDev> inst;
     std::vector<PrimDev> prim;

@@ -92,12 +92,14 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_simulate(const __grid_constant__ 
         Seq seq;
         seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
         int bounce = 0;
+        int hint = -1;
         if (P.seq_out) seq_add(seq, 0u, flag_of(p), boundary_of(p));
         while (bounce < P.max_bounce && p.time < P.max_time) {
             const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
             Hit h;
-            trace<TREE>(P.acc, p.pos, p.mom, tmin, P.tmax, h);
+            trace<TREE>(P.acc, p.pos, p.mom, tmin, P.tmax, hint, h);
             if ((h.prim_boundary & 0xffffu) == 0xffffu) break;
+            hint = (int)(h.iindex_identity >> 16);
             h.normal = normalize(h.normal);
             const int command = propagate(P.tab, p, h, rng);
             bounce++;
@@ -121,6 +123,121 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_simulate(const __grid_constant__ 
         if (lane == 0) base = atomicAdd(P.hit_count, (unsigned long long)__popc(mask));
         base = __shfl_sync(0xffffffffu, base, 0);
         if (is_hit) store_photon(P.hit_unordered + base + __popc(mask & ((1u << lane) - 1u)), p);
+    }
+}
+
+// ---- persistent form: lanes refill from a photon pool so a warp never idles behind its longest photon --------
+
+GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng)
+{
+    int lo = 0, hi = P.num_gs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(P.gs_end + mid) > (unsigned long long)idx) hi = mid; else lo = mid + 1;
+    }
+    const float4* g = P.gs + 6 * (size_t)lo;
+    float4 gq[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) gq[k] = __ldg(g + k);
+    const unsigned long long photon_idx = P.photon_offset + (unsigned long long)idx;
+    rng_init(rng, P.seed, photon_idx, P.position0);
+    p.pos = f3(0.f, 0.f, 0.f); p.time = 0.f; p.mom = f3(0.f, 0.f, 0.f); p.hitcount_iindex = 0u;
+    p.pol = f3(0.f, 0.f, 0.f); p.wavelength = 0.f;
+    p.orient_boundary_flag = 0u; p.identity = 0u; p.index = 0u; p.flagmask = 0u;
+    const int gencode = __float_as_int(gq[0].x);
+    switch (gencode) {
+        case GBO_GS_TORCH: gen_torch(p, rng, gq, photon_idx); break;
+        case GBO_GS_CERENKOV:
+        case GBO_GS_G4Cerenkov_modified: gen_cerenkov(P.tab, p, rng, gq); break;
+        case GBO_GS_SCINTILLATION:
+        case GBO_GS_DsG4Scintillation_r4695: gen_scint(P.tab, p, rng, gq); break;
+        case GBO_GS_INPUT_PHOTON: load_photon(p, P.input_photon + idx); set_flag(p, GBO_TORCH); break;
+        default: break;
+    }
+    set_index(p, photon_idx);
+}
+
+template <bool TREE>
+__global__ void __launch_bounds__(SIM_BLOCK) k_simulate_pool(const __grid_constant__ Params P,
+                                                             unsigned long long* pool, int refill_min)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt = (1u << lane) - 1u;
+    bool live = false;
+    bool pool_open = true;
+    long long idx = -1;
+    int bounce = 0;
+    int hint = -1;
+    Photon p;
+    Rng rng;
+    Seq seq;
+    for (;;) {
+        // refill: idle lanes take consecutive photon indices with one atomic per warp
+        const unsigned idle = __ballot_sync(0xffffffffu, !live);
+        if (pool_open && __popc(idle) >= refill_min) {
+            unsigned long long base = 0;
+            const int leader = __ffs(idle) - 1;
+            if ((int)lane == leader) base = atomicAdd(pool, (unsigned long long)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base + __popc(idle) >= (unsigned long long)P.num_photon) pool_open = false;
+            if (!live) {
+                const unsigned long long mine = base + __popc(idle & lt);
+                if (mine < (unsigned long long)P.num_photon) {
+                    idx = (long long)mine;
+                    generate(P, idx, p, rng);
+                    bounce = 0;
+                    hint = -1;
+                    seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
+                    if (P.seq_out) seq_add(seq, 0u, flag_of(p), boundary_of(p));
+                    live = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, live)) {
+            if (!pool_open) break;
+            continue;
+        }
+        bool done = false;
+        if (live) {
+            if (bounce < P.max_bounce && p.time < P.max_time) {
+                const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
+                Hit h;
+                trace<TREE>(P.acc, p.pos, p.mom, tmin, P.tmax, hint, h);
+                if ((h.prim_boundary & 0xffffu) == 0xffffu) {
+                    done = true;
+                } else {
+                    hint = (int)(h.iindex_identity >> 16);
+                    h.normal = normalize(h.normal);
+                    const int command = propagate(P.tab, p, h, rng);
+                    bounce++;
+                    if (P.seq_out) seq_add(seq, (unsigned)bounce, flag_of(p), boundary_of(p));
+                    done = command == CMD_BREAK;
+                }
+            } else {
+                done = true;
+            }
+        }
+        const bool is_hit = done && (p.flagmask & P.hitmask) == P.hitmask;
+        if (done) {
+            if (is_hit) atomicOr(P.bitmap + (idx >> 5), 1u << (idx & 31));
+            if (P.photon_out) store_photon(P.photon_out + idx, p);
+            if (P.seq_out) {
+                ulonglong2* s = reinterpret_cast<ulonglong2*>(P.seq_out + idx);
+                s[0] = make_ulonglong2(seq.his[0], seq.his[1]);
+                s[1] = make_ulonglong2(seq.bnd[0], seq.bnd[1]);
+            }
+            live = false;
+        }
+        if (P.hit_unordered) {
+            const unsigned hm = __ballot_sync(0xffffffffu, is_hit);
+            if (hm) {
+                const int leader = __ffs(hm) - 1;
+                unsigned long long base = 0;
+                if ((int)lane == leader) base = atomicAdd(P.hit_count, (unsigned long long)__popc(hm));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (is_hit) store_photon(P.hit_unordered + base + __popc(hm & lt), p);
+            }
+        }
     }
 }
 
@@ -346,7 +463,7 @@ struct gbo_engine {
     gbo_config cfg{};
     cudaStream_t stream = nullptr;
     // geometry
-    DBuf<BvhNode> tlas;
+    DBuf<BvhNode2> tlas;
     DBuf<int32_t> tlas_index;
     DBuf<InstDev> inst;
     DBuf<PrimDev> prim;
@@ -360,6 +477,7 @@ struct gbo_engine {
     int bnd_nx = 0, bnd_ny = 0, hd_factor = 0;
     float nm0 = 60.f, nms = 1.f;
     bool has_tree = false;
+    long long pool_grid[2] = {0, 0};        // resident blocks of k_simulate_pool<false|true>
     // event
     DBuf<gbo_quad6> gs;
     DBuf<unsigned long long> gs_end;
@@ -400,6 +518,9 @@ int gbo_config_default(gbo_config* c)
     c->record_photon = 0;
     c->record_seq = 0;
     c->max_photon = 0;
+    c->kernel_mode = 1;
+    c->refill_min = 32;
+    c->blocks_per_sm = 0;
     long long iv;
     float fv;
     if (env_int("OPTICKS_MAX_BOUNCE", iv)) c->max_bounce = (int32_t)iv;
@@ -507,7 +628,7 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
         const unsigned tc = g->node[noff].q3.u[2];
         if (tc < GBO_CSG_NODE) e->has_tree = true;
     }
-    TRY(upload(e->tlas, acc.tlas.data(), acc.tlas.size(), e->stream));
+    TRY(upload(e->tlas, acc.tlas2.data(), acc.tlas2.size(), e->stream));
     TRY(upload(e->tlas_index, acc.tlas_index.data(), acc.tlas_index.size(), e->stream));
     TRY(upload(e->inst, acc.inst.data(), acc.inst.size(), e->stream));
     TRY(upload(e->prim, acc.prim.data(), acc.prim.size(), e->stream));
@@ -528,6 +649,18 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     TRY(make_texture(&e->bnd_array, &e->bnd_tex, g->bnd, e->bnd_nx, e->bnd_ny, true));
     TRY(make_texture(&e->icdf_array, &e->icdf_tex, g->icdf, g->icdf_nx, g->icdf_ny, false));
     TRY(e->counters.ensure(4));
+    {
+        int sms = 0, b0 = 0, b1 = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_simulate_pool<false>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_simulate_pool<true>, SIM_BLOCK, 0) != cudaSuccess) {
+            gbo_engine_destroy(e);
+            return fail(GBO_ERR_CUDA, "occupancy query failed");
+        }
+        const int want = e->cfg.blocks_per_sm;
+        e->pool_grid[0] = (long long)sms * (want > 0 && want < b0 ? want : (b0 > 0 ? b0 : 1));
+        e->pool_grid[1] = (long long)sms * (want > 0 && want < b1 ? want : (b1 > 0 ? b1 : 1));
+    }
     if (cudaStreamSynchronize(e->stream) != cudaSuccess) {
         gbo_engine_destroy(e);
         return fail(GBO_ERR_CUDA, "geometry upload failed");
@@ -609,11 +742,21 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
 
     CU(cudaMemsetAsync(e->counters.ptr, 0, 4 * sizeof(unsigned long long), s));
     int launches = prior_launches;
+    const bool pool = e->cfg.kernel_mode == 0;
+    if (pool && num_photon > 0) CU(cudaMemsetAsync(e->bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
     CU(cudaEventRecord(e->ev[1], s));
     if (num_photon > 0) {
-        const long long blocks = (num_photon + SIM_BLOCK - 1) / SIM_BLOCK;
-        if (e->has_tree) k_simulate<true><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
-        else k_simulate<false><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
+        if (pool) {
+            const long long need = (num_photon + SIM_BLOCK - 1) / SIM_BLOCK;
+            const long long grid = need < e->pool_grid[e->has_tree] ? need : e->pool_grid[e->has_tree];
+            const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
+            if (e->has_tree) k_simulate_pool<true><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, e->counters.ptr + 2, refill);
+            else k_simulate_pool<false><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, e->counters.ptr + 2, refill);
+        } else {
+            const long long blocks = (num_photon + SIM_BLOCK - 1) / SIM_BLOCK;
+            if (e->has_tree) k_simulate<true><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
+            else k_simulate<false><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
+        }
         CU(cudaGetLastError());
         launches++;
     }

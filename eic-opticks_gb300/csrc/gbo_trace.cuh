@@ -5,11 +5,13 @@
 //   * intersections with t in (tmin, tmax) via intersect_prim on the object-frame ray (the instance's inverse
 //     transform applied to the world ray; t is shared between frames);
 //   * the closest t wins; equal t resolve to the lowest (instance, prim) so that the result does not depend on
-//     traversal order;
+//     traversal order or on the instance hint;
 //   * the object-frame normal goes to the world frame through the inverse-transpose
 //     (optixTransformNormalFromObjectToWorldSpace); identity instances skip both transforms;
 //   * iindex|identity and globalPrimIdx|boundary packed in 16-bit halves (CSGOptiX7.cu:753, :929);
 //   * a miss returns boundary 0xffff (__miss__ms).
+// Traversal: the instance the photon last hit is intersected first (photons mostly stay inside one solid), then
+// the TLAS is walked front to back with nodes that carry both child boxes, pruning boxes beyond the current best.
 #pragma once
 #include "gbo_csg.cuh"
 #include "gbo_physics.cuh"
@@ -18,7 +20,7 @@
 namespace gbo {
 
 struct Accel {
-    const BvhNode* tlas;
+    const BvhNode2* tlas;
     const int32_t* tlas_index;
     const InstDev* inst;
     const PrimDev* prim;
@@ -42,21 +44,15 @@ GBO_DEV float3 safe_inv(float3 d) { return f3(1.f / d.x, 1.f / d.y, 1.f / d.z); 
 
 GBO_DEV float3 inst_point(const InstDev& d, float3 v)
 {
-    const float4 c0 = *reinterpret_cast<const float4*>(d.c0);
-    const float4 c1 = *reinterpret_cast<const float4*>(d.c1);
-    const float4 c2 = *reinterpret_cast<const float4*>(d.c2);
-    return f3(c0.x * v.x + c0.y * v.y + c0.z * v.z + c0.w * 1.f,
-              c1.x * v.x + c1.y * v.y + c1.z * v.z + c1.w * 1.f,
-              c2.x * v.x + c2.y * v.y + c2.z * v.z + c2.w * 1.f);
+    return f3(d.c0[0] * v.x + d.c0[1] * v.y + d.c0[2] * v.z + d.c0[3] * 1.f,
+              d.c1[0] * v.x + d.c1[1] * v.y + d.c1[2] * v.z + d.c1[3] * 1.f,
+              d.c2[0] * v.x + d.c2[1] * v.y + d.c2[2] * v.z + d.c2[3] * 1.f);
 }
 GBO_DEV float3 inst_vector(const InstDev& d, float3 v)
 {
-    const float4 c0 = *reinterpret_cast<const float4*>(d.c0);
-    const float4 c1 = *reinterpret_cast<const float4*>(d.c1);
-    const float4 c2 = *reinterpret_cast<const float4*>(d.c2);
-    return f3(c0.x * v.x + c0.y * v.y + c0.z * v.z + c0.w * 0.f,
-              c1.x * v.x + c1.y * v.y + c1.z * v.z + c1.w * 0.f,
-              c2.x * v.x + c2.y * v.y + c2.z * v.z + c2.w * 0.f);
+    return f3(d.c0[0] * v.x + d.c0[1] * v.y + d.c0[2] * v.z + d.c0[3] * 0.f,
+              d.c1[0] * v.x + d.c1[1] * v.y + d.c1[2] * v.z + d.c1[3] * 0.f,
+              d.c2[0] * v.x + d.c2[1] * v.y + d.c2[2] * v.z + d.c2[3] * 0.f);
 }
 GBO_DEV float3 inst_normal(const InstDev& d, float3 n)    // transpose of the inverse 3x3
 {
@@ -69,8 +65,8 @@ GBO_DEV InstDev load_inst(const InstDev* p)
 {
     const float4* q = reinterpret_cast<const float4*>(p);
     InstDev d;
-    float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
-    int4 e = __ldg(reinterpret_cast<const int4*>(q + 3));
+    const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    const int4 e = __ldg(reinterpret_cast<const int4*>(q + 3));
     d.c0[0] = a.x; d.c0[1] = a.y; d.c0[2] = a.z; d.c0[3] = a.w;
     d.c1[0] = b.x; d.c1[1] = b.y; d.c1[2] = b.z; d.c1[3] = b.w;
     d.c2[0] = c.x; d.c2[1] = c.y; d.c2[2] = c.z; d.c2[3] = c.w;
@@ -88,61 +84,87 @@ GBO_DEV bool prim_hit(float4& is, const Accel& a, int node_offset, float t_min, 
     return false;
 }
 
-constexpr int TRAVERSAL_STACK = 64;
+struct Best {
+    float t;
+    unsigned key;
+    float4 is;
+    int inst;
+    unsigned pb;
+};
 
 template <bool TREE>
-GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tmax, Hit& h)
+GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float tmin, Best& b)
 {
-    float best_t = tmax;
-    unsigned best_key = 0xffffffffu;
-    float4 best_is = make_float4(0.f, 0.f, 0.f, 0.f);
-    int best_inst = -1;
-    unsigned best_pb = 0u;
-    const float3 inv = safe_inv(dir);
+    const InstDev d = load_inst(a.inst + ii);
+    const float3 oo = d.is_identity ? pos : inst_point(d, pos);
+    const float3 od = d.is_identity ? dir : inst_vector(d, dir);
+    const float3 oinv = safe_inv(od);
+    const int2 so = __ldg(reinterpret_cast<const int2*>(a.solid + d.solid));
+    for (int k2 = 0; k2 < so.y; k2++) {
+        const float4* pq = reinterpret_cast<const float4*>(a.prim + so.x + k2);
+        const float4 pb0 = __ldg(pq), pb1 = __ldg(pq + 1);
+        float ptn;
+        if (!slab(pb0, pb1, oo, oinv, tmin, b.t, ptn)) continue;
+        float4 is;
+        if (!prim_hit<TREE>(is, a, __float_as_int(pb0.w), tmin, oo, od)) continue;
+        const unsigned key = ((unsigned)ii << 16) | (unsigned)k2;
+        if (is.w < b.t || (is.w == b.t && b.key != 0xffffffffu && key < b.key)) {
+            b.t = is.w; b.key = key; b.is = is; b.inst = ii; b.pb = __float_as_uint(pb1.w);
+        }
+    }
+}
 
+constexpr int TRAVERSAL_STACK = 64;
+constexpr int HINT_FIRST = 0x7fffff;     // leaf item standing for the hint instance
+
+// work items: an inner node index (>= 0) or a leaf range encoded as -(1 + (first << 8 | count))
+GBO_DEV int leaf_item(int first, int count) { return -(1 + ((first << 8) | count)); }
+
+template <bool TREE>
+GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tmax, int hint, Hit& h)
+{
+    Best b;
+    b.t = tmax; b.key = 0xffffffffu; b.is = make_float4(0.f, 0.f, 0.f, 0.f); b.inst = -1; b.pb = 0u;
+    const float3 inv = safe_inv(dir);
     int stack[TRAVERSAL_STACK];
     int sp = 0;
-    int ni = 0;
+    int item = 0;
+    if (hint >= 0) { stack[sp++] = 0; item = leaf_item(HINT_FIRST, 1); }
     for (;;) {
-        const float4* nq = reinterpret_cast<const float4*>(a.tlas + ni);
-        const float4 nb0 = __ldg(nq), nb1 = __ldg(nq + 1);
-        const int count = __float_as_int(nb1.w);
-        float tn;
-        bool visit = slab(nb0, nb1, pos, inv, tmin, best_t, tn);
-        if (visit && count > 0) {
-            const int first = __float_as_int(nb0.w);
+        int next = -0x7fffffff;
+        if (item < 0) {
+            const int code = -item - 1;
+            const int first = code >> 8, count = code & 0xff;
+#pragma unroll 1
             for (int k = 0; k < count; k++) {
-                const int ii = __ldg(a.tlas_index + first + k);
-                const InstDev d = load_inst(a.inst + ii);
-                const float3 oo = d.is_identity ? pos : inst_point(d, pos);
-                const float3 od = d.is_identity ? dir : inst_vector(d, dir);
-                const float3 oinv = safe_inv(od);
-                const int2 so = __ldg(reinterpret_cast<const int2*>(a.solid + d.solid));
-                for (int k2 = 0; k2 < so.y; k2++) {
-                    const float4* pq = reinterpret_cast<const float4*>(a.prim + so.x + k2);
-                    const float4 pb0 = __ldg(pq), pb1 = __ldg(pq + 1);
-                    float ptn;
-                    if (!slab(pb0, pb1, oo, oinv, tmin, best_t, ptn)) continue;
-                    float4 is;
-                    if (!prim_hit<TREE>(is, a, __float_as_int(pb0.w), tmin, oo, od)) continue;
-                    const unsigned key = ((unsigned)ii << 16) | (unsigned)k2;
-                    if (is.w < best_t || (is.w == best_t && best_key != 0xffffffffu && key < best_key)) {
-                        best_t = is.w; best_key = key; best_is = is; best_inst = ii;
-                        best_pb = __float_as_uint(pb1.w);
-                    }
-                }
+                const int ii = first == HINT_FIRST ? hint : __ldg(a.tlas_index + first + k);
+                if (first == HINT_FIRST || ii != hint) test_instance<TREE>(a, ii, pos, dir, tmin, b);
             }
-        } else if (visit) {
-            const int left = ni + 1, right = __float_as_int(nb0.w);
-            if (sp < TRAVERSAL_STACK) stack[sp++] = right;
-            ni = left;
-            continue;
+        } else {
+            const float4* nq = reinterpret_cast<const float4*>(a.tlas + item);
+            const float4 l0 = __ldg(nq), h0 = __ldg(nq + 1), l1 = __ldg(nq + 2), h1 = __ldg(nq + 3);
+            float t0, t1;
+            const bool v0 = slab(l0, h0, pos, inv, tmin, b.t, t0);
+            const bool v1 = slab(l1, h1, pos, inv, tmin, b.t, t1);
+            const int c0 = __float_as_int(h0.w), c1 = __float_as_int(h1.w);
+            const int it0 = c0 > 0 ? leaf_item(__float_as_int(l0.w), c0) : __float_as_int(l0.w);
+            const int it1 = c1 > 0 ? leaf_item(__float_as_int(l1.w), c1) : __float_as_int(l1.w);
+            if (v0 && v1) {                         // nearer child next, the other on the stack
+                const bool near0 = t0 <= t1;
+                next = near0 ? it0 : it1;
+                if (sp < TRAVERSAL_STACK) stack[sp++] = near0 ? it1 : it0;
+            } else if (v0) {
+                next = it0;
+            } else if (v1) {
+                next = it1;
+            }
         }
+        if (next != -0x7fffffff) { item = next; continue; }
         if (sp == 0) break;
-        ni = stack[--sp];
+        item = stack[--sp];
     }
 
-    if (best_inst < 0) {
+    if (b.inst < 0) {
         h.normal = f3(0.f, 0.f, 0.f);
         h.t = 1.f;
         h.lposcost = 0.f;
@@ -151,21 +173,21 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
         h.prim_boundary = 0xffffffffu;
         return;
     }
-    const InstDev d = load_inst(a.inst + best_inst);
-    float3 n = f3(best_is.x, best_is.y, best_is.z);
+    const InstDev d = load_inst(a.inst + b.inst);
+    float3 n = f3(b.is.x, b.is.y, b.is.z);
     float3 lpos;
     if (d.is_identity) {
-        lpos = pos + best_is.w * dir;
+        lpos = pos + b.is.w * dir;
     } else {
         n = inst_normal(d, n);
-        lpos = inst_point(d, pos) + best_is.w * inst_vector(d, dir);
+        lpos = inst_point(d, pos) + b.is.w * inst_vector(d, dir);
     }
     h.normal = n;
-    h.t = best_is.w;
+    h.t = b.is.w;
     h.lposcost = lpos.z / sqrtf(dot(lpos, lpos));
     h.lposfphi = 0.f;
     h.iindex_identity = ((d.iindex & 0xffffu) << 16) | (d.identity & 0xffffu);
-    h.prim_boundary = best_pb;
+    h.prim_boundary = b.pb;
 }
 
 }  // namespace gbo

@@ -41,7 +41,8 @@ class Config(C.Structure):
                 ("propagate_epsilon0", C.c_float), ("epsilon0_mask", C.c_uint32), ("hit_mask", C.c_uint32),
                 ("rng_seed", C.c_uint64), ("rng_offset", C.c_uint64), ("event_skipahead", C.c_uint64),
                 ("tmax", C.c_float), ("debug_tag", C.c_int32), ("record_photon", C.c_int32),
-                ("record_seq", C.c_int32), ("max_photon", C.c_int64)]
+                ("record_seq", C.c_int32), ("max_photon", C.c_int64), ("kernel_mode", C.c_int32),
+                ("refill_min", C.c_int32), ("blocks_per_sm", C.c_int32), ("reserved", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -169,6 +170,8 @@ class Engine:
 
     def hits(self, out=None):
         n = self.num_hit()
+        if n < 0:       # no event yet: let the library report the state error
+            _check(self.lib.gbo_copy_hits(self.handle, None, 0, 0), "gbo_copy_hits")
         out = np.zeros(n, dtype=L.PHOTON) if out is None else out
         _check(self.lib.gbo_copy_hits(self.handle, out.ctypes.data_as(C.c_void_p), 0, n), "gbo_copy_hits")
         return out

@@ -75,6 +75,10 @@ typedef struct gbo_config {
     int32_t  record_photon;         /* keep the full photon array of each event */
     int32_t  record_seq;            /* keep seqhis/seqbnd of each event */
     int64_t  max_photon;            /* capacity limit per event (0: no limit beyond device memory) */
+    int32_t  kernel_mode;           /* 0: persistent photon-pool kernel, 1: one thread per photon (default) */
+    int32_t  refill_min;            /* pool kernel: idle lanes a warp waits for before refilling (1..32, 32) */
+    int32_t  blocks_per_sm;         /* pool kernel: resident blocks per SM (0: occupancy maximum) */
+    int32_t  reserved;
 } gbo_config;
 
 typedef struct gbo_stats {

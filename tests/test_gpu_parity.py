@@ -172,3 +172,20 @@ def test_errors_are_reported(E):
     with pytest.raises(E.GBOError):
         eng.simulate(0, gs, None)
     eng.close()
+
+
+def test_kernel_forms_bit_identical(E):
+    """The photon-pool kernel and the one-thread-per-photon kernel produce the same bytes for every photon."""
+    z = load_golden("sim_crystal_array.npz")
+    arrays = golden_arrays(z)
+    outs = []
+    for mode, refill in ((1, 1), (0, 1), (0, 8), (0, 32)):
+        eng = E.Engine(arrays, record_photon=1, record_seq=1, kernel_mode=mode, refill_min=refill)
+        n = eng.simulate(int(z["event_index"]), z["gs"])
+        outs.append((eng.photons(), eng.seq(), eng.hits(), n))
+        eng.close()
+    p0, s0, h0, n0 = outs[0]
+    for p, s, h, n in outs[1:]:
+        assert np.array_equal(p.view(np.uint32), p0.view(np.uint32))
+        assert np.array_equal(s.view(np.uint64), s0.view(np.uint64))
+        assert n == n0 and np.array_equal(h.view(np.uint32), h0.view(np.uint32))
