@@ -966,3 +966,182 @@ int gbo_scint_wavelength(gbo_engine* e, const float* u, int32_t n, float* out)
 }
 
 }  // extern "C"
+
+// ================================================================================================================
+// Simulation without any allocation.
+//
+// Some callers cannot allocate device memory while events are processed: a trigger or DAQ process whose device
+// memory is carved up once at start-up by another runtime, a host framework that forbids allocator calls on its
+// event threads because cudaMalloc/cudaFree synchronise the device and stall every other stream, or code that
+// must not grow its footprint after initialisation.  gbo_simulate_noalloc serves them: gensteps in and hits out
+// are caller-owned device buffers, and all intermediate state (genstep prefix, hit bitmap and its scan, the
+// unordered hit staging, counters) lives in one fixed file-scope device array.  The array is part of the
+// loaded library image, so every GPU that loads libgbopticks.so holds its GBO_NOALLOC_SCRATCH_BYTES until the
+// process exits.  The engine's geometry must have been created beforehand (gbo_engine_create allocates; this
+// entry point never does).
+// ================================================================================================================
+
+namespace gbo {
+
+constexpr long long NA_MAX_PHOTON = 1ll << 22;            // photons per call
+constexpr long long NA_MAX_HIT = 1ll << 17;               // hits per call
+constexpr long long NA_MAX_GENSTEP = 1ll << 15;           // gensteps per call
+constexpr long long NA_WORDS = NA_MAX_PHOTON / 32;
+constexpr long long NA_BLOCKS = NA_WORDS / SCAN_WORDS;
+// byte offsets inside the scratch array (each a multiple of 256)
+constexpr size_t NA_OFF_COUNTERS = 0;                                             // 4 x u64
+constexpr size_t NA_OFF_GS_END = 256;                                             // NA_MAX_GENSTEP x u64
+constexpr size_t NA_OFF_BITMAP = NA_OFF_GS_END + NA_MAX_GENSTEP * 8;              // NA_WORDS x u32
+constexpr size_t NA_OFF_PREFIX = NA_OFF_BITMAP + NA_WORDS * 4;                    // NA_WORDS x u32
+constexpr size_t NA_OFF_BLOCK_SUM = NA_OFF_PREFIX + NA_WORDS * 4;                 // NA_BLOCKS x u32
+constexpr size_t NA_OFF_BLOCK_OFF = NA_OFF_BLOCK_SUM + NA_BLOCKS * 4;             // NA_BLOCKS x u64
+constexpr size_t NA_OFF_STAGING = NA_OFF_BLOCK_OFF + NA_BLOCKS * 8;               // NA_MAX_HIT x sphoton
+constexpr size_t NA_BYTES = NA_OFF_STAGING + NA_MAX_HIT * sizeof(gbo_sphoton);
+static_assert(NA_OFF_BITMAP % 256 == 0 && NA_OFF_PREFIX % 256 == 0 && NA_OFF_BLOCK_SUM % 256 == 0 &&
+              NA_OFF_BLOCK_OFF % 256 == 0 && NA_OFF_STAGING % 256 == 0, "scratch sections stay 256-byte aligned");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+// The one-thread-per-photon program with a bounded hit append: hits beyond the staging capacity are counted
+// but not stored, and the host reports the overflow.
+template <bool TREE>
+__global__ void __launch_bounds__(SIM_BLOCK) k_simulate_bounded(const __grid_constant__ Params P, long long cap)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    Photon p;
+    bool is_hit = false;
+    if (idx < P.num_photon) {
+        Rng rng;
+        generate(P, idx, p, rng);
+        int bounce = 0;
+        int hint = -1;
+        while (bounce < P.max_bounce && p.time < P.max_time) {
+            const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
+            Hit h;
+            trace<TREE>(P.acc, p.pos, p.mom, tmin, P.tmax, hint, h);
+            if ((h.prim_boundary & 0xffffu) == 0xffffu) break;
+            hint = (int)(h.iindex_identity >> 16);
+            h.normal = normalize(h.normal);
+            const int command = propagate(P.tab, p, h, rng);
+            bounce++;
+            if (command == CMD_BREAK) break;
+        }
+        is_hit = (p.flagmask & P.hitmask) == P.hitmask;
+    }
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned mask = __ballot_sync(0xffffffffu, is_hit);
+    const long long word = idx >> 5;
+    if (lane == 0 && word * 32 < P.num_photon) P.bitmap[word] = mask;
+    if (mask) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(P.hit_count, (unsigned long long)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const unsigned long long slot = base + __popc(mask & ((1u << lane) - 1u));
+        if (is_hit && slot < (unsigned long long)cap) store_photon(P.hit_unordered + slot, p);
+    }
+}
+
+}  // namespace gbo
+
+namespace {
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[NA_MAX_DEVICES] = {nullptr};
+
+// Device address of the scratch array on the current device, looked up once per device.
+int noalloc_scratch(int device, unsigned char** out)
+{
+    if (device < 0 || device >= NA_MAX_DEVICES) return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: device %d out of range", device);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (err != cudaSuccess || !p)
+            return fail(GBO_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(err));
+        g_noalloc_ptr[device] = p;
+    }
+    *out = (unsigned char*)g_noalloc_ptr[device];
+    return GBO_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int64_t gbo_noalloc_scratch_bytes(void) { return (int64_t)NA_BYTES; }
+
+int gbo_simulate_noalloc(gbo_engine* e, int32_t event_id, const void* d_gs, int64_t num_gs, const void* d_input_photon,
+                         int64_t num_input_photon, gbo_sphoton* d_hits, int64_t hit_capacity, int64_t* num_hit,
+                         void* cuda_stream)
+{
+    if (!e || !num_hit) return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: null engine or num_hit");
+    *num_hit = 0;
+    if (num_gs < 0 || (num_gs > 0 && !d_gs)) return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: bad gensteps");
+    if (num_gs > NA_MAX_GENSTEP)
+        return fail(GBO_ERR_CAPACITY, "gbo_simulate_noalloc: %lld gensteps above the limit of %lld", (long long)num_gs,
+                    NA_MAX_GENSTEP);
+    if (hit_capacity < 0 || (hit_capacity > 0 && !d_hits)) return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: bad hit buffer");
+    CU(cudaSetDevice(e->device));
+    unsigned char* s_base = nullptr;
+    int rc = noalloc_scratch(e->device, &s_base);
+    if (rc) return rc;
+    cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : e->stream;
+    unsigned long long* counters = (unsigned long long*)(s_base + NA_OFF_COUNTERS);
+    unsigned long long* gs_end = (unsigned long long*)(s_base + NA_OFF_GS_END);
+    uint32_t* bitmap = (uint32_t*)(s_base + NA_OFF_BITMAP);
+    uint32_t* word_prefix = (uint32_t*)(s_base + NA_OFF_PREFIX);
+    uint32_t* block_sum = (uint32_t*)(s_base + NA_OFF_BLOCK_SUM);
+    unsigned long long* block_offset = (unsigned long long*)(s_base + NA_OFF_BLOCK_OFF);
+    gbo_sphoton* staging = (gbo_sphoton*)(s_base + NA_OFF_STAGING);
+    if (num_gs == 0) return GBO_OK;
+
+    // counters left over from the previous call must start at zero
+    CU(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
+    k_genstep_prefix<<<1, 1024, 0, s>>>((const gbo_quad6*)d_gs, (int)num_gs, gs_end);
+    CU(cudaGetLastError());
+    unsigned long long total = 0;
+    CU(cudaMemcpyAsync(&total, gs_end + (num_gs - 1), sizeof(total), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    if ((long long)total > NA_MAX_PHOTON)
+        return fail(GBO_ERR_CAPACITY, "gbo_simulate_noalloc: %llu photons above the limit of %lld", total, NA_MAX_PHOTON);
+    if (num_input_photon > 0 && (long long)num_input_photon < (long long)total)
+        return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: %lld input photons for %llu photon slots", (long long)num_input_photon, total);
+
+    Params P = make_params(e);
+    P.position0 = e->cfg.rng_offset + e->cfg.event_skipahead * (uint64_t)(event_id < 0 ? 0 : event_id);
+    P.gs = (const float4*)d_gs;
+    P.gs_end = gs_end;
+    P.num_gs = (int)num_gs;
+    P.num_photon = (long long)total;
+    P.input_photon = (const gbo_sphoton*)d_input_photon;
+    P.hit_unordered = staging;
+    P.hit_count = counters;
+    P.bitmap = bitmap;
+    const long long words = ((long long)total + 31) / 32;
+    const long long nblk = (words + SCAN_WORDS - 1) / SCAN_WORDS;
+    if (total > 0) {
+        const long long blocks = ((long long)total + SIM_BLOCK - 1) / SIM_BLOCK;
+        if (e->has_tree) k_simulate_bounded<true><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P, NA_MAX_HIT);
+        else k_simulate_bounded<false><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P, NA_MAX_HIT);
+        CU(cudaGetLastError());
+        k_word_prefix<<<(unsigned)nblk, SCAN_WORDS, 0, s>>>(bitmap, words, word_prefix, block_sum);
+        k_block_offsets<<<1, 1024, 0, s>>>(block_sum, nblk, block_offset, counters + 1);
+        CU(cudaGetLastError());
+    }
+    unsigned long long found = 0;
+    CU(cudaMemcpyAsync(&found, counters + 1, sizeof(found), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    *num_hit = (int64_t)found;
+    if ((long long)found > NA_MAX_HIT)
+        return fail(GBO_ERR_CAPACITY, "gbo_simulate_noalloc: %llu hits above the staging limit of %lld", found, NA_MAX_HIT);
+    if ((long long)found > hit_capacity)
+        return fail(GBO_ERR_CAPACITY, "gbo_simulate_noalloc: %llu hits, hit buffer holds %lld", found, (long long)hit_capacity);
+    if (found > 0) {
+        k_gather_unordered<<<(unsigned)((found + 255) / 256), 256, 0, s>>>(staging, counters, 0ull, bitmap, word_prefix,
+                                                                          block_offset, d_hits);
+        CU(cudaGetLastError());
+        CU(cudaStreamSynchronize(s));
+    }
+    return GBO_OK;
+}
+
+}  // extern "C"

@@ -120,6 +120,22 @@ int         gbo_rng_sequence(int device, uint64_t seed, uint64_t subsequence0, u
 int         gbo_texture_lookup(gbo_engine* e, int32_t which, const float* xy, int32_t n, float* out);
 int         gbo_scint_wavelength(gbo_engine* e, const float* u, int32_t n, float* out);
 
+/* gbo_simulate_noalloc : has no counterpart in the reference.  One event like gbo_simulate_device, for callers
+ * that may not allocate device memory while events run (memory reserved up front by another runtime, or event
+ * threads on which cudaMalloc/cudaFree must not be called because they synchronise the device).  Gensteps
+ * (d_gs), optional input photons and the hit buffer (d_hits, room for hit_capacity hits) are the caller's device
+ * memory; hits come back in photon order and *num_hit receives their number.  Everything else lives in one fixed
+ * device array of gbo_noalloc_scratch_bytes() bytes (about 9.3 MB) that each GPU loading the library keeps until
+ * the process exits; no allocating call is made.  Limits per call: 32768 gensteps, 4194304 photons, 131072 hits;
+ * above them the call returns GBO_ERR_CAPACITY (for hits, *num_hit still reports the count).  The first call on a
+ * device looks up the array's device address, so make it before any stream capture.  Calls share the array and
+ * keep the previous call's contents: two calls in flight at the same time on one GPU race and corrupt each other,
+ * so serialise them.  The call is synchronous on cuda_stream (NULL: the engine's stream). */
+int64_t     gbo_noalloc_scratch_bytes(void);
+int         gbo_simulate_noalloc(gbo_engine* e, int32_t event_id, const void* d_gs, int64_t num_gs,
+                                 const void* d_input_photon, int64_t num_input_photon, gbo_sphoton* d_hits,
+                                 int64_t hit_capacity, int64_t* num_hit, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

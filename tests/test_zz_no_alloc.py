@@ -1,0 +1,65 @@
+"""gbo_simulate_noalloc : the simulation entry point for callers that cannot allocate device memory per event.
+
+Its hits must equal those of the allocating device entry point (gbo_simulate_device) for the same event, bit for
+bit (the photon program is deterministic), on two calls in a row so that state left in the shared scratch array
+by the first call cannot leak into the second.  This file is collected last so that a run stopping at the first
+failure has already run every other test; it also passes alone in a fresh process.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    from eic_opticks_gb300 import engine as E, geometry as G, gensteps as GS
+    lib = E.load()
+    lib.gbo_simulate_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                         C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.c_void_p]
+    lib.gbo_noalloc_scratch_bytes.restype = C.c_int64
+    eng = E.Engine(G.crystal_array().arrays(), device=0)
+    gs = GS.crystal_scint_gensteps(60, 1500, seed=21)
+    d_gs = torch.from_numpy(gs.copy()).cuda()
+    yield torch, E, lib, eng, gs, d_gs
+    eng.close()
+
+
+def noalloc_hits(torch, E, lib, eng, d_gs, n_gs, event_id, capacity):
+    d_hits = torch.zeros((capacity, 16), dtype=torch.float32, device="cuda")
+    n = C.c_int64(-1)
+    rc = lib.gbo_simulate_noalloc(eng.handle, event_id, C.c_void_p(d_gs.data_ptr()), n_gs, None, 0,
+                                  C.c_void_p(d_hits.data_ptr()), capacity, C.byref(n), None)
+    return rc, n.value, d_hits
+
+
+def test_scratch_is_modest(setup):
+    torch, E, lib, eng, gs, d_gs = setup
+    assert 0 < lib.gbo_noalloc_scratch_bytes() <= 16 << 20
+
+
+def test_noalloc_matches_device_entry_point_twice(setup):
+    torch, E, lib, eng, gs, d_gs = setup
+    for event_id in (5, 6):
+        want_n = eng.simulate_device(event_id, d_gs.data_ptr(), len(gs))
+        want = eng.hits()
+        rc, n, d_hits = noalloc_hits(torch, E, lib, eng, d_gs, len(gs), event_id, 2 * want_n + 16)
+        assert rc == 0, lib.gbo_last_error()
+        assert n == want_n
+        got = d_hits[:n].cpu().numpy().view(E.L.PHOTON).reshape(-1)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_noalloc_rejects_sizes_beyond_limits(setup):
+    torch, E, lib, eng, gs, d_gs = setup
+    too_many = 40000                      # above the 32768 genstep limit
+    big = torch.zeros((too_many, 6, 4), dtype=torch.float32, device="cuda")
+    rc, n, _ = noalloc_hits(torch, E, lib, eng, big, too_many, 0, 16)
+    assert rc == 4 and b"genstep" in lib.gbo_last_error()
+    rc, n, _ = noalloc_hits(torch, E, lib, eng, d_gs, len(gs), 5, 1)     # hit buffer too small
+    assert rc == 4 and n > 1 and b"hit buffer" in lib.gbo_last_error()
