@@ -71,7 +71,7 @@ struct Builder {
         nodes.push_back(BvhNode{});
         for (int k = 0; k < 3; k++) { nodes[self].bmin[k] = (float)bb.lo[k]; nodes[self].bmax[k] = (float)bb.hi[k]; }
         const int n = end - begin;
-        if (n <= 2 || depth >= 48) {
+        if (n <= 2 || (depth >= 48 && n <= 255)) {      // leaf counts fit the 8-bit field of the traversal items
             nodes[self].left_first = begin;
             nodes[self].count = n;
             return self;
@@ -239,9 +239,9 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
     if (order.empty()) {            // root is a leaf: one node whose second child is empty
         BvhNode2 n{};
         child(0, n.lo0, n.hi0, n.first0, n.count0);
-        for (int k = 0; k < 3; k++) { n.lo1[k] = 1.f; n.hi1[k] = -1.f; }
+        for (int k = 0; k < 3; k++) { n.lo1[k] = 0.f; n.hi1[k] = 0.f; }
         n.first1 = 0;
-        n.count1 = 0x7fffffff;      // never visited: empty box
+        n.count1 = -1;              // no second child: never visited
         out.tlas2.push_back(n);
     } else {
         for (int id : order) {

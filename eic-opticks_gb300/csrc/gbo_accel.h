@@ -25,8 +25,8 @@ struct BvhNode {
 static_assert(sizeof(BvhNode) == 32, "BvhNode is 32 bytes");
 
 // Traversal node: the boxes of both children, so one 64 B load decides which children to visit and in which
-// order.  For child c, count_c > 0 marks a leaf holding tlas_index[first_c .. first_c+count_c), else first_c
-// is the inner node to visit.
+// order.  For child c, count_c > 0 marks a leaf holding tlas_index[first_c .. first_c+count_c) (at most 255),
+// count_c == 0 an inner node first_c, count_c < 0 an absent child (only in a root whose single child is a leaf).
 struct BvhNode2 {
     float lo0[3]; int32_t first0;
     float hi0[3]; int32_t count0;

@@ -36,12 +36,14 @@ constexpr float PI_F = 3.14159265358979323846f;
 // ---- Philox4x32-10, stateless counter form ------------------------------------------------------------------
 // A photon's stream position p (draws consumed so far, including the offset and event skipahead) maps to the
 // 128-bit counter (p >> 2, subsequence) and output lane p & 3 : the layout curand's Philox state walks.
+// Blocks are computed lazily: skip() only moves the position, so a block whose four outputs are all
+// alignment "burn" draws of the reference is never computed.
 struct Rng {
-    uint64_t block;       // low 64 bits of the counter
+    uint64_t pos;         // draws consumed (position in the subsequence)
+    uint64_t cached;      // block index held in out[], ~0 when none
     uint32_t sub_lo, sub_hi;
     uint32_t key0, key1;
     uint32_t out[4];
-    int lane;
 };
 
 GBO_DEV void philox10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, uint32_t* o)
@@ -62,37 +64,33 @@ GBO_DEV void philox10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32
     o[0] = c0; o[1] = c1; o[2] = c2; o[3] = c3;
 }
 
-GBO_DEV void rng_refill(Rng& r)
-{
-    philox10((uint32_t)r.block, (uint32_t)(r.block >> 32), r.sub_lo, r.sub_hi, r.key0, r.key1, r.out);
-}
-
 GBO_DEV void rng_init(Rng& r, uint64_t seed, uint64_t subsequence, uint64_t position)
 {
     r.key0 = (uint32_t)seed;
     r.key1 = (uint32_t)(seed >> 32);
     r.sub_lo = (uint32_t)subsequence;
     r.sub_hi = (uint32_t)(subsequence >> 32);
-    r.block = position >> 2;
-    r.lane = (int)(position & 3u);
-    rng_refill(r);
+    r.pos = position;
+    r.cached = ~0ull;
 }
+
+GBO_DEV void skip(Rng& r, unsigned n) { r.pos += n; }
 
 GBO_DEV float uniform(Rng& r)
 {
+    const uint64_t b = r.pos >> 2;
+    if (b != r.cached) {
+        philox10((uint32_t)b, (uint32_t)(b >> 32), r.sub_lo, r.sub_hi, r.key0, r.key1, r.out);
+        r.cached = b;
+    }
     uint32_t x;
-    switch (r.lane) {                // explicit select keeps out[] in registers
+    switch ((unsigned)r.pos & 3u) {  // explicit select keeps out[] in registers
         case 0: x = r.out[0]; break;
         case 1: x = r.out[1]; break;
         case 2: x = r.out[2]; break;
         default: x = r.out[3]; break;
     }
-    r.lane += 1;
-    if (r.lane == 4) {
-        r.block += 1;
-        r.lane = 0;
-        rng_refill(r);
-    }
+    r.pos += 1;
     return (float)x * 2.3283064365386963e-10f + (2.3283064365386963e-10f / 2.0f);
 }
 

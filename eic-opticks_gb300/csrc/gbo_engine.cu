@@ -29,6 +29,9 @@
 
 namespace gbo {
 
+#ifndef GBO_SIM_MINB
+#define GBO_SIM_MINB 1              // minimum resident blocks per SM asked of ptxas for the simulate kernels
+#endif
 constexpr int SIM_BLOCK = 128;
 constexpr int SCAN_WORDS = 256;     // words per block in k_word_prefix
 
@@ -53,7 +56,7 @@ struct Params {
 };
 
 template <bool TREE>
-__global__ void __launch_bounds__(SIM_BLOCK) k_simulate(const __grid_constant__ Params P)
+__global__ void __launch_bounds__(SIM_BLOCK, GBO_SIM_MINB) k_simulate(const __grid_constant__ Params P)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = idx < P.num_photon;
@@ -159,7 +162,7 @@ GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng)
 
 template <bool TREE>
 __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_pool(const __grid_constant__ Params P,
-                                                             unsigned long long* pool, int refill_min)
+                                                             unsigned long long* pool, int refill_min, int period)
 {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt = (1u << lane) - 1u;
@@ -168,13 +171,15 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_pool(const __grid_consta
     long long idx = -1;
     int bounce = 0;
     int hint = -1;
+    int it = 0;
     Photon p;
     Rng rng;
     Seq seq;
-    for (;;) {
-        // refill: idle lanes take consecutive photon indices with one atomic per warp
+    for (;; it++) {
+        // refill every `period` steps (or when the warp is empty): idle lanes take consecutive photon indices
+        // with one atomic per warp
         const unsigned idle = __ballot_sync(0xffffffffu, !live);
-        if (pool_open && __popc(idle) >= refill_min) {
+        if (pool_open && (idle == 0xffffffffu || (it % period == 0 && __popc(idle) >= refill_min))) {
             unsigned long long base = 0;
             const int leader = __ffs(idle) - 1;
             if ((int)lane == leader) base = atomicAdd(pool, (unsigned long long)__popc(idle));
@@ -518,9 +523,10 @@ int gbo_config_default(gbo_config* c)
     c->record_photon = 0;
     c->record_seq = 0;
     c->max_photon = 0;
-    c->kernel_mode = 1;
-    c->refill_min = 32;
+    c->kernel_mode = 0;
+    c->refill_min = 8;
     c->blocks_per_sm = 0;
+    c->refill_period = 1;
     long long iv;
     float fv;
     if (env_int("OPTICKS_MAX_BOUNCE", iv)) c->max_bounce = (int32_t)iv;
@@ -750,8 +756,9 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
             const long long need = (num_photon + SIM_BLOCK - 1) / SIM_BLOCK;
             const long long grid = need < e->pool_grid[e->has_tree] ? need : e->pool_grid[e->has_tree];
             const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
-            if (e->has_tree) k_simulate_pool<true><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, e->counters.ptr + 2, refill);
-            else k_simulate_pool<false><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, e->counters.ptr + 2, refill);
+            const int period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
+            if (e->has_tree) k_simulate_pool<true><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, e->counters.ptr + 2, refill, period);
+            else k_simulate_pool<false><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, e->counters.ptr + 2, refill, period);
         } else {
             const long long blocks = (num_photon + SIM_BLOCK - 1) / SIM_BLOCK;
             if (e->has_tree) k_simulate<true><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
@@ -903,6 +910,46 @@ int gbo_get_stats(const gbo_engine* e, gbo_stats* out)
 {
     if (!e || !out) return fail(GBO_ERR_ARG, "gbo_get_stats: null argument");
     *out = e->stats;
+    return GBO_OK;
+}
+
+int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs, const gbo_sphoton* input_photon,
+                 int64_t num_input_photon, int32_t trials, gbo_tune_result* out)
+{
+    if (!e || !out) return fail(GBO_ERR_ARG, "gbo_autotune: null argument");
+    if (trials < 1) trials = 1;
+    std::memset(out, 0, sizeof(*out));
+    struct Cand { int mode, refill, period; };
+    std::vector<Cand> cands = {{1, 32, 1}};
+    for (int r : {1, 2, 4, 8, 16, 32})
+        for (int p : {1, 4}) cands.push_back({0, r, p});
+    const gbo_config saved = e->cfg;
+    float best = 1e30f;
+    Cand pick = cands[0];
+    for (size_t c = 0; c < cands.size() && c < 32; c++) {
+        e->cfg.kernel_mode = cands[c].mode;
+        e->cfg.refill_min = cands[c].refill;
+        e->cfg.refill_period = cands[c].period;
+        float ms = 1e30f;
+        for (int t = 0; t <= trials; t++) {
+            int rc = gbo_simulate(e, event_id, gs, num_gs, input_photon, num_input_photon);
+            if (rc) { e->cfg = saved; return rc; }
+            if (t > 0 && e->stats.ms_simulate < ms) ms = e->stats.ms_simulate;   // first run warms up
+        }
+        out->cand_mode[c] = cands[c].mode;
+        out->cand_refill[c] = cands[c].refill;
+        out->cand_period[c] = cands[c].period;
+        out->cand_ms[c] = ms;
+        out->num_candidates = (int32_t)(c + 1);
+        if (ms < best) { best = ms; pick = cands[c]; }
+    }
+    e->cfg = saved;
+    e->cfg.kernel_mode = pick.mode;
+    e->cfg.refill_min = pick.refill;
+    e->cfg.refill_period = pick.period;
+    out->kernel_mode = pick.mode;
+    out->refill_min = pick.refill;
+    out->refill_period = pick.period;
     return GBO_OK;
 }
 

@@ -331,7 +331,7 @@ GBO_DEV int propagate_to_boundary(const Tables& t, Photon& p, const State& s, fl
     const float scattering_length = s.material1.z;
     const float reemission_prob = s.material1.w;
     const float group_velocity = s.m1group2.x;
-    if (t.debug_tag) { uniform(rng); uniform(rng); }
+    if (t.debug_tag) skip(rng, 2);
     const float u_scattering = uniform(rng);
     const float u_absorption = uniform(rng);
     const float scattering_distance = -scattering_length * logf(u_scattering);
@@ -399,7 +399,7 @@ GBO_DEV int propagate_at_boundary(const Tables& t, Photon& p, const State& s, fl
     const float TTx = E2_tx * tinv, TTy = E2_ty * tinv;
     const float TransCoeff = (tir || n1c1 == 0.f) ? 0.f : n2c2 * (E2_tx * E2_tx + E2_ty * E2_ty) / n1c1;
 
-    if (t.debug_tag) uniform(rng);
+    if (t.debug_tag) skip(rng, 1);
     const float u_reflect = uniform(rng);
     const bool reflect = u_reflect > TransCoeff;
 
@@ -414,7 +414,7 @@ GBO_DEV int propagate_at_boundary(const Tables& t, Photon& p, const State& s, fl
         p.pol = TTx * A_trans + TTy * A_paral;
     }
     flag = reflect ? GBO_BOUNDARY_REFLECT : GBO_BOUNDARY_TRANSMIT;
-    if (t.debug_tag && reflect) { uniform(rng); uniform(rng); uniform(rng); uniform(rng); }
+    if (t.debug_tag && reflect) skip(rng, 4);
     return CMD_CONTINUE;
 }
 
@@ -437,7 +437,7 @@ GBO_DEV int propagate_at_surface(const Tables& t, Photon& p, const State& s, flo
     const float absorb = s.surface.y;
     const float reflect_diffuse_ = s.surface.w;
     const float u_surface = uniform(rng);
-    if (t.debug_tag) uniform(rng);
+    if (t.debug_tag) skip(rng, 1);
     const int action = u_surface < absorb + detect ? CMD_BREAK : CMD_CONTINUE;
     if (action == CMD_BREAK) {
         flag = u_surface < absorb ? GBO_SURFACE_ABSORB : GBO_SURFACE_DETECT;
@@ -487,7 +487,7 @@ GBO_DEV int propagate(const Tables& t, Photon& p, const Hit& h, Rng& rng)
         else if (ems == GBO_EMS_SURFACE) command = propagate_at_surface(t, p, s, h.normal, rng, flag);
         else if (h.lposcost < 0.f) command = propagate_at_surface(t, p, s, h.normal, rng, flag);
         else if (ems == GBO_EMS_ZPLUS_SENSOR_A) {
-            uniform(rng);
+            skip(rng, 1);
             flag = GBO_SURFACE_DETECT;
             command = CMD_BREAK;
         }

@@ -144,9 +144,9 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
             const float4* nq = reinterpret_cast<const float4*>(a.tlas + item);
             const float4 l0 = __ldg(nq), h0 = __ldg(nq + 1), l1 = __ldg(nq + 2), h1 = __ldg(nq + 3);
             float t0, t1;
-            const bool v0 = slab(l0, h0, pos, inv, tmin, b.t, t0);
-            const bool v1 = slab(l1, h1, pos, inv, tmin, b.t, t1);
             const int c0 = __float_as_int(h0.w), c1 = __float_as_int(h1.w);
+            const bool v0 = c0 >= 0 && slab(l0, h0, pos, inv, tmin, b.t, t0);
+            const bool v1 = c1 >= 0 && slab(l1, h1, pos, inv, tmin, b.t, t1);
             const int it0 = c0 > 0 ? leaf_item(__float_as_int(l0.w), c0) : __float_as_int(l0.w);
             const int it1 = c1 > 0 ? leaf_item(__float_as_int(l1.w), c1) : __float_as_int(l1.w);
             if (v0 && v1) {                         // nearer child next, the other on the stack

@@ -42,7 +42,13 @@ class Config(C.Structure):
                 ("rng_seed", C.c_uint64), ("rng_offset", C.c_uint64), ("event_skipahead", C.c_uint64),
                 ("tmax", C.c_float), ("debug_tag", C.c_int32), ("record_photon", C.c_int32),
                 ("record_seq", C.c_int32), ("max_photon", C.c_int64), ("kernel_mode", C.c_int32),
-                ("refill_min", C.c_int32), ("blocks_per_sm", C.c_int32), ("reserved", C.c_int32)]
+                ("refill_min", C.c_int32), ("blocks_per_sm", C.c_int32), ("refill_period", C.c_int32)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("kernel_mode", C.c_int32), ("refill_min", C.c_int32), ("refill_period", C.c_int32),
+                ("num_candidates", C.c_int32), ("cand_mode", C.c_int32 * 32), ("cand_refill", C.c_int32 * 32),
+                ("cand_period", C.c_int32 * 32), ("cand_ms", C.c_float * 32)]
 
 
 class Stats(C.Structure):
@@ -84,6 +90,8 @@ def load(path=LIB):
     lib.gbo_rng_sequence.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_void_p]
     lib.gbo_texture_lookup.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
     lib.gbo_scint_wavelength.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
+    lib.gbo_autotune.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
+                                 C.c_void_p]
     _lib = lib
     return lib
 
@@ -195,6 +203,19 @@ class Engine:
         s = Stats()
         _check(self.lib.gbo_get_stats(self.handle, C.byref(s)), "gbo_get_stats")
         return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def autotune(self, event_id, gensteps, input_photon=None, trials=2):
+        """Time every candidate kernel form on this sample event and keep the fastest (gbo_autotune)."""
+        gs = np.ascontiguousarray(gensteps, dtype=np.float32)
+        inp = np.ascontiguousarray(input_photon) if input_photon is not None else None
+        r = TuneResult()
+        _check(self.lib.gbo_autotune(self.handle, int(event_id), gs.ctypes.data_as(C.c_void_p), len(gs),
+                                     inp.ctypes.data_as(C.c_void_p) if inp is not None else None,
+                                     len(inp) if inp is not None else 0, int(trials), C.byref(r)), "gbo_autotune")
+        cands = [dict(mode=r.cand_mode[i], refill=r.cand_refill[i], period=r.cand_period[i], ms=r.cand_ms[i])
+                 for i in range(r.num_candidates)]
+        self.config.kernel_mode, self.config.refill_min, self.config.refill_period = r.kernel_mode, r.refill_min, r.refill_period
+        return dict(kernel_mode=r.kernel_mode, refill_min=r.refill_min, refill_period=r.refill_period, candidates=cands)
 
     def texture_lookup(self, which, xy):
         xy = np.ascontiguousarray(xy, dtype=np.float32)

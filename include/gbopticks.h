@@ -75,11 +75,18 @@ typedef struct gbo_config {
     int32_t  record_photon;         /* keep the full photon array of each event */
     int32_t  record_seq;            /* keep seqhis/seqbnd of each event */
     int64_t  max_photon;            /* capacity limit per event (0: no limit beyond device memory) */
-    int32_t  kernel_mode;           /* 0: persistent photon-pool kernel, 1: one thread per photon (default) */
-    int32_t  refill_min;            /* pool kernel: idle lanes a warp waits for before refilling (1..32, 32) */
+    int32_t  kernel_mode;           /* 0: persistent photon-pool kernel (default), 1: one thread per photon */
+    int32_t  refill_min;            /* pool kernel: idle lanes a warp waits for before refilling (1..32, 8) */
     int32_t  blocks_per_sm;         /* pool kernel: resident blocks per SM (0: occupancy maximum) */
-    int32_t  reserved;
+    int32_t  refill_period;         /* pool kernel: steps between refill checks (compaction period, >= 1) */
 } gbo_config;
+
+/* Result of gbo_autotune: the kernel form chosen and the simulate time of every candidate tried. */
+typedef struct gbo_tune_result {
+    int32_t kernel_mode, refill_min, refill_period, num_candidates;
+    int32_t cand_mode[32], cand_refill[32], cand_period[32];
+    float   cand_ms[32];
+} gbo_tune_result;
 
 typedef struct gbo_stats {
     int64_t num_photon;
@@ -107,6 +114,13 @@ const void* gbo_device_hits(const gbo_engine* e);
 int         gbo_reset(gbo_engine* e, int32_t event_id);
 int         gbo_get_stats(const gbo_engine* e, gbo_stats* out);
 const char* gbo_last_error(void);
+
+/* gbo_autotune : no counterpart in the reference (its launch shape is fixed by OptiX).  Runs the given sample
+ * event with every candidate kernel form (one thread per photon; photon pool with refill thresholds 1..32 and
+ * refill periods 1, 4), `trials` timed runs each after one warm-up, and keeps the fastest in the engine's config. */
+int         gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs,
+                         const gbo_sphoton* input_photon, int64_t num_input_photon, int32_t trials,
+                         gbo_tune_result* out);
 
 /* Known-answer entry points; the reference drives equivalent test kernels from QSimTest (qudarap/QSim.cu,
  * qudarap/tests/QSimTest.cc:700-770):
