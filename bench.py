@@ -204,6 +204,8 @@ def main():
     geom, gs = workload(seed=1 + rank, num_gs=args.gensteps)
     n_photon = int(gs.view(np.uint32)[:, 0, 3].astype(np.int64).sum())
     eng = E.Engine(geom, device=local)
+    # kernel form picked by the autotuner on a 10% sample of the workload (setup, outside the timed region)
+    tune = eng.autotune(0, gs[: max(1, len(gs) // 10)], trials=2)
 
     d_gs = torch.from_numpy(gs.copy()).to(f"cuda:{local}")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -275,6 +277,9 @@ def main():
         "dtype": "f32", "data": "synthetic (seeded numpy gensteps with the reference genstep layout)",
         "config": {"workload": WORKLOAD if args.gensteps == 2000 else WORKLOAD + "_%dgs" % args.gensteps, "photons_per_step": n_photon, "gensteps_per_step": len(gs),
                    "hits_per_step": hits, "path": "plain: one event per launch", "l2": "flushed (256 MB write) between timed steps",
+                   "kernel": {"mode": "photon pool" if tune["kernel_mode"] == 0 else "one thread per photon",
+                              "refill_min": tune["refill_min"], "refill_period": tune["refill_period"],
+                              "chosen_by": "autotuner on 10% sample"},
                    "max_bounce": 31, "parallelism": "replicas" if world > 1 else "1 GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

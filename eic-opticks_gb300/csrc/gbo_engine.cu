@@ -53,7 +53,16 @@ struct Params {
     gbo_sphoton* hit_unordered;
     unsigned long long* hit_count;
     uint32_t* bitmap;
+    // several events in one launch: event e owns gensteps [ev_gs_begin[e], ev_gs_begin[e+1]) and launch photons
+    // [ev_photon_begin[e], ev_photon_begin[e+1]); its photons use stream position ev_pos0[e] and event-local indices
+    int num_events;                         // 0: single event (photon_offset, position0 above)
+    const int* ev_gs_begin;
+    const unsigned long long* ev_photon_begin;
+    const unsigned long long* ev_pos0;
+    unsigned long long* hit_gidx;           // launch index of each unordered hit (batched launches)
 };
+
+GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng);
 
 template <bool TREE>
 __global__ void __launch_bounds__(SIM_BLOCK, GBO_SIM_MINB) k_simulate(const __grid_constant__ Params P)
@@ -63,34 +72,8 @@ __global__ void __launch_bounds__(SIM_BLOCK, GBO_SIM_MINB) k_simulate(const __gr
     Photon p;
     bool is_hit = false;
     if (active) {
-        int lo = 0, hi = P.num_gs - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (__ldg(P.gs_end + mid) > (unsigned long long)idx) hi = mid; else lo = mid + 1;
-        }
-        const float4* g = P.gs + 6 * (size_t)lo;
-        float4 gq[6];
-#pragma unroll
-        for (int k = 0; k < 6; k++) gq[k] = __ldg(g + k);
-        const unsigned long long photon_idx = P.photon_offset + (unsigned long long)idx;
-
         Rng rng;
-        rng_init(rng, P.seed, photon_idx, P.position0);
-
-        p.pos = f3(0.f, 0.f, 0.f); p.time = 0.f; p.mom = f3(0.f, 0.f, 0.f); p.hitcount_iindex = 0u;
-        p.pol = f3(0.f, 0.f, 0.f); p.wavelength = 0.f;
-        p.orient_boundary_flag = 0u; p.identity = 0u; p.index = 0u; p.flagmask = 0u;
-        const int gencode = __float_as_int(gq[0].x);
-        switch (gencode) {
-            case GBO_GS_TORCH: gen_torch(p, rng, gq, photon_idx); break;
-            case GBO_GS_CERENKOV:
-            case GBO_GS_G4Cerenkov_modified: gen_cerenkov(P.tab, p, rng, gq); break;
-            case GBO_GS_SCINTILLATION:
-            case GBO_GS_DsG4Scintillation_r4695: gen_scint(P.tab, p, rng, gq); break;
-            case GBO_GS_INPUT_PHOTON: load_photon(p, P.input_photon + idx); set_flag(p, GBO_TORCH); break;
-            default: break;
-        }
-        set_index(p, photon_idx);
+        generate(P, idx, p, rng);
 
         Seq seq;
         seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
@@ -125,7 +108,10 @@ __global__ void __launch_bounds__(SIM_BLOCK, GBO_SIM_MINB) k_simulate(const __gr
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(P.hit_count, (unsigned long long)__popc(mask));
         base = __shfl_sync(0xffffffffu, base, 0);
-        if (is_hit) store_photon(P.hit_unordered + base + __popc(mask & ((1u << lane) - 1u)), p);
+        if (is_hit) {
+            store_photon(P.hit_unordered + base + __popc(mask & ((1u << lane) - 1u)), p);
+            if (P.hit_gidx) P.hit_gidx[base + __popc(mask & ((1u << lane) - 1u))] = (unsigned long long)idx;
+        }
     }
 }
 
@@ -142,8 +128,18 @@ GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng)
     float4 gq[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) gq[k] = __ldg(g + k);
-    const unsigned long long photon_idx = P.photon_offset + (unsigned long long)idx;
-    rng_init(rng, P.seed, photon_idx, P.position0);
+    unsigned long long photon_idx = P.photon_offset + (unsigned long long)idx;
+    uint64_t pos0 = P.position0;
+    if (P.num_events > 0) {
+        int a = 0, z = P.num_events - 1;          // event owning genstep lo
+        while (a < z) {
+            const int m = (a + z + 1) >> 1;
+            if (__ldg(P.ev_gs_begin + m) <= lo) a = m; else z = m - 1;
+        }
+        photon_idx = (unsigned long long)idx - __ldg(P.ev_photon_begin + a);
+        pos0 = __ldg(P.ev_pos0 + a);
+    }
+    rng_init(rng, P.seed, photon_idx, pos0);
     p.pos = f3(0.f, 0.f, 0.f); p.time = 0.f; p.mom = f3(0.f, 0.f, 0.f); p.hitcount_iindex = 0u;
     p.pol = f3(0.f, 0.f, 0.f); p.wavelength = 0.f;
     p.orient_boundary_flag = 0u; p.identity = 0u; p.index = 0u; p.flagmask = 0u;
@@ -240,7 +236,10 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_pool(const __grid_consta
                 unsigned long long base = 0;
                 if ((int)lane == leader) base = atomicAdd(P.hit_count, (unsigned long long)__popc(hm));
                 base = __shfl_sync(0xffffffffu, base, leader);
-                if (is_hit) store_photon(P.hit_unordered + base + __popc(hm & lt), p);
+                if (is_hit) {
+                    store_photon(P.hit_unordered + base + __popc(hm & lt), p);
+                    if (P.hit_gidx) P.hit_gidx[base + __popc(hm & lt)] = (unsigned long long)idx;
+                }
             }
         }
     }
@@ -338,18 +337,34 @@ __global__ void k_gather_photons(const gbo_sphoton* photons, const uint32_t* bit
 // thread per unordered hit: its photon index gives the bitmap rank, i.e. its place in photon order
 __global__ void k_gather_unordered(const gbo_sphoton* unordered, const unsigned long long* count,
                                    unsigned long long photon_offset, const uint32_t* bitmap, const uint32_t* word_prefix,
-                                   const unsigned long long* block_offset, gbo_sphoton* hits)
+                                   const unsigned long long* block_offset, gbo_sphoton* hits,
+                                   const unsigned long long* gidx = nullptr)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if ((unsigned long long)i >= *count) return;
     const gbo_sphoton* src = unordered + i;
     const unsigned long long full = ((unsigned long long)(__ldg(&src->identity) >> 24) << 32) | __ldg(&src->index);
-    const unsigned long long rel = full - photon_offset;
+    const unsigned long long rel = gidx ? gidx[i] : full - photon_offset;
     const long long w = (long long)(rel >> 5);
     const unsigned j = (unsigned)(rel & 31u);
     const uint32_t m = bitmap[w];
     const unsigned long long rank = block_offset[w / SCAN_WORDS] + word_prefix[w] + __popc(m & ((1u << j) - 1u));
     copy_photon(hits + rank, src);
+}
+
+// hit rank of each event boundary photon: event e's hits are ordered hits [out[e], out[e+1])
+__global__ void k_event_hit_ranges(const unsigned long long* ev_photon_begin, int n_ev, long long num_photon,
+                                   const uint32_t* bitmap, const uint32_t* word_prefix,
+                                   const unsigned long long* block_offset, const unsigned long long* total_hits,
+                                   unsigned long long* out)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e > n_ev) return;
+    const unsigned long long j = ev_photon_begin[e];
+    if ((long long)j >= num_photon) { out[e] = *total_hits; return; }
+    const long long w = (long long)(j >> 5);
+    const unsigned b = (unsigned)(j & 31u);
+    out[e] = block_offset[w / SCAN_WORDS] + word_prefix[w] + __popc(bitmap[w] & ((1u << b) - 1u));
 }
 
 // ---- known-answer kernels (the reference keeps equivalents in qudarap/QSim.cu for QSimTest) -----------------
@@ -1192,3 +1207,5 @@ int gbo_simulate_noalloc(gbo_engine* e, int32_t event_id, const void* d_gs, int6
 }
 
 }  // extern "C"
+
+#include "gbo_serve.inl"

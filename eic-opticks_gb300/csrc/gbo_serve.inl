@@ -1,0 +1,450 @@
+// gbo_serve.inl : continuous-batching event server over one engine (included at the end of gbo_engine.cu).
+//
+// The reference runs one event at a time: G4CXOpticks::simulate uploads the gensteps, launches, synchronises and
+// gathers hits before returning (qudarap/QSim.cc:428-631, CSGOptiX/CSGOptiX.cc:1172-1174); its service layer
+// (CSGOptiX/CSGOptiXService.h) serves one request at a time.  Here producer threads submit events and go on; a
+// worker thread packs whatever events are waiting into one launch (every photon of every packed event in one
+// simulate kernel, events kept apart by their genstep and photon ranges), runs up to `slots` such batches at once
+// on separate CUDA streams so a new batch fills the SMs that the previous one's tail leaves idle, admits events
+// only while the batch's device buffers fit the HBM budget, and hands back each event's hits in photon order with
+// its submit-to-hits latency.  Each event's results are those it gets alone: its photons keep their event-local
+// indices and the event's own Philox stream positions.
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <thread>
+#include <unordered_map>
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct ServerEvent {
+    uint64_t ticket = 0;
+    int32_t event_id = 0;
+    std::vector<gbo_quad6> gs;
+    std::vector<gbo_sphoton> input;
+    long long num_photon = 0;
+    Clock::time_point t_submit, t_done;
+    int status = 0;             // 0 waiting, 1 on the GPU, 2 done, 3 failed
+    std::vector<gbo_sphoton> hits;
+    std::string error;
+};
+
+template <typename T>
+struct HBuf {                   // pinned host staging
+    T* ptr = nullptr;
+    size_t cap = 0;
+    int ensure(size_t n)
+    {
+        if (n <= cap && ptr) return 0;
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        cap = 0;
+        size_t want = n < 1 ? 1 : n;
+        if (cudaMallocHost(&ptr, want * sizeof(T)) != cudaSuccess) { ptr = nullptr; return fail(GBO_ERR_CUDA, "cudaMallocHost failed"); }
+        cap = want;
+        return 0;
+    }
+    void release() { if (ptr) cudaFreeHost(ptr); ptr = nullptr; cap = 0; }
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_kernels = nullptr, ev_done = nullptr;
+    int phase = 0;              // 0 idle, 1 kernels running, 2 hit download running
+    std::vector<std::shared_ptr<ServerEvent>> events;
+    long long num_photon = 0;
+    unsigned long long num_hit = 0;
+    DBuf<gbo_quad6> gs;
+    DBuf<unsigned long long> gs_end, ev_photon_begin, ev_pos0, block_offset, counters, hit_gidx, ev_hit;
+    DBuf<int> ev_gs_begin;
+    DBuf<gbo_sphoton> input, hits_unordered, hits;
+    DBuf<uint32_t> bitmap, word_prefix, block_sum;
+    HBuf<gbo_quad6> h_gs;
+    HBuf<unsigned long long> h_gs_end, h_ev_photon_begin, h_ev_pos0, h_ev_hit, h_counters;
+    HBuf<int> h_ev_gs_begin;
+    HBuf<gbo_sphoton> h_input, h_hits;
+
+    void release()
+    {
+        gs.release(); gs_end.release(); ev_photon_begin.release(); ev_pos0.release(); block_offset.release();
+        counters.release(); hit_gidx.release(); ev_hit.release(); ev_gs_begin.release(); input.release();
+        hits_unordered.release(); hits.release(); bitmap.release(); word_prefix.release(); block_sum.release();
+        h_gs.release(); h_gs_end.release(); h_ev_photon_begin.release(); h_ev_pos0.release(); h_ev_hit.release();
+        h_counters.release(); h_ev_gs_begin.release(); h_input.release(); h_hits.release();
+        if (ev_kernels) cudaEventDestroy(ev_kernels);
+        if (ev_done) cudaEventDestroy(ev_done);
+        if (stream) cudaStreamDestroy(stream);
+        ev_kernels = ev_done = nullptr;
+        stream = nullptr;
+    }
+};
+
+// device bytes per photon slot of a batch: bitmap + prefix bits, unordered + ordered hit capacity, hit index
+constexpr double SERVE_BYTES_PER_PHOTON = 0.25 + 64.0 + 64.0 + 8.0;
+
+}  // namespace
+
+struct gbo_server {
+    gbo_engine* e = nullptr;
+    gbo_server_config cfg{};
+    long long max_batch_photon = 0;
+    std::vector<Slot> slots;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<ServerEvent>> pending;
+    std::unordered_map<uint64_t, std::shared_ptr<ServerEvent>> events;
+    bool stop = false;
+    uint64_t next_ticket = 1;
+    gbo_server_stats stats{};
+};
+
+namespace {
+
+int launch_batch(gbo_server* sv, Slot& sl)
+{
+    gbo_engine* e = sv->e;
+    cudaStream_t s = sl.stream;
+    const int n_ev = (int)sl.events.size();
+    long long n_gs = 0, n_input = 0;
+    for (auto& ev : sl.events) { n_gs += (long long)ev->gs.size(); n_input += (long long)ev->input.size(); }
+    int rc;
+    if ((rc = sl.h_gs.ensure(n_gs)) || (rc = sl.h_gs_end.ensure(n_gs)) || (rc = sl.h_ev_gs_begin.ensure(n_ev + 1)) ||
+        (rc = sl.h_ev_photon_begin.ensure(n_ev + 1)) || (rc = sl.h_ev_pos0.ensure(n_ev)) ||
+        (rc = sl.h_ev_hit.ensure(n_ev + 1)) || (rc = sl.h_counters.ensure(4)) || (rc = sl.h_input.ensure(n_input)))
+        return rc;
+    long long g = 0, p = 0, ip = 0;
+    unsigned long long total = 0;
+    for (int k = 0; k < n_ev; k++) {
+        ServerEvent& ev = *sl.events[k];
+        sl.h_ev_gs_begin.ptr[k] = (int)g;
+        sl.h_ev_photon_begin.ptr[k] = (unsigned long long)p;
+        sl.h_ev_pos0.ptr[k] = e->cfg.rng_offset + e->cfg.event_skipahead * (uint64_t)(ev.event_id < 0 ? 0 : ev.event_id);
+        for (const gbo_quad6& q : ev.gs) {
+            sl.h_gs.ptr[g] = q;
+            total += q.q[0].u[3];
+            sl.h_gs_end.ptr[g] = total;
+            g++;
+        }
+        if (!ev.input.empty()) std::memcpy(sl.h_input.ptr + ip, ev.input.data(), ev.input.size() * sizeof(gbo_sphoton));
+        ip += (long long)ev.input.size();
+        p = (long long)total;
+    }
+    sl.h_ev_gs_begin.ptr[n_ev] = (int)g;
+    sl.h_ev_photon_begin.ptr[n_ev] = total;
+    const long long N = (long long)total;
+    sl.num_photon = N;
+    const long long words = (N + 31) / 32;
+    const long long nblk = (words + SCAN_WORDS - 1) / SCAN_WORDS;
+    if ((rc = sl.gs.ensure(n_gs)) || (rc = sl.gs_end.ensure(n_gs)) || (rc = sl.ev_gs_begin.ensure(n_ev + 1)) ||
+        (rc = sl.ev_photon_begin.ensure(n_ev + 1)) || (rc = sl.ev_pos0.ensure(n_ev)) || (rc = sl.ev_hit.ensure(n_ev + 1)) ||
+        (rc = sl.counters.ensure(4)) || (rc = sl.bitmap.ensure(words)) || (rc = sl.word_prefix.ensure(words)) ||
+        (rc = sl.block_sum.ensure(nblk)) || (rc = sl.block_offset.ensure(nblk)) || (rc = sl.hits_unordered.ensure(N)) ||
+        (rc = sl.hit_gidx.ensure(N)) || (rc = sl.hits.ensure(N)) || (rc = sl.input.ensure(n_input)))
+        return rc;
+    CU(cudaMemcpyAsync(sl.gs.ptr, sl.h_gs.ptr, n_gs * sizeof(gbo_quad6), cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(sl.gs_end.ptr, sl.h_gs_end.ptr, n_gs * sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(sl.ev_gs_begin.ptr, sl.h_ev_gs_begin.ptr, (n_ev + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(sl.ev_photon_begin.ptr, sl.h_ev_photon_begin.ptr, (n_ev + 1) * sizeof(unsigned long long),
+                       cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(sl.ev_pos0.ptr, sl.h_ev_pos0.ptr, n_ev * sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
+    if (n_input) CU(cudaMemcpyAsync(sl.input.ptr, sl.h_input.ptr, n_input * sizeof(gbo_sphoton), cudaMemcpyHostToDevice, s));
+    CU(cudaMemsetAsync(sl.counters.ptr, 0, 4 * sizeof(unsigned long long), s));
+
+    Params P = make_params(e);
+    P.gs = reinterpret_cast<const float4*>(sl.gs.ptr);
+    P.gs_end = sl.gs_end.ptr;
+    P.num_gs = (int)n_gs;
+    P.num_photon = N;
+    P.input_photon = n_input ? sl.input.ptr : nullptr;
+    P.hit_unordered = sl.hits_unordered.ptr;
+    P.hit_count = sl.counters.ptr;
+    P.bitmap = sl.bitmap.ptr;
+    P.num_events = n_ev;
+    P.ev_gs_begin = sl.ev_gs_begin.ptr;
+    P.ev_photon_begin = sl.ev_photon_begin.ptr;
+    P.ev_pos0 = sl.ev_pos0.ptr;
+    P.hit_gidx = sl.hit_gidx.ptr;
+    if (N > 0) {
+        if (e->cfg.kernel_mode == 0) {
+            CU(cudaMemsetAsync(sl.bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
+            const long long need = (N + SIM_BLOCK - 1) / SIM_BLOCK;
+            const long long grid = need < e->pool_grid[e->has_tree] ? need : e->pool_grid[e->has_tree];
+            const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
+            const int period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
+            if (e->has_tree) k_simulate_pool<true><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, sl.counters.ptr + 2, refill, period);
+            else k_simulate_pool<false><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, sl.counters.ptr + 2, refill, period);
+        } else {
+            const long long blocks = (N + SIM_BLOCK - 1) / SIM_BLOCK;
+            if (e->has_tree) k_simulate<true><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
+            else k_simulate<false><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
+        }
+        CU(cudaGetLastError());
+        k_word_prefix<<<(unsigned)nblk, SCAN_WORDS, 0, s>>>(sl.bitmap.ptr, words, sl.word_prefix.ptr, sl.block_sum.ptr);
+        k_block_offsets<<<1, 1024, 0, s>>>(sl.block_sum.ptr, nblk, sl.block_offset.ptr, sl.counters.ptr + 1);
+        k_gather_unordered<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(sl.hits_unordered.ptr, sl.counters.ptr, 0ull,
+                                                                       sl.bitmap.ptr, sl.word_prefix.ptr,
+                                                                       sl.block_offset.ptr, sl.hits.ptr, sl.hit_gidx.ptr);
+        k_event_hit_ranges<<<(n_ev + 1 + 127) / 128, 128, 0, s>>>(sl.ev_photon_begin.ptr, n_ev, N, sl.bitmap.ptr,
+                                                                  sl.word_prefix.ptr, sl.block_offset.ptr,
+                                                                  sl.counters.ptr + 1, sl.ev_hit.ptr);
+        CU(cudaGetLastError());
+        CU(cudaMemcpyAsync(sl.h_ev_hit.ptr, sl.ev_hit.ptr, (n_ev + 1) * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    } else {
+        for (int k = 0; k <= n_ev; k++) sl.h_ev_hit.ptr[k] = 0;
+    }
+    CU(cudaMemcpyAsync(sl.h_counters.ptr, sl.counters.ptr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CU(cudaEventRecord(sl.ev_kernels, s));
+    sl.phase = 1;
+    return GBO_OK;
+}
+
+void finish_slot(gbo_server* sv, Slot& sl, int rc)
+{
+    std::lock_guard<std::mutex> lock(sv->mu);
+    const Clock::time_point now = Clock::now();
+    for (size_t k = 0; k < sl.events.size(); k++) {
+        ServerEvent& ev = *sl.events[k];
+        if (rc == GBO_OK) {
+            const unsigned long long a = sl.h_ev_hit.ptr[k], b = sl.h_ev_hit.ptr[k + 1];
+            ev.hits.assign(sl.h_hits.ptr + a, sl.h_hits.ptr + b);
+            ev.status = 2;
+        } else {
+            ev.status = 3;
+            ev.error = g_last_error;
+        }
+        ev.t_done = now;
+        sv->stats.events_done++;
+    }
+    sv->stats.batches++;
+    sv->stats.photons += sl.num_photon;
+    sl.events.clear();
+    sl.phase = 0;
+    sv->cv_done.notify_all();
+}
+
+void serve_loop(gbo_server* sv)
+{
+    cudaSetDevice(sv->e->device);
+    for (;;) {
+        bool busy = false;
+        for (Slot& sl : sv->slots) {
+            if (sl.phase == 1) {
+                busy = true;
+                cudaError_t q = cudaEventQuery(sl.ev_kernels);
+                if (q == cudaErrorNotReady) continue;
+                if (q != cudaSuccess) { fail(GBO_ERR_CUDA, "batch failed: %s", cudaGetErrorString(q)); finish_slot(sv, sl, GBO_ERR_CUDA); continue; }
+                sl.num_hit = sl.h_counters.ptr[1];
+                int rc = sl.h_hits.ensure(sl.num_hit);
+                if (!rc && sl.num_hit &&
+                    cudaMemcpyAsync(sl.h_hits.ptr, sl.hits.ptr, sl.num_hit * sizeof(gbo_sphoton), cudaMemcpyDeviceToHost,
+                                    sl.stream) != cudaSuccess)
+                    rc = fail(GBO_ERR_CUDA, "hit download failed");
+                if (!rc && cudaEventRecord(sl.ev_done, sl.stream) != cudaSuccess) rc = fail(GBO_ERR_CUDA, "event record failed");
+                if (rc) { finish_slot(sv, sl, rc); continue; }
+                sl.phase = 2;
+            } else if (sl.phase == 2) {
+                busy = true;
+                cudaError_t q = cudaEventQuery(sl.ev_done);
+                if (q == cudaErrorNotReady) continue;
+                finish_slot(sv, sl, q == cudaSuccess ? GBO_OK : fail(GBO_ERR_CUDA, "hit download: %s", cudaGetErrorString(q)));
+            }
+        }
+        // admit waiting events into idle slots
+        for (Slot& sl : sv->slots) {
+            if (sl.phase != 0) continue;
+            {
+                std::lock_guard<std::mutex> lock(sv->mu);
+                long long photons = 0;
+                while (!sv->pending.empty()) {
+                    auto& ev = sv->pending.front();
+                    if (!sl.events.empty() && (photons + ev->num_photon > sv->max_batch_photon ||
+                                               (int)sl.events.size() >= sv->cfg.max_batch_events))
+                        break;
+                    photons += ev->num_photon;
+                    ev->status = 1;
+                    sl.events.push_back(ev);
+                    sv->pending.pop_front();
+                }
+            }
+            if (sl.events.empty()) continue;
+            busy = true;
+            int rc = launch_batch(sv, sl);
+            if (rc) finish_slot(sv, sl, rc);
+        }
+        std::unique_lock<std::mutex> lock(sv->mu);
+        if (sv->stop && sv->pending.empty()) {
+            bool idle = true;
+            for (Slot& sl : sv->slots) idle = idle && sl.phase == 0;
+            if (idle) break;
+        }
+        if (busy) {
+            lock.unlock();
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+        } else {
+            sv->cv_work.wait_for(lock, std::chrono::milliseconds(2));
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbo_server_config_default(gbo_server_config* c)
+{
+    if (!c) return fail(GBO_ERR_ARG, "gbo_server_config_default: null config");
+    std::memset(c, 0, sizeof(*c));
+    c->slots = 2;
+    c->max_batch_photon = 16ll << 20;
+    c->hbm_budget_bytes = 120ll << 30;
+    c->max_batch_events = 4096;
+    return GBO_OK;
+}
+
+int gbo_server_create(gbo_engine* e, const gbo_server_config* cfg, gbo_server** out)
+{
+    if (!e || !out) return fail(GBO_ERR_ARG, "gbo_server_create: null argument");
+    *out = nullptr;
+    gbo_server_config c;
+    if (cfg) c = *cfg; else gbo_server_config_default(&c);
+    if (c.slots < 1 || c.slots > 8) return fail(GBO_ERR_ARG, "gbo_server_create: slots %d not in 1..8", c.slots);
+    if (c.max_batch_events < 1) return fail(GBO_ERR_ARG, "gbo_server_create: max_batch_events must be positive");
+    CU(cudaSetDevice(e->device));
+    auto* sv = new gbo_server();
+    sv->e = e;
+    sv->cfg = c;
+    const long long by_budget = (long long)((double)c.hbm_budget_bytes / (SERVE_BYTES_PER_PHOTON * c.slots));
+    sv->max_batch_photon = c.max_batch_photon > 0 && c.max_batch_photon < by_budget ? c.max_batch_photon : by_budget;
+    if (sv->max_batch_photon < 1) { delete sv; return fail(GBO_ERR_CAPACITY, "gbo_server_create: HBM budget below one photon per slot"); }
+    sv->slots.resize((size_t)c.slots);
+    for (Slot& sl : sv->slots) {
+        if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sl.ev_kernels, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sl.ev_done, cudaEventDisableTiming) != cudaSuccess) {
+            for (Slot& x : sv->slots) x.release();
+            delete sv;
+            return fail(GBO_ERR_CUDA, "gbo_server_create: stream/event creation failed");
+        }
+    }
+    sv->worker = std::thread(serve_loop, sv);
+    *out = sv;
+    return GBO_OK;
+}
+
+int gbo_server_submit(gbo_server* sv, int32_t event_id, const gbo_quad6* gs, int64_t num_gs, const gbo_sphoton* input_photon,
+                      int64_t num_input_photon, uint64_t* ticket)
+{
+    if (!sv || !ticket) return fail(GBO_ERR_ARG, "gbo_server_submit: null argument");
+    if (num_gs < 0 || (num_gs > 0 && !gs)) return fail(GBO_ERR_ARG, "gbo_server_submit: bad gensteps");
+    if (num_input_photon < 0 || (num_input_photon > 0 && !input_photon)) return fail(GBO_ERR_ARG, "gbo_server_submit: bad input photons");
+    auto ev = std::make_shared<ServerEvent>();
+    ev->event_id = event_id;
+    ev->gs.assign(gs, gs + num_gs);
+    if (num_input_photon) ev->input.assign(input_photon, input_photon + num_input_photon);
+    long long n = 0;
+    bool has_input_gs = false;
+    for (const gbo_quad6& q : ev->gs) { n += q.q[0].u[3]; has_input_gs |= q.q[0].i[0] == GBO_GS_INPUT_PHOTON; }
+    if (has_input_gs && num_input_photon < n)
+        return fail(GBO_ERR_ARG, "gbo_server_submit: INPUT_PHOTON gensteps need %lld photons, %lld given", n, (long long)num_input_photon);
+    if (n > sv->max_batch_photon)
+        return fail(GBO_ERR_CAPACITY, "gbo_server_submit: event of %lld photons above the batch limit %lld", n, sv->max_batch_photon);
+    ev->num_photon = n;
+    ev->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lock(sv->mu);
+        if (sv->stop) return fail(GBO_ERR_STATE, "gbo_server_submit: server stopping");
+        ev->ticket = sv->next_ticket++;
+        sv->events[ev->ticket] = ev;
+        sv->pending.push_back(ev);
+        sv->stats.events_submitted++;
+    }
+    sv->cv_work.notify_one();
+    *ticket = ev->ticket;
+    return GBO_OK;
+}
+
+int gbo_server_wait(gbo_server* sv, uint64_t ticket, int64_t timeout_us)
+{
+    if (!sv) return fail(GBO_ERR_ARG, "gbo_server_wait: null server");
+    std::unique_lock<std::mutex> lock(sv->mu);
+    auto it = sv->events.find(ticket);
+    if (it == sv->events.end()) return fail(GBO_ERR_ARG, "gbo_server_wait: unknown ticket %llu", (unsigned long long)ticket);
+    std::shared_ptr<ServerEvent> ev = it->second;
+    auto done = [&] { return ev->status >= 2; };
+    if (timeout_us < 0) sv->cv_done.wait(lock, done);
+    else if (!sv->cv_done.wait_for(lock, std::chrono::microseconds(timeout_us), done))
+        return fail(GBO_ERR_TIMEOUT, "gbo_server_wait: event %llu not done", (unsigned long long)ticket);
+    if (ev->status == 3) return fail(GBO_ERR_DEVICE, "event %llu failed: %s", (unsigned long long)ticket, ev->error.c_str());
+    return GBO_OK;
+}
+
+int gbo_server_event_info(gbo_server* sv, uint64_t ticket, int64_t* num_photon, int64_t* num_hit, double* latency_s)
+{
+    if (!sv) return fail(GBO_ERR_ARG, "gbo_server_event_info: null server");
+    std::lock_guard<std::mutex> lock(sv->mu);
+    auto it = sv->events.find(ticket);
+    if (it == sv->events.end()) return fail(GBO_ERR_ARG, "gbo_server_event_info: unknown ticket");
+    ServerEvent& ev = *it->second;
+    if (ev.status < 2) return fail(GBO_ERR_STATE, "gbo_server_event_info: event not done");
+    if (num_photon) *num_photon = ev.num_photon;
+    if (num_hit) *num_hit = (int64_t)ev.hits.size();
+    if (latency_s) *latency_s = std::chrono::duration<double>(ev.t_done - ev.t_submit).count();
+    return GBO_OK;
+}
+
+int gbo_server_copy_hits(gbo_server* sv, uint64_t ticket, gbo_sphoton* dst, int64_t offset, int64_t count)
+{
+    if (!sv || (!dst && count > 0)) return fail(GBO_ERR_ARG, "gbo_server_copy_hits: null argument");
+    std::lock_guard<std::mutex> lock(sv->mu);
+    auto it = sv->events.find(ticket);
+    if (it == sv->events.end()) return fail(GBO_ERR_ARG, "gbo_server_copy_hits: unknown ticket");
+    ServerEvent& ev = *it->second;
+    if (ev.status != 2) return fail(GBO_ERR_STATE, "gbo_server_copy_hits: event not done");
+    if (offset < 0 || count < 0 || offset + count > (int64_t)ev.hits.size()) return fail(GBO_ERR_ARG, "gbo_server_copy_hits: range outside hits");
+    if (count) std::memcpy(dst, ev.hits.data() + offset, (size_t)count * sizeof(gbo_sphoton));
+    return GBO_OK;
+}
+
+int gbo_server_release(gbo_server* sv, uint64_t ticket)
+{
+    if (!sv) return fail(GBO_ERR_ARG, "gbo_server_release: null server");
+    std::lock_guard<std::mutex> lock(sv->mu);
+    auto it = sv->events.find(ticket);
+    if (it == sv->events.end()) return fail(GBO_ERR_ARG, "gbo_server_release: unknown ticket");
+    if (it->second->status < 2) return fail(GBO_ERR_STATE, "gbo_server_release: event still in flight");
+    sv->events.erase(it);
+    return GBO_OK;
+}
+
+int gbo_server_get_stats(gbo_server* sv, gbo_server_stats* out)
+{
+    if (!sv || !out) return fail(GBO_ERR_ARG, "gbo_server_get_stats: null argument");
+    std::lock_guard<std::mutex> lock(sv->mu);
+    *out = sv->stats;
+    out->max_batch_photon = sv->max_batch_photon;
+    return GBO_OK;
+}
+
+void gbo_server_destroy(gbo_server* sv)
+{
+    if (!sv) return;
+    {
+        std::lock_guard<std::mutex> lock(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv_work.notify_all();
+    if (sv->worker.joinable()) sv->worker.join();
+    cudaSetDevice(sv->e->device);
+    for (Slot& sl : sv->slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        sl.release();
+    }
+    delete sv;
+}
+
+}  // extern "C"

@@ -232,6 +232,97 @@ class Engine:
         return out
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("max_batch_events", C.c_int32), ("max_batch_photon", C.c_int64),
+                ("hbm_budget_bytes", C.c_int64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("events_submitted", C.c_int64), ("events_done", C.c_int64), ("batches", C.c_int64),
+                ("photons", C.c_int64), ("max_batch_photon", C.c_int64)]
+
+
+def _server_protos(lib):
+    if getattr(lib, "_server_protos", False):
+        return
+    lib.gbo_server_config_default.argtypes = [C.POINTER(ServerConfig)]
+    lib.gbo_server_create.argtypes = [C.c_void_p, C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]
+    lib.gbo_server_submit.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                      C.POINTER(C.c_uint64)]
+    lib.gbo_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_int64]
+    lib.gbo_server_event_info.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                          C.POINTER(C.c_double)]
+    lib.gbo_server_copy_hits.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p, C.c_int64, C.c_int64]
+    lib.gbo_server_release.argtypes = [C.c_void_p, C.c_uint64]
+    lib.gbo_server_get_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+    lib.gbo_server_destroy.argtypes = [C.c_void_p]
+    lib._server_protos = True
+
+
+class Server:
+    """Continuous-batching event server over an Engine (gbo_server_*): submit from any thread, wait, fetch hits."""
+
+    def __init__(self, engine, **cfg):
+        self.lib = engine.lib
+        _server_protos(self.lib)
+        c = ServerConfig()
+        _check(self.lib.gbo_server_config_default(C.byref(c)), "gbo_server_config_default")
+        for k, v in cfg.items():
+            setattr(c, k, v)
+        h = C.c_void_p()
+        _check(self.lib.gbo_server_create(engine.handle, C.byref(c), C.byref(h)), "gbo_server_create")
+        self.handle = h
+        self.engine = engine
+
+    def submit(self, event_id, gensteps, input_photon=None):
+        gs = np.ascontiguousarray(gensteps, dtype=np.float32)
+        inp = np.ascontiguousarray(input_photon) if input_photon is not None else None
+        t = C.c_uint64()
+        _check(self.lib.gbo_server_submit(self.handle, int(event_id), gs.ctypes.data_as(C.c_void_p), len(gs),
+                                          inp.ctypes.data_as(C.c_void_p) if inp is not None else None,
+                                          len(inp) if inp is not None else 0, C.byref(t)), "gbo_server_submit")
+        return t.value
+
+    def wait(self, ticket, timeout_us=-1):
+        rc = self.lib.gbo_server_wait(self.handle, C.c_uint64(ticket), int(timeout_us))
+        if rc == 6:
+            return False
+        _check(rc, "gbo_server_wait")
+        return True
+
+    def info(self, ticket):
+        n, h, lat = C.c_int64(), C.c_int64(), C.c_double()
+        _check(self.lib.gbo_server_event_info(self.handle, C.c_uint64(ticket), C.byref(n), C.byref(h), C.byref(lat)),
+               "gbo_server_event_info")
+        return dict(num_photon=n.value, num_hit=h.value, latency_s=lat.value)
+
+    def hits(self, ticket):
+        n = self.info(ticket)["num_hit"]
+        out = np.zeros(n, dtype=L.PHOTON)
+        _check(self.lib.gbo_server_copy_hits(self.handle, C.c_uint64(ticket), out.ctypes.data_as(C.c_void_p), 0, n),
+               "gbo_server_copy_hits")
+        return out
+
+    def release(self, ticket):
+        _check(self.lib.gbo_server_release(self.handle, C.c_uint64(ticket)), "gbo_server_release")
+
+    def stats(self):
+        s = ServerStats()
+        _check(self.lib.gbo_server_get_stats(self.handle, C.byref(s)), "gbo_server_get_stats")
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.gbo_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class SEvt:
     """Genstep / input-photon collection and hit download, shaped like sysrap/SEvt's static API."""
 

@@ -39,7 +39,8 @@ enum {
     GBO_ERR_CUDA = 2,       /* a CUDA runtime call failed */
     GBO_ERR_STATE = 3,      /* call out of order (e.g. hits requested before any simulate) */
     GBO_ERR_CAPACITY = 4,   /* request above a configured or fixed limit */
-    GBO_ERR_DEVICE = 5      /* a kernel reported an error through its status word */
+    GBO_ERR_DEVICE = 5,     /* a kernel reported an error through its status word, or a served event failed */
+    GBO_ERR_TIMEOUT = 6     /* gbo_server_wait ran out of time; the event is still in flight */
 };
 
 typedef struct gbo_engine gbo_engine;
@@ -133,6 +134,36 @@ int         gbo_rng_sequence(int device, uint64_t seed, uint64_t subsequence0, u
                              int32_t per_seq, float* out);
 int         gbo_texture_lookup(gbo_engine* e, int32_t which, const float* xy, int32_t n, float* out);
 int         gbo_scint_wavelength(gbo_engine* e, const float* u, int32_t n, float* out);
+
+/* ---- event server (continuous batching) ----------------------------------------------------------------------
+ * The reference simulates one event per synchronous call (G4CXOpticks::simulate, g4cx/G4CXOpticks.cc:466-486;
+ * its service layer CSGOptiX/CSGOptiXService.h answers one request at a time).  The server replaces that call for
+ * multi-threaded producers: gbo_server_submit copies an event's gensteps (and input photons) and returns a ticket
+ * at once (thread-safe); a worker thread packs waiting events into one simulate launch, runs up to `slots` launches
+ * at once on separate streams, admits events while the launches' device buffers fit hbm_budget_bytes, and keeps
+ * each finished event's hits on the host until gbo_server_release.  Results equal those of gbo_simulate for the
+ * same event id. */
+typedef struct gbo_server gbo_server;
+typedef struct gbo_server_config {
+    int32_t slots;                  /* launches in flight at once (1..8, 2) */
+    int32_t max_batch_events;       /* events per launch (4096) */
+    int64_t max_batch_photon;       /* photons per launch (16M); also bounded by the budget */
+    int64_t hbm_budget_bytes;       /* device memory the server's launches may hold (120 GB) */
+} gbo_server_config;
+typedef struct gbo_server_stats {
+    int64_t events_submitted, events_done, batches, photons, max_batch_photon;
+} gbo_server_stats;
+
+int  gbo_server_config_default(gbo_server_config* cfg);
+int  gbo_server_create(gbo_engine* e, const gbo_server_config* cfg, gbo_server** out);
+int  gbo_server_submit(gbo_server* s, int32_t event_id, const gbo_quad6* gs, int64_t num_gs,
+                       const gbo_sphoton* input_photon, int64_t num_input_photon, uint64_t* ticket);
+int  gbo_server_wait(gbo_server* s, uint64_t ticket, int64_t timeout_us);          /* <0 : wait without limit */
+int  gbo_server_event_info(gbo_server* s, uint64_t ticket, int64_t* num_photon, int64_t* num_hit, double* latency_s);
+int  gbo_server_copy_hits(gbo_server* s, uint64_t ticket, gbo_sphoton* dst, int64_t offset, int64_t count);
+int  gbo_server_release(gbo_server* s, uint64_t ticket);
+int  gbo_server_get_stats(gbo_server* s, gbo_server_stats* out);
+void gbo_server_destroy(gbo_server* s);
 
 /* gbo_simulate_noalloc : has no counterpart in the reference.  One event like gbo_simulate_device, for callers
  * that may not allocate device memory while events run (memory reserved up front by another runtime, or event
