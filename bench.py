@@ -165,6 +165,120 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+def mixed_events(num_events, seed=11, lo=3.0, hi=7.0):
+    """Serving workload: events drawn 50/50 from the crystal-array scintillation and water Cerenkov generators,
+    photons per event log-uniform in [10^lo, 10^hi]."""
+    ge.load_package()
+    from eic_opticks_gb300 import geometry as G, gensteps as GS
+    rng = np.random.default_rng(seed)
+    wc = G.water_cube()
+    ca = G.crystal_array()
+    events = []
+    for k in range(num_events):
+        photons = int(10 ** rng.uniform(lo, hi))
+        if rng.uniform() < 0.5:
+            gs = GS.crystal_scint_gensteps(max(1, photons // 5000), min(5000, photons), seed=5000 + k)
+            events.append(("crystal", 10000 + k, gs))
+        else:
+            gs = GS.water_cerenkov_gensteps(wc, max(1, photons // 100), seed=7000 + k)
+            events.append(("water", 10000 + k, gs))
+    return {"crystal": ca.arrays(), "water": wc.arrays()}, events
+
+
+def pct(v, q):
+    return float(np.percentile(np.asarray(v), q)) if len(v) else None
+
+
+def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
+    """Plain one-launch-per-event path vs the continuous-batching server on the mixed serving workload.
+
+    * plain capacity: events processed one synchronous gbo_simulate call at a time (the reference's way);
+    * batched capacity: every event submitted at once from `submitters` threads, server drains them;
+    * latency under load: Poisson arrivals at `load` x the plain capacity, from `submitters` threads, for both
+      paths (the plain path serves arrivals first-come first-served with one call at a time).
+    """
+    import threading
+    from eic_opticks_gb300 import engine as E
+    arrays, events = mixed_events(num_events, lo=lo, hi=hi)
+    engines = {k: E.Engine(a) for k, a in arrays.items()}
+    photons = {id(ev[2]): int(ev[2].view(np.uint32)[:, 0, 3].astype(np.int64).sum()) for ev in events}
+    total_photons = sum(photons.values())
+    for kind, eid, gs in events[:4]:                          # warm-up
+        engines[kind].simulate(eid, gs)
+    # ---- plain capacity (closed loop)
+    t0 = time.perf_counter()
+    for kind, eid, gs in events:
+        engines[kind].simulate(eid, gs)
+        engines[kind].hits()
+    plain_s = time.perf_counter() - t0
+    plain_rate = total_photons / plain_s
+    servers = {k: E.Server(e, slots=2) for k, e in engines.items()}
+
+    def run_batched(arrivals):
+        tickets = [None] * len(events)
+        start = time.perf_counter()
+
+        def producer(idx):
+            for i in idx:
+                if arrivals is not None:
+                    delay = start + arrivals[i] - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                kind, eid, gs = events[i]
+                tickets[i] = (kind, servers[kind].submit(eid, gs))
+
+        th = [threading.Thread(target=producer, args=(range(j, len(events), submitters),)) for j in range(submitters)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        lat = []
+        for kind, t in tickets:
+            servers[kind].wait(t)
+        elapsed = time.perf_counter() - start
+        for kind, t in tickets:
+            lat.append(servers[kind].info(t)["latency_s"])
+            servers[kind].release(t)
+        return elapsed, lat
+
+    run_batched(None)                                       # warm-up of the server buffers
+    batched_s, _ = run_batched(None)
+    batched_rate = total_photons / batched_s
+    # ---- latency at `load` x plain capacity, Poisson arrivals
+    mean_photons = total_photons / len(events)
+    rate_events = load * plain_rate / mean_photons
+    rng = np.random.default_rng(3)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_events, len(events)))
+    _, lat_b = run_batched(arrivals)
+    # plain path on the same arrivals: one call at a time, first come first served
+    lat_p = []
+    start = time.perf_counter()
+    for i in np.argsort(arrivals):
+        kind, eid, gs = events[i]
+        now = time.perf_counter() - start
+        if now < arrivals[i]:
+            time.sleep(arrivals[i] - now)
+        engines[kind].simulate(eid, gs)
+        engines[kind].hits()
+        lat_p.append(time.perf_counter() - start - arrivals[i])
+    stats = {k: s.stats() for k, s in servers.items()}
+    for s in servers.values():
+        s.close()
+    for e in engines.values():
+        e.close()
+    return {
+        "workload": "mixed 50/50 crystal-array scintillation / water Cerenkov, photons per event log-uniform "
+                    "1e%g-1e%g" % (lo, hi),
+        "events": len(events), "photons": total_photons, "submitter_threads": submitters,
+        "plain_photons_per_s": plain_rate, "batched_photons_per_s": batched_rate,
+        "batched_over_plain": batched_rate / plain_rate,
+        "arrivals": "Poisson at %.0f%% of plain capacity (%.1f events/s)" % (100 * load, rate_events),
+        "batched_latency_ms": {"p50": 1e3 * pct(lat_b, 50), "p99": 1e3 * pct(lat_b, 99)},
+        "plain_latency_ms": {"p50": 1e3 * pct(lat_p, 50), "p99": 1e3 * pct(lat_p, 99)},
+        "batches": {k: v["batches"] for k, v in stats.items()},
+    }
+
+
 def dist_init(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
@@ -181,6 +295,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the batched-serving comparison")
     ap.add_argument("--gensteps", type=int, default=2000, help="gensteps per event (2000 is the benchmark workload)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -288,6 +403,9 @@ def main():
                      "kernel_ms": sim_mean, "peak_source": peak_kind},
         "clocks": clk.summary(),
     }
+    if not args.no_serving and world == 1:
+        line["serving"] = serving_bench()                                   # the 1e3-1e7 serving stream
+        line["serving_small_events"] = serving_bench(num_events=1500, lo=3.0, hi=5.0)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(geom, gs)
     print(json.dumps(line))

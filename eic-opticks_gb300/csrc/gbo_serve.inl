@@ -254,11 +254,19 @@ void serve_loop(gbo_server* sv)
                 finish_slot(sv, sl, q == cudaSuccess ? GBO_OK : fail(GBO_ERR_CUDA, "hit download: %s", cudaGetErrorString(q)));
             }
         }
-        // admit waiting events into idle slots
+        // admit waiting events into idle slots: at once when the GPU has nothing in flight, otherwise only once
+        // enough photons wait to fill the GPU (min_batch_photon), so that batches do not degenerate to single events
         for (Slot& sl : sv->slots) {
             if (sl.phase != 0) continue;
+            int in_flight = 0;
+            for (Slot& x : sv->slots) in_flight += x.phase != 0;
             {
                 std::lock_guard<std::mutex> lock(sv->mu);
+                if (in_flight > 0) {
+                    long long waiting = 0;
+                    for (auto& ev : sv->pending) { waiting += ev->num_photon; if (waiting >= sv->cfg.min_batch_photon) break; }
+                    if (waiting < sv->cfg.min_batch_photon) continue;
+                }
                 long long photons = 0;
                 while (!sv->pending.empty()) {
                     auto& ev = sv->pending.front();
@@ -303,6 +311,7 @@ int gbo_server_config_default(gbo_server_config* c)
     c->max_batch_photon = 16ll << 20;
     c->hbm_budget_bytes = 120ll << 30;
     c->max_batch_events = 4096;
+    c->min_batch_photon = 2ll << 20;
     return GBO_OK;
 }
 

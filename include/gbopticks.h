@@ -149,6 +149,7 @@ typedef struct gbo_server_config {
     int32_t max_batch_events;       /* events per launch (4096) */
     int64_t max_batch_photon;       /* photons per launch (16M); also bounded by the budget */
     int64_t hbm_budget_bytes;       /* device memory the server's launches may hold (120 GB) */
+    int64_t min_batch_photon;       /* while a launch is in flight, start another only once this many photons wait (2M) */
 } gbo_server_config;
 typedef struct gbo_server_stats {
     int64_t events_submitted, events_done, batches, photons, max_batch_photon;
