@@ -542,6 +542,7 @@ int gbo_config_default(gbo_config* c)
     c->refill_min = 8;
     c->blocks_per_sm = 0;
     c->refill_period = 1;
+    c->max_slot = 0;
     long long iv;
     float fv;
     if (env_int("OPTICKS_MAX_BOUNCE", iv)) c->max_bounce = (int32_t)iv;
@@ -551,6 +552,7 @@ int gbo_config_default(gbo_config* c)
     if (const char* s = std::getenv("OPTICKS_PROPAGATE_EPSILON0_MASK")) c->epsilon0_mask = parse_flag_mask(s);
     if (const char* s = std::getenv("OPTICKS_HIT_MASK")) c->hit_mask = parse_flag_mask(s);
     if (env_int("OPTICKS_EVENT_SKIPAHEAD", iv)) c->event_skipahead = (uint64_t)iv;
+    if (env_int("OPTICKS_MAX_SLOT", iv)) c->max_slot = iv;
     if (const char* s = std::getenv("QRng__SEED_OFFSET")) {
         char* end = nullptr;
         c->rng_seed = std::strtoull(s, &end, 10);
@@ -723,16 +725,27 @@ static Params make_params(gbo_engine* e)
     return P;
 }
 
-// runs one event whose gensteps (and input photons) are already in e->gs / e->input on the device
+// Where one launch of an event goes: a launch covers event photons [photon_offset, photon_offset + n) and writes
+// its photon/seq records from photon_base and its ordered hits from hit_base; `capacity` photons are reserved for
+// the whole event so that later launches of a sliced event do not reallocate.
+struct LaunchPlace {
+    unsigned long long photon_offset = 0;
+    long long photon_base = 0;
+    long long hit_base = 0;
+    long long capacity = 0;
+};
+
+// runs one launch whose gensteps (and input photons) are already on the device
 static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int64_t num_gs,
                      const gbo_sphoton* d_input, int64_t num_input, long long num_photon, cudaStream_t s,
-                     int prior_launches)
+                     int prior_launches, LaunchPlace at = LaunchPlace())
 {
     const bool keep_photon = e->cfg.record_photon != 0;
     const bool keep_seq = e->cfg.record_seq != 0;
     int rc;
-    if (e->cfg.max_photon > 0 && num_photon > e->cfg.max_photon)
-        return fail(GBO_ERR_CAPACITY, "event of %lld photons above max_photon %lld", num_photon, (long long)e->cfg.max_photon);
+    if (at.capacity < at.photon_base + num_photon) at.capacity = at.photon_base + num_photon;
+    if (e->cfg.max_photon > 0 && at.capacity > e->cfg.max_photon)
+        return fail(GBO_ERR_CAPACITY, "event of %lld photons above max_photon %lld", at.capacity, (long long)e->cfg.max_photon);
     if (num_input > 0 && num_input < num_photon)
         return fail(GBO_ERR_ARG, "%lld input photons for %lld photon slots", (long long)num_input, num_photon);
     const long long words = (num_photon + 31) / 32;
@@ -741,10 +754,10 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     if ((rc = e->word_prefix.ensure(words))) return rc;
     if ((rc = e->block_sum.ensure(nblk))) return rc;
     if ((rc = e->block_offset.ensure(nblk))) return rc;
-    if ((rc = e->hits.ensure(num_photon))) return rc;
-    if (keep_photon) { if ((rc = e->photon.ensure(num_photon))) return rc; }
+    if (at.photon_base == 0 && (rc = e->hits.ensure(at.capacity))) return rc;
+    if (keep_photon) { if (at.photon_base == 0 && (rc = e->photon.ensure(at.capacity))) return rc; }
     else { if ((rc = e->hits_unordered.ensure(num_photon))) return rc; }
-    if (keep_seq) { if ((rc = e->seq.ensure(num_photon))) return rc; }
+    if (keep_seq && at.photon_base == 0) { if ((rc = e->seq.ensure(at.capacity))) return rc; }
 
     Params P = make_params(e);
     const uint64_t skip = e->cfg.event_skipahead * (uint64_t)(event_id < 0 ? 0 : event_id);
@@ -753,10 +766,10 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     P.gs_end = e->gs_end.ptr;
     P.num_gs = (int)num_gs;
     P.num_photon = num_photon;
-    P.photon_offset = 0;
+    P.photon_offset = at.photon_offset;
     P.input_photon = d_input;
-    P.photon_out = keep_photon ? e->photon.ptr : nullptr;
-    P.seq_out = keep_seq ? e->seq.ptr : nullptr;
+    P.photon_out = keep_photon ? e->photon.ptr + at.photon_base : nullptr;
+    P.seq_out = keep_seq ? e->seq.ptr + at.photon_base : nullptr;
     P.hit_unordered = keep_photon ? nullptr : e->hits_unordered.ptr;
     P.hit_count = e->counters.ptr;
     P.bitmap = e->bitmap.ptr;
@@ -789,12 +802,14 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
         launches += 2;
         if (keep_photon) {
             const long long threads = words * 32;
-            k_gather_photons<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(e->photon.ptr, e->bitmap.ptr, e->word_prefix.ptr,
-                                                                                e->block_offset.ptr, words, e->hits.ptr);
+            k_gather_photons<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+                e->photon.ptr + at.photon_base, e->bitmap.ptr, e->word_prefix.ptr, e->block_offset.ptr, words,
+                e->hits.ptr + at.hit_base);
         } else {
             // the unordered count is only known on the device: launch for the worst case and let threads exit
             k_gather_unordered<<<(unsigned)((num_photon + 255) / 256), 256, 0, s>>>(
-                e->hits_unordered.ptr, e->counters.ptr, 0ull, e->bitmap.ptr, e->word_prefix.ptr, e->block_offset.ptr, e->hits.ptr);
+                e->hits_unordered.ptr, e->counters.ptr, at.photon_offset, e->bitmap.ptr, e->word_prefix.ptr,
+                e->block_offset.ptr, e->hits.ptr + at.hit_base);
         }
         launches++;
         CU(cudaGetLastError());
@@ -802,10 +817,10 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     CU(cudaEventRecord(e->ev[3], s));
     CU(cudaMemcpyAsync(e->host_counters, e->counters.ptr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
-    e->num_photon = num_photon;
-    e->num_hit = (long long)e->host_counters[1];
+    e->num_photon = at.photon_base + num_photon;
+    e->num_hit = at.hit_base + (long long)e->host_counters[1];
     e->event_id = event_id;
-    e->stats.num_photon = num_photon;
+    e->stats.num_photon = e->num_photon;
     e->stats.num_hit = e->num_hit;
     e->stats.simulate_launches = num_photon > 0 ? 1 : 0;
     e->stats.kernel_launches = launches;
@@ -835,13 +850,76 @@ int gbo_simulate(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         return fail(GBO_ERR_ARG, "gbo_simulate: INPUT_PHOTON gensteps need %llu photons, %lld given", total,
                     (long long)num_input_photon);
     cudaStream_t s = e->stream;
+    const long long max_slot = e->cfg.max_slot;
+    if (max_slot <= 0 || (long long)total <= max_slot) {
+        CU(cudaEventRecord(e->ev[0], s));
+        int rc;
+        if ((rc = upload(e->gs, gs, (size_t)num_gs, s))) return rc;
+        if ((rc = upload(e->gs_end, end.data(), end.size(), s))) return rc;
+        if (num_input_photon > 0) { if ((rc = upload(e->input, input_photon, (size_t)num_input_photon, s))) return rc; }
+        return run_event(e, event_id, e->gs.ptr, num_gs, num_input_photon > 0 ? e->input.ptr : nullptr, num_input_photon,
+                         (long long)total, s, 0);
+    }
+    // Device-memory-bounded slicing of one event into launches of at most max_slot photons, at genstep
+    // granularity (SGenstep::GetGenstepSlices, qudarap/QSim.cc:481-529); every photon keeps its event-level index
+    // (photon_slot_offset + idx, CSGOptiX7.cu:415) so the event's results do not depend on the slicing.
+    LaunchPlace at;
+    at.capacity = (long long)total;
+    gbo_stats acc{};
+    int64_t g0 = 0;
+    while (g0 < num_gs) {
+        int64_t g1 = g0;
+        unsigned long long n = 0;
+        while (g1 < num_gs && (g1 == g0 || (long long)(n + gs[g1].q[0].u[3]) <= max_slot)) n += gs[g1++].q[0].u[3];
+        std::vector<unsigned long long> part((size_t)(g1 - g0));
+        unsigned long long c = 0;
+        for (int64_t i = g0; i < g1; i++) { c += gs[i].q[0].u[3]; part[(size_t)(i - g0)] = c; }
+        CU(cudaEventRecord(e->ev[0], s));
+        int rc;
+        if ((rc = upload(e->gs, gs + g0, (size_t)(g1 - g0), s))) return rc;
+        if ((rc = upload(e->gs_end, part.data(), part.size(), s))) return rc;
+        const bool inp = num_input_photon > 0;
+        if (inp && n > 0) { if ((rc = upload(e->input, input_photon + at.photon_offset, (size_t)n, s))) return rc; }
+        if ((rc = run_event(e, event_id, e->gs.ptr, g1 - g0, inp ? e->input.ptr : nullptr, inp ? (int64_t)n : 0,
+                            (long long)n, s, 0, at)))
+            return rc;
+        acc.ms_upload += e->stats.ms_upload;
+        acc.ms_simulate += e->stats.ms_simulate;
+        acc.ms_compact += e->stats.ms_compact;
+        acc.simulate_launches += e->stats.simulate_launches;
+        acc.kernel_launches += e->stats.kernel_launches;
+        at.photon_offset += n;
+        at.photon_base += (long long)n;
+        at.hit_base = e->num_hit;
+        g0 = g1;
+    }
+    acc.num_photon = e->num_photon;
+    acc.num_hit = e->num_hit;
+    e->stats = acc;
+    return GBO_OK;
+}
+
+int gbo_simulate_slice(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs,
+                       const gbo_sphoton* input_photon, int64_t num_input_photon, uint64_t photon_offset)
+{
+    if (!e) return fail(GBO_ERR_ARG, "gbo_simulate_slice: null engine");
+    if (num_gs < 0 || (num_gs > 0 && !gs)) return fail(GBO_ERR_ARG, "gbo_simulate_slice: bad gensteps");
+    if (num_gs > 0x7fffffff) return fail(GBO_ERR_CAPACITY, "gbo_simulate_slice: %lld gensteps", (long long)num_gs);
+    if (num_input_photon < 0 || (num_input_photon > 0 && !input_photon)) return fail(GBO_ERR_ARG, "gbo_simulate_slice: bad input photons");
+    CU(cudaSetDevice(e->device));
+    std::vector<unsigned long long> end((size_t)num_gs);
+    unsigned long long total = 0;
+    for (int64_t i = 0; i < num_gs; i++) { total += gs[i].q[0].u[3]; end[(size_t)i] = total; }
+    cudaStream_t s = e->stream;
     CU(cudaEventRecord(e->ev[0], s));
     int rc;
     if ((rc = upload(e->gs, gs, (size_t)num_gs, s))) return rc;
     if ((rc = upload(e->gs_end, end.data(), end.size(), s))) return rc;
     if (num_input_photon > 0) { if ((rc = upload(e->input, input_photon, (size_t)num_input_photon, s))) return rc; }
+    LaunchPlace at;
+    at.photon_offset = photon_offset;
     return run_event(e, event_id, e->gs.ptr, num_gs, num_input_photon > 0 ? e->input.ptr : nullptr, num_input_photon,
-                     (long long)total, s, 0);
+                     (long long)total, s, 0, at);
 }
 
 int gbo_simulate_device(gbo_engine* e, int32_t event_id, const void* d_gs, int64_t num_gs, const void* d_input,

@@ -42,7 +42,8 @@ class Config(C.Structure):
                 ("rng_seed", C.c_uint64), ("rng_offset", C.c_uint64), ("event_skipahead", C.c_uint64),
                 ("tmax", C.c_float), ("debug_tag", C.c_int32), ("record_photon", C.c_int32),
                 ("record_seq", C.c_int32), ("max_photon", C.c_int64), ("kernel_mode", C.c_int32),
-                ("refill_min", C.c_int32), ("blocks_per_sm", C.c_int32), ("refill_period", C.c_int32)]
+                ("refill_min", C.c_int32), ("blocks_per_sm", C.c_int32), ("refill_period", C.c_int32),
+                ("max_slot", C.c_int64)]
 
 
 class TuneResult(C.Structure):
@@ -80,6 +81,7 @@ def load(path=LIB):
     lib.gbo_engine_destroy.argtypes = [C.c_void_p]
     lib.gbo_simulate.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
     lib.gbo_simulate_device.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
+    lib.gbo_simulate_slice.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_uint64]
     lib.gbo_num_hit.argtypes = [C.c_void_p]
     lib.gbo_num_photon.argtypes = [C.c_void_p]
     lib.gbo_device_hits.argtypes = [C.c_void_p]
@@ -162,6 +164,16 @@ class Engine:
         _check(self.lib.gbo_simulate(self.handle, int(event_id), gs.ctypes.data_as(C.c_void_p), len(gs),
                                      inp.ctypes.data_as(C.c_void_p) if inp is not None else None,
                                      len(inp) if inp is not None else 0), "gbo_simulate")
+        return self.num_hit()
+
+    def simulate_slice(self, event_id, gensteps, photon_offset, input_photon=None):
+        """One launch of the event photons photon_offset.. (gbo_simulate_slice)."""
+        gs = np.ascontiguousarray(gensteps, dtype=np.float32)
+        inp = np.ascontiguousarray(input_photon) if input_photon is not None else None
+        _check(self.lib.gbo_simulate_slice(self.handle, int(event_id), gs.ctypes.data_as(C.c_void_p), len(gs),
+                                           inp.ctypes.data_as(C.c_void_p) if inp is not None else None,
+                                           len(inp) if inp is not None else 0, C.c_uint64(int(photon_offset))),
+               "gbo_simulate_slice")
         return self.num_hit()
 
     def simulate_device(self, event_id, d_gs_ptr, num_gs, d_input_ptr=0, num_input=0, stream=0):

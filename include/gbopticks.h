@@ -80,6 +80,7 @@ typedef struct gbo_config {
     int32_t  refill_min;            /* pool kernel: idle lanes a warp waits for before refilling (1..32, 8) */
     int32_t  blocks_per_sm;         /* pool kernel: resident blocks per SM (0: occupancy maximum) */
     int32_t  refill_period;         /* pool kernel: steps between refill checks (compaction period, >= 1) */
+    int64_t  max_slot;              /* OPTICKS_MAX_SLOT: photons per launch, larger events are sliced (0: no slicing) */
 } gbo_config;
 
 /* Result of gbo_autotune: the kernel form chosen and the simulate time of every candidate tried. */
@@ -106,6 +107,12 @@ int         gbo_simulate(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, i
                          const gbo_sphoton* input_photon, int64_t num_input_photon);
 int         gbo_simulate_device(gbo_engine* e, int32_t event_id, const void* d_gs, int64_t num_gs,
                                 const void* d_input_photon, int64_t num_input_photon, void* cuda_stream);
+/* gbo_simulate_slice : one launch of a slice of an event, the photons of `gs` being event photons
+ * photon_offset + i (the reference's photon_slot_offset, CSGOptiX/CSGOptiX.cc prepareParam, used by QSim::simulate's
+ * genstep slices qudarap/QSim.cc:481-529); RNG streams and photon indices are those of the whole event, so slices
+ * simulated separately (e.g. on different GPUs) give exactly the photons of the whole event. */
+int         gbo_simulate_slice(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs,
+                               const gbo_sphoton* input_photon, int64_t num_input_photon, uint64_t photon_offset);
 int64_t     gbo_num_hit(const gbo_engine* e);
 int64_t     gbo_num_photon(const gbo_engine* e);
 int         gbo_copy_hits(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64_t count);

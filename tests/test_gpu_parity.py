@@ -189,3 +189,40 @@ def test_kernel_forms_bit_identical(E):
         assert np.array_equal(p.view(np.uint32), p0.view(np.uint32))
         assert np.array_equal(s.view(np.uint64), s0.view(np.uint64))
         assert n == n0 and np.array_equal(h.view(np.uint32), h0.view(np.uint32))
+
+
+@pytest.mark.parametrize("max_slot", [500, 1000, 1234])
+def test_sliced_event_equals_whole(E, max_slot):
+    """An event cut into launches of at most max_slot photons (OPTICKS_MAX_SLOT) gives the whole event's bytes."""
+    z = load_golden("sim_crystal_array.npz")
+    arrays = golden_arrays(z)
+    whole = E.Engine(arrays, record_photon=1, record_seq=1)
+    n0 = whole.simulate(2, z["gs"])
+    p0, s0, h0 = whole.photons(), whole.seq(), whole.hits()
+    whole.close()
+    sliced = E.Engine(arrays, record_photon=1, record_seq=1, max_slot=max_slot)
+    n1 = sliced.simulate(2, z["gs"])
+    assert sliced.stats()["simulate_launches"] > 1
+    assert n1 == n0
+    assert np.array_equal(sliced.photons().view(np.uint32), p0.view(np.uint32))
+    assert np.array_equal(sliced.seq().view(np.uint64), s0.view(np.uint64))
+    assert np.array_equal(sliced.hits().view(np.uint32), h0.view(np.uint32))
+    sliced.close()
+
+
+def test_shards_on_separate_launches_equal_whole(E):
+    """Event shards simulated as separate launches (as on separate GPUs) concatenate to the whole event's hits."""
+    from eic_opticks_gb300 import geometry as G, gensteps as GS, shard
+    arrays = G.crystal_array().arrays()
+    gs = GS.crystal_scint_gensteps(50, 800, seed=12)
+    eng = E.Engine(arrays)
+    eng.simulate(7, gs)
+    whole = eng.hits()
+    parts = []
+    for rank in range(3):
+        part, offset = shard.shard_gensteps(gs, rank, 3)
+        eng.simulate_slice(7, part, offset)
+        parts.append(eng.hits())
+    eng.close()
+    merged = shard.merge_hits(parts)
+    assert np.array_equal(merged.view(np.uint32), whole.view(np.uint32))
