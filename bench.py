@@ -102,9 +102,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def workload(seed=1, num_gs=2000):
+LARGE_SPHERE = "large_sphere_20000_sensors_scint_100M"
+
+
+def workload(seed=1, num_gs=2000, kind="crystal_array"):
+    """crystal_array: num_gs Poisson(5000) scintillation gensteps in the 8x8 CsI array (the headline event).
+    large_sphere: 20,000 gensteps of 5,000 photons (100M) uniform in r < 17 m of the 17.7 m liquid-scintillator
+    sphere with 20,000 instanced CSG sensors."""
     ge.load_package()
     from eic_opticks_gb300 import geometry as G, gensteps as GS
+    if kind == "large_sphere":
+        return G.large_sphere().arrays(), GS.sphere_scint_gensteps(20000, 5000, seed=seed)
     geom = G.crystal_array().arrays()
     gs = GS.crystal_scint_gensteps(num_gs, 5000, seed=seed)
     return geom, gs
@@ -297,6 +305,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the batched-serving comparison")
     ap.add_argument("--gensteps", type=int, default=2000, help="gensteps per event (2000 is the benchmark workload)")
+    ap.add_argument("--workload", default="crystal_array", choices=["crystal_array", "large_sphere"])
+    ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
+                    help="1: binary64 root polish and position/time accumulators")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -316,9 +327,9 @@ def main():
         dist.barrier()
     ge.load_package()
     from eic_opticks_gb300 import engine as E
-    geom, gs = workload(seed=1 + rank, num_gs=args.gensteps)
+    geom, gs = workload(seed=1 + rank, num_gs=args.gensteps, kind=args.workload)
     n_photon = int(gs.view(np.uint32)[:, 0, 3].astype(np.int64).sum())
-    eng = E.Engine(geom, device=local)
+    eng = E.Engine(geom, device=local, precision=args.precision)
     # kernel form picked by the autotuner on a 10% sample of the workload (setup, outside the timed region)
     tune = eng.autotune(0, gs[: max(1, len(gs) // 10)], trials=2)
 
@@ -389,8 +400,12 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded numpy gensteps with the reference genstep layout)",
-        "config": {"workload": WORKLOAD if args.gensteps == 2000 else WORKLOAD + "_%dgs" % args.gensteps, "photons_per_step": n_photon, "gensteps_per_step": len(gs),
+        "dtype": "f32" if not args.precision else "f32+f64",
+        "data": "synthetic (seeded numpy gensteps with the reference genstep layout)",
+        "config": {"workload": (LARGE_SPHERE if args.workload == "large_sphere" else
+                                WORKLOAD if args.gensteps == 2000 else WORKLOAD + "_%dgs" % args.gensteps),
+                   "precision": "binary64 root polish + accumulators" if args.precision else "binary32",
+                   "photons_per_step": n_photon, "gensteps_per_step": len(gs),
                    "hits_per_step": hits, "path": "plain: one event per launch", "l2": "flushed (256 MB write) between timed steps",
                    "kernel": {"mode": "photon pool" if tune["kernel_mode"] == 0 else "one thread per photon",
                               "refill_min": tune["refill_min"], "refill_period": tune["refill_period"],

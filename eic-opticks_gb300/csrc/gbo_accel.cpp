@@ -176,6 +176,7 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
         }
     }
     out.inst.resize(num_inst);
+    out.inst64.assign(12 * (size_t)num_inst, 0.0);
     std::vector<Box> inst_box(num_inst);
     for (int i = 0; i < num_inst; i++) {
         const gbo_qat4& q = inst[i];
@@ -199,6 +200,11 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
             c[1] = (float)r[1][j];
             c[2] = (float)r[2][j];
             c[3] = (float)it[j];
+            double* c64 = out.inst64.data() + 12 * (size_t)i + 4 * j;
+            c64[0] = r[0][j];
+            c64[1] = r[1][j];
+            c64[2] = r[2][j];
+            c64[3] = it[j];
         }
         d.solid = s;
         d.identity = (uint32_t)q.q2.i[3];

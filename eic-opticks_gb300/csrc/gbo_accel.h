@@ -62,6 +62,7 @@ struct AccelHost {
     std::vector<BvhNode2> tlas2;         // traversal form of tlas (root is node 0; a single-leaf tree has one node)
     std::vector<int32_t> tlas_index;     // leaf ranges index into this permutation of instances
     std::vector<InstDev> inst;
+    std::vector<double> inst64;          // the same inverse columns in binary64, 12 per instance (precision mode)
     std::vector<PrimDev> prim;
     std::vector<SolidDev> solid;
     int max_depth = 0;

@@ -68,6 +68,27 @@ GBO_DEV void robust_roots(float& t1, float& t2, float& disc, float& sdisc, float
     t2 = fmaxf(root1, root2);
 }
 
+// Precision mode: Newton polish in binary64 of a binary32 root of a t^2 + 2 b t + c = 0, the coefficients formed
+// in binary64 from the binary32 ray.  The binary32 root loses accuracy both to the resolution of t and to the
+// cancellation in c = |O|^2 - r^2 when the ray starts far from the quadric, so every accepted quadric root is
+// polished.  Each Newton step evaluates the residual in binary64 and divides in binary32: the correction is a few
+// ulp of t, so its own relative error of 2^-24 is immaterial, and binary64 division is slow on this part.  Two
+// steps from the binary32 root.  The polished root replaces the binary32 one only when it is still above t_min:
+// every root a leaf returns stays strictly above the t_min it was given, which is what makes the CSG tree's loop
+// tranches advance and end.
+GBO_DEV float polish_root(float t, float t_min, double a, double b, double c)
+{
+    double x = (double)t;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const double f = fma(fma(a, x, 2.0 * b), x, c);
+        const float df = (float)(2.0 * fma(a, x, b));
+        if (df != 0.f) x -= (double)((float)f / df);
+    }
+    const float r = (float)x;
+    return r > t_min && r < __int_as_float(0x7f800000) ? r : t;
+}
+
 GBO_DEV void robust_roots_disq(float t_min, float& t1, float& t2, float& disc, float& sdisc, float d, float b, float c)
 {
     disc = b * b - d * c;
@@ -80,7 +101,7 @@ GBO_DEV void robust_roots_disq(float t_min, float& t1, float& t2, float& disc, f
 }
 
 // csg_intersect_leaf_sphere.h:14-55
-GBO_DEV bool leaf_sphere(float4& is, float4 q0, float t_min, float3 ro, float3 rd)
+GBO_DEV bool leaf_sphere(float4& is, float4 q0, float t_min, float3 ro, float3 rd, bool polish = false)
 {
     const float3 center = f3(q0.x, q0.y, q0.z);
     const float radius = q0.w;
@@ -91,7 +112,14 @@ GBO_DEV bool leaf_sphere(float4& is, float4 q0, float t_min, float3 ro, float3 r
     const float d = dot(D, D);
     float root1, root2, disc, sdisc;
     robust_roots(root1, root2, disc, sdisc, d, b, c);
-    const float t_cand = sdisc > 0.f ? (root1 > t_min ? root1 : root2) : t_min;
+    float t_cand = sdisc > 0.f ? (root1 > t_min ? root1 : root2) : t_min;
+    if (polish && t_cand > t_min) {
+        const double ox = (double)ro.x - q0.x, oy = (double)ro.y - q0.y, oz = (double)ro.z - q0.z;
+        const double a2 = (double)rd.x * rd.x + (double)rd.y * rd.y + (double)rd.z * rd.z;
+        const double b2 = ox * rd.x + oy * rd.y + oz * rd.z;
+        const double c2 = ox * ox + oy * oy + oz * oz - (double)radius * radius;
+        t_cand = polish_root(t_cand, t_min, a2, b2, c2);
+    }
     const bool valid = t_cand > t_min;
     if (valid) {
         is.x = (O.x + t_cand * D.x) / radius;
@@ -103,7 +131,7 @@ GBO_DEV bool leaf_sphere(float4& is, float4 q0, float t_min, float3 ro, float3 r
 }
 
 // csg_intersect_leaf_zsphere.h:44-151
-GBO_DEV bool leaf_zsphere(float4& is, float4 q0, float2 q1, float t_min, float3 ro, float3 rd)
+GBO_DEV bool leaf_zsphere(float4& is, float4 q0, float2 q1, float t_min, float3 ro, float3 rd, bool polish = false)
 {
     const float3 center = f3(q0.x, q0.y, q0.z);
     const float3 O = ro - center;
@@ -137,6 +165,14 @@ GBO_DEV bool leaf_zsphere(float4& is, float4 q0, float2 q1, float t_min, float3 
     if (valid) {
         is.w = t_cand;
         if (t_cand == t1sph || t_cand == t2sph) {
+            if (polish) {
+                const double ox = (double)ro.x - center.x, oy = (double)ro.y - center.y, oz = (double)ro.z - center.z;
+                const double a2 = (double)rd.x * rd.x + (double)rd.y * rd.y + (double)rd.z * rd.z;
+                const double b2 = ox * rd.x + oy * rd.y + oz * rd.z;
+                const double c2 = ox * ox + oy * oy + oz * oz - (double)radius * radius;
+                t_cand = polish_root(t_cand, t_min, a2, b2, c2);
+                is.w = t_cand;
+            }
             is.x = (O.x + t_cand * D.x) / radius;
             is.y = (O.y + t_cand * D.y) / radius;
             is.z = (O.z + t_cand * D.z) / radius;
@@ -150,7 +186,7 @@ GBO_DEV bool leaf_zsphere(float4& is, float4 q0, float2 q1, float t_min, float3 
 }
 
 // csg_intersect_leaf_cylinder.h:33-82
-GBO_DEV bool leaf_cylinder(float4& is, float4 q0, float2 q1, float t_min, float3 ro, float3 rd)
+GBO_DEV bool leaf_cylinder(float4& is, float4 q0, float2 q1, float t_min, float3 ro, float3 rd, bool polish = false)
 {
     const float r = q0.w, z1 = q1.x, z2 = q1.y;
     const float ox = ro.x, oy = ro.y, oz = ro.z;
@@ -175,6 +211,12 @@ GBO_DEV bool leaf_cylinder(float4& is, float4 q0, float2 q1, float t_min, float3
     const bool valid = t_cand > t_min && t_cand < __int_as_float(0x7f800000);
     if (valid) {
         const bool sheet = (t_cand == t_near || t_cand == t_far);
+        if (sheet && polish) {
+            const double a2 = (double)vx * vx + (double)vy * vy;
+            const double b2 = (double)ox * vx + (double)oy * vy;
+            const double c2 = (double)ox * ox + (double)oy * oy - (double)r * r;
+            t_cand = polish_root(t_cand, t_min, a2, b2, c2);
+        }
         is.x = sheet ? (ox + t_cand * vx) / r : 0.f;
         is.y = sheet ? (oy + t_cand * vy) / r : 0.f;
         is.z = sheet ? 0.f : (t_cand == t_z1cap ? -1.f : 1.f);
@@ -385,7 +427,7 @@ GBO_DEV bool leaf_phicut(float4& is, float4 q0, float t_min, float3 o, float3 d)
 
 // csg_intersect_leaf.h:174-325
 GBO_DEV bool intersect_leaf(float4& is, const gbo_csgnode* node, const float4* plan, const gbo_qat4* itra,
-                            float t_min, float3 ro, float3 rd)
+                            float t_min, float3 ro, float3 rd, bool polish = false)
 {
     is = make_float4(0.f, 0.f, 0.f, 0.f);
     const NodeView nd = load_node(node);
@@ -400,9 +442,9 @@ GBO_DEV bool intersect_leaf(float4& is, const gbo_csgnode* node, const float4* p
     }
     bool valid = false;
     switch (nd.typecode) {
-        case GBO_CSG_SPHERE:           valid = leaf_sphere(is, nd.q0, t_min, origin, direction); break;
-        case GBO_CSG_ZSPHERE:          valid = leaf_zsphere(is, nd.q0, nd.q1, t_min, origin, direction); break;
-        case GBO_CSG_CYLINDER:         valid = leaf_cylinder(is, nd.q0, nd.q1, t_min, origin, direction); break;
+        case GBO_CSG_SPHERE:           valid = leaf_sphere(is, nd.q0, t_min, origin, direction, polish); break;
+        case GBO_CSG_ZSPHERE:          valid = leaf_zsphere(is, nd.q0, nd.q1, t_min, origin, direction, polish); break;
+        case GBO_CSG_CYLINDER:         valid = leaf_cylinder(is, nd.q0, nd.q1, t_min, origin, direction, polish); break;
         case GBO_CSG_BOX3:             valid = leaf_box3(is, nd.q0, t_min, origin, direction); break;
         case GBO_CSG_CONE:             valid = leaf_cone(is, nd.q0, t_min, origin, direction); break;
         case GBO_CSG_CONVEXPOLYHEDRON: valid = leaf_convexpolyhedron(is, nd.q0, plan, t_min, origin, direction); break;
@@ -448,9 +490,13 @@ GBO_DEV unsigned postorder_next(unsigned i, unsigned elev) { return (i & 1u) ? i
 
 constexpr int CSG_STACK = 15;
 constexpr int TRANCHE_STACK = 4;
+// Guard on tranches evaluated per tree: every loop tranche restarts above the last root, so an evaluation ends after
+// a few tranches per leaf root; this bound, far above that, turns any arithmetic corner that failed to advance into
+// a miss instead of an unbounded loop.
+constexpr int MAX_TRANCHES = 256;
 
 GBO_DEV bool intersect_tree(float4& isect, const gbo_csgnode* node, const float4* plan, const gbo_qat4* itra,
-                            float t_min, float3 ro, float3 rd)
+                            float t_min, float3 ro, float3 rd, bool polish = false)
 {
     const int numNode = (int)__ldg(&node->q0.u[0]);
     const unsigned height = (unsigned)(__ffs(numNode + 1) - 2);
@@ -465,8 +511,10 @@ GBO_DEV bool intersect_tree(float4& isect, const gbo_csgnode* node, const float4
 
     float4 cdata[CSG_STACK];
     int ccurr = -1;
+    int tranches = 0;
 
     while (tr_curr > -1 && !err) {
+        if (++tranches > MAX_TRANCHES) { err = true; break; }
         const unsigned slice = tr_slice[tr_curr];
         const float tmin = tr_tmin[tr_curr];
         tr_curr--;
@@ -480,7 +528,7 @@ GBO_DEV bool intersect_tree(float4& isect, const gbo_csgnode* node, const float4
             if (typecode == GBO_CSG_ZERO) { nodeIdx = postorder_next(nodeIdx, elevation); continue; }
             if (typecode >= GBO_CSG_NODE) {
                 float4 nd_isect;
-                intersect_leaf(nd_isect, nd, plan, itra, tmin, ro, rd);
+                intersect_leaf(nd_isect, nd, plan, itra, tmin, ro, rd, polish);
                 nd_isect.w = copysignf(nd_isect.w, nodeIdx % 2 == 0 ? -1.f : 1.f);
                 if (ccurr >= CSG_STACK - 1) { err = true; break; }
                 cdata[++ccurr] = nd_isect;
@@ -536,11 +584,11 @@ GBO_DEV bool intersect_tree(float4& isect, const gbo_csgnode* node, const float4
 
 // csg_intersect_tree.h:683-719 (list nodes are not supported)
 GBO_DEV bool intersect_prim(float4& isect, const gbo_csgnode* node, const float4* plan, const gbo_qat4* itra,
-                            float t_min, float3 o, float3 d)
+                            float t_min, float3 o, float3 d, bool polish = false)
 {
     const unsigned typecode = node_typecode(node);
-    if (typecode >= GBO_CSG_LEAF) return intersect_leaf(isect, node, plan, itra, t_min, o, d);
-    if (typecode < GBO_CSG_NODE) return intersect_tree(isect, node, plan, itra, t_min, o, d);
+    if (typecode >= GBO_CSG_LEAF) return intersect_leaf(isect, node, plan, itra, t_min, o, d, polish);
+    if (typecode < GBO_CSG_NODE) return intersect_tree(isect, node, plan, itra, t_min, o, d, polish);
     isect = make_float4(0.f, 0.f, 0.f, 0.f);
     return false;
 }

@@ -64,7 +64,9 @@ struct Params {
 
 GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng);
 
-template <bool TREE>
+// Kernel forms: TREE when any prim is a CSG tree; PRECISE for the precision mode (binary64 root polish in the
+// quadric leaves, binary64 position / time accumulators).  The default form compiles none of the latter.
+template <bool TREE, bool PRECISE>
 __global__ void __launch_bounds__(SIM_BLOCK, GBO_SIM_MINB) k_simulate(const __grid_constant__ Params P)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -73,7 +75,9 @@ __global__ void __launch_bounds__(SIM_BLOCK, GBO_SIM_MINB) k_simulate(const __gr
     bool is_hit = false;
     if (active) {
         Rng rng;
+        Acc64 acc;
         generate(P, idx, p, rng);
+        if (PRECISE) acc_init(acc, p);
 
         Seq seq;
         seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
@@ -83,11 +87,11 @@ __global__ void __launch_bounds__(SIM_BLOCK, GBO_SIM_MINB) k_simulate(const __gr
         while (bounce < P.max_bounce && p.time < P.max_time) {
             const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
             Hit h;
-            trace<TREE>(P.acc, p.pos, p.mom, tmin, P.tmax, hint, h);
+            trace<TREE, PRECISE>(P.acc, p.pos, p.mom, tmin, P.tmax, hint, h);
             if ((h.prim_boundary & 0xffffu) == 0xffffu) break;
             hint = (int)(h.iindex_identity >> 16);
             h.normal = normalize(h.normal);
-            const int command = propagate(P.tab, p, h, rng);
+            const int command = propagate(P.tab, p, h, rng, PRECISE ? &acc : nullptr);
             bounce++;
             if (P.seq_out) seq_add(seq, (unsigned)bounce, flag_of(p), boundary_of(p));
             if (command == CMD_BREAK) break;
@@ -156,7 +160,7 @@ GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng)
     set_index(p, photon_idx);
 }
 
-template <bool TREE>
+template <bool TREE, bool PRECISE>
 __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_pool(const __grid_constant__ Params P,
                                                              unsigned long long* pool, int refill_min, int period)
 {
@@ -170,6 +174,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_pool(const __grid_consta
     int it = 0;
     Photon p;
     Rng rng;
+    Acc64 acc;
     Seq seq;
     for (;; it++) {
         // refill every `period` steps (or when the warp is empty): idle lanes take consecutive photon indices
@@ -186,6 +191,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_pool(const __grid_consta
                 if (mine < (unsigned long long)P.num_photon) {
                     idx = (long long)mine;
                     generate(P, idx, p, rng);
+                    if (PRECISE) acc_init(acc, p);
                     bounce = 0;
                     hint = -1;
                     seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
@@ -203,13 +209,13 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_pool(const __grid_consta
             if (bounce < P.max_bounce && p.time < P.max_time) {
                 const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
                 Hit h;
-                trace<TREE>(P.acc, p.pos, p.mom, tmin, P.tmax, hint, h);
+                trace<TREE, PRECISE>(P.acc, p.pos, p.mom, tmin, P.tmax, hint, h);
                 if ((h.prim_boundary & 0xffffu) == 0xffffu) {
                     done = true;
                 } else {
                     hint = (int)(h.iindex_identity >> 16);
                     h.normal = normalize(h.normal);
-                    const int command = propagate(P.tab, p, h, rng);
+                    const int command = propagate(P.tab, p, h, rng, PRECISE ? &acc : nullptr);
                     bounce++;
                     if (P.seq_out) seq_add(seq, (unsigned)bounce, flag_of(p), boundary_of(p));
                     done = command == CMD_BREAK;
@@ -388,6 +394,21 @@ __global__ void k_tex_lookup(Tables t, const float2* xy, int n, int which, float
     else out[i] = make_float4(tex2D<float>(t.icdf_tex, c.x, c.y), 0.f, 0.f, 0.f);
 }
 
+// one thread per ray: the engine's closest-hit query (CSG/CSGScan.cu's _CSGScan_intersect plays this role for the
+// reference); t = -1 on a miss
+template <bool TREE, bool POLISH>
+__global__ void k_trace_rays(Accel acc, const float3* pos, const float3* dir, int n, float tmin, float tmax,
+                             float* t_out, unsigned* boundary_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Hit h;
+    trace<TREE, POLISH>(acc, pos[i], dir[i], tmin, tmax, -1, h);
+    const bool miss = (h.prim_boundary & 0xffffu) == 0xffffu;
+    t_out[i] = miss ? -1.f : h.t;
+    boundary_out[i] = miss ? 0xffffffffu : (h.prim_boundary & 0xffffu);
+}
+
 __global__ void k_scint_wavelength(Tables t, const float* u, int n, float* out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -486,6 +507,7 @@ struct gbo_engine {
     DBuf<BvhNode2> tlas;
     DBuf<int32_t> tlas_index;
     DBuf<InstDev> inst;
+    DBuf<double> inst64;                   // precision mode only
     DBuf<PrimDev> prim;
     DBuf<SolidDev> solid;
     DBuf<gbo_csgnode> node;
@@ -497,7 +519,7 @@ struct gbo_engine {
     int bnd_nx = 0, bnd_ny = 0, hd_factor = 0;
     float nm0 = 60.f, nms = 1.f;
     bool has_tree = false;
-    long long pool_grid[2] = {0, 0};        // resident blocks of k_simulate_pool<false|true>
+    long long pool_grid[4] = {0, 0, 0, 0};  // resident blocks of k_simulate_pool per kernel form
     // event
     DBuf<gbo_quad6> gs;
     DBuf<unsigned long long> gs_end;
@@ -515,6 +537,33 @@ struct gbo_engine {
     int32_t event_id = -1;
     gbo_stats stats{};
 };
+
+template <bool TREE, bool PRECISE>
+static void launch_form(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s)
+{
+    if (e->cfg.kernel_mode == 0) {
+        const int form = (TREE ? 1 : 0) | (PRECISE ? 2 : 0);
+        const long long need = (n + SIM_BLOCK - 1) / SIM_BLOCK;
+        const long long grid = need < e->pool_grid[form] ? need : e->pool_grid[form];
+        const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
+        const int period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
+        k_simulate_pool<TREE, PRECISE><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
+    } else {
+        k_simulate<TREE, PRECISE><<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
+    }
+}
+
+// One launch of the simulation kernel over n photons in the engine's kernel form (pool or one thread per photon,
+// CSG trees or not, precision mode or not); `pool` is the photon-pool counter, zeroed by the caller.
+static void launch_simulate(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s)
+{
+    const bool precise = e->cfg.precision != 0;
+    if (e->has_tree) {
+        if (precise) launch_form<true, true>(e, P, n, pool, s); else launch_form<true, false>(e, P, n, pool, s);
+    } else {
+        if (precise) launch_form<false, true>(e, P, n, pool, s); else launch_form<false, false>(e, P, n, pool, s);
+    }
+}
 
 extern "C" {
 
@@ -591,7 +640,7 @@ void gbo_engine_destroy(gbo_engine* e)
     if (e->icdf_tex) cudaDestroyTextureObject(e->icdf_tex);
     if (e->bnd_array) cudaFreeArray(e->bnd_array);
     if (e->icdf_array) cudaFreeArray(e->icdf_array);
-    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->prim.release(); e->solid.release();
+    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->prim.release(); e->solid.release();
     e->node.release(); e->plan.release(); e->itra.release(); e->optical.release();
     e->gs.release(); e->gs_end.release(); e->input.release(); e->photon.release(); e->seq.release();
     e->hits_unordered.release(); e->hits.release(); e->bitmap.release(); e->word_prefix.release();
@@ -654,6 +703,7 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     TRY(upload(e->tlas, acc.tlas2.data(), acc.tlas2.size(), e->stream));
     TRY(upload(e->tlas_index, acc.tlas_index.data(), acc.tlas_index.size(), e->stream));
     TRY(upload(e->inst, acc.inst.data(), acc.inst.size(), e->stream));
+    if (e->cfg.precision) TRY(upload(e->inst64, acc.inst64.data(), acc.inst64.size(), e->stream));
     TRY(upload(e->prim, acc.prim.data(), acc.prim.size(), e->stream));
     TRY(upload(e->solid, acc.solid.data(), acc.solid.size(), e->stream));
     TRY(upload(e->node, g->node, (size_t)g->num_node, e->stream));
@@ -673,16 +723,17 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     TRY(make_texture(&e->icdf_array, &e->icdf_tex, g->icdf, g->icdf_nx, g->icdf_ny, false));
     TRY(e->counters.ensure(4));
     {
-        int sms = 0, b0 = 0, b1 = 0;
+        int sms = 0, b[4] = {0, 0, 0, 0};
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_simulate_pool<false>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_simulate_pool<true>, SIM_BLOCK, 0) != cudaSuccess) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_simulate_pool<false, false>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_simulate_pool<true, false>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_simulate_pool<false, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_simulate_pool<true, true>, SIM_BLOCK, 0) != cudaSuccess) {
             gbo_engine_destroy(e);
             return fail(GBO_ERR_CUDA, "occupancy query failed");
         }
         const int want = e->cfg.blocks_per_sm;
-        e->pool_grid[0] = (long long)sms * (want > 0 && want < b0 ? want : (b0 > 0 ? b0 : 1));
-        e->pool_grid[1] = (long long)sms * (want > 0 && want < b1 ? want : (b1 > 0 ? b1 : 1));
+        for (int f = 0; f < 4; f++) e->pool_grid[f] = (long long)sms * (want > 0 && want < b[f] ? want : (b[f] > 0 ? b[f] : 1));
     }
     if (cudaStreamSynchronize(e->stream) != cudaSuccess) {
         gbo_engine_destroy(e);
@@ -700,6 +751,7 @@ static Params make_params(gbo_engine* e)
     P.acc.tlas = e->tlas.ptr;
     P.acc.tlas_index = e->tlas_index.ptr;
     P.acc.inst = e->inst.ptr;
+    P.acc.inst64 = e->inst64.ptr;
     P.acc.prim = e->prim.ptr;
     P.acc.solid = e->solid.ptr;
     P.acc.node = e->node.ptr;
@@ -780,18 +832,7 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     if (pool && num_photon > 0) CU(cudaMemsetAsync(e->bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
     CU(cudaEventRecord(e->ev[1], s));
     if (num_photon > 0) {
-        if (pool) {
-            const long long need = (num_photon + SIM_BLOCK - 1) / SIM_BLOCK;
-            const long long grid = need < e->pool_grid[e->has_tree] ? need : e->pool_grid[e->has_tree];
-            const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
-            const int period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
-            if (e->has_tree) k_simulate_pool<true><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, e->counters.ptr + 2, refill, period);
-            else k_simulate_pool<false><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, e->counters.ptr + 2, refill, period);
-        } else {
-            const long long blocks = (num_photon + SIM_BLOCK - 1) / SIM_BLOCK;
-            if (e->has_tree) k_simulate<true><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
-            else k_simulate<false><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
-        }
+        launch_simulate(e, P, num_photon, e->counters.ptr + 2, s);
         CU(cudaGetLastError());
         launches++;
     }
@@ -1095,6 +1136,36 @@ int gbo_texture_lookup(gbo_engine* e, int32_t which, const float* xy, int32_t n,
     });
 }
 
+int gbo_trace_rays(gbo_engine* e, const float* pos, const float* dir, int32_t n, float tmin, float tmax, float* t_out,
+                   uint32_t* boundary_out)
+{
+    if (!e || !pos || !dir || !t_out || !boundary_out || n <= 0) return fail(GBO_ERR_ARG, "gbo_trace_rays: bad arguments");
+    CU(cudaSetDevice(e->device));
+    Params P = make_params(e);
+    std::vector<float> in((size_t)n * 6);
+    std::memcpy(in.data(), pos, (size_t)n * 12);
+    std::memcpy(in.data() + (size_t)n * 3, dir, (size_t)n * 12);
+    std::vector<float> out((size_t)n * 2);
+    const int form = (e->has_tree ? 1 : 0) | (e->cfg.precision ? 2 : 0);
+    int rc = with_scratch(in.size() * 4, in.data(), out.size() * 4, out.data(), [&](void* d_in, void* d_out) {
+        const float3* dp = (const float3*)d_in;
+        const float3* dd = (const float3*)((float*)d_in + (size_t)n * 3);
+        float* dt = (float*)d_out;
+        unsigned* db = (unsigned*)((float*)d_out + n);
+        const unsigned g = (unsigned)((n + 127) / 128);
+        switch (form) {
+            case 0: k_trace_rays<false, false><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            case 1: k_trace_rays<true, false><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            case 2: k_trace_rays<false, true><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            default: k_trace_rays<true, true><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+        }
+    });
+    if (rc) return rc;
+    std::memcpy(t_out, out.data(), (size_t)n * 4);
+    std::memcpy(boundary_out, out.data() + n, (size_t)n * 4);
+    return GBO_OK;
+}
+
 int gbo_scint_wavelength(gbo_engine* e, const float* u, int32_t n, float* out)
 {
     if (!e || !u || !out || n <= 0) return fail(GBO_ERR_ARG, "gbo_scint_wavelength: bad arguments");
@@ -1214,6 +1285,7 @@ int gbo_simulate_noalloc(gbo_engine* e, int32_t event_id, const void* d_gs, int6
                          void* cuda_stream)
 {
     if (!e || !num_hit) return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: null engine or num_hit");
+    if (e->cfg.precision) return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: the precision mode is not available here");
     *num_hit = 0;
     if (num_gs < 0 || (num_gs > 0 && !d_gs)) return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: bad gensteps");
     if (num_gs > NA_MAX_GENSTEP)

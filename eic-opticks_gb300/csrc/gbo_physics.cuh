@@ -29,6 +29,26 @@ struct Tables {
     int debug_tag;
 };
 
+// Precision mode keeps each photon's global position and time in binary64 and rounds them to the binary32
+// record after every advance, so metre-scale paths do not accumulate binary32 rounding step by step.
+struct Acc64 { double x, y, z, t; };
+GBO_DEV void acc_init(Acc64& a, const Photon& p) { a.x = p.pos.x; a.y = p.pos.y; a.z = p.pos.z; a.t = p.time; }
+
+GBO_DEV void advance(Photon& p, float d, float group_velocity, Acc64* acc)
+{
+    if (acc) {
+        acc->t += (double)(d / group_velocity);         // the increment in binary32, its sum in binary64
+        acc->x += (double)d * (double)p.mom.x;
+        acc->y += (double)d * (double)p.mom.y;
+        acc->z += (double)d * (double)p.mom.z;
+        p.time = (float)acc->t;
+        p.pos = f3((float)acc->x, (float)acc->y, (float)acc->z);
+    } else {
+        p.time += d / group_velocity;
+        p.pos = p.pos + d * p.mom;
+    }
+}
+
 struct State {
     float4 material1, m1group2, material2, surface;
     uint4 optical;
@@ -325,7 +345,7 @@ GBO_DEV void rayleigh_scatter(Photon& p, Rng& rng)
 }
 
 GBO_DEV int propagate_to_boundary(const Tables& t, Photon& p, const State& s, float distance_to_boundary, Rng& rng,
-                                  unsigned& flag)
+                                  unsigned& flag, Acc64* acc = nullptr)
 {
     const float absorption_length = s.material1.y;
     const float scattering_length = s.material1.z;
@@ -339,8 +359,7 @@ GBO_DEV int propagate_to_boundary(const Tables& t, Photon& p, const State& s, fl
 
     if (absorption_distance <= scattering_distance) {
         if (absorption_distance <= distance_to_boundary) {
-            p.time += absorption_distance / group_velocity;
-            p.pos = p.pos + absorption_distance * p.mom;
+            advance(p, absorption_distance, group_velocity, acc);
             const float u_reemit = reemission_prob == 0.f ? 2.f : uniform(rng);
             if (u_reemit < reemission_prob) {
                 const float u_re_wavelength = uniform(rng);
@@ -358,14 +377,12 @@ GBO_DEV int propagate_to_boundary(const Tables& t, Photon& p, const State& s, fl
             return CMD_BREAK;
         }
     } else if (scattering_distance <= distance_to_boundary) {
-        p.time += scattering_distance / group_velocity;
-        p.pos = p.pos + scattering_distance * p.mom;
+        advance(p, scattering_distance, group_velocity, acc);
         rayleigh_scatter(p, rng);
         flag = GBO_BULK_SCATTER;
         return CMD_CONTINUE;
     }
-    p.pos = p.pos + distance_to_boundary * p.mom;
-    p.time += distance_to_boundary / group_velocity;
+    advance(p, distance_to_boundary, group_velocity, acc);
     return CMD_BOUNDARY;
 }
 
@@ -470,7 +487,7 @@ GBO_DEV int propagate_at_surface(const Tables& t, Photon& p, const State& s, flo
 }
 
 // qsim::propagate : one step given the normalized intersect
-GBO_DEV int propagate(const Tables& t, Photon& p, const Hit& h, Rng& rng)
+GBO_DEV int propagate(const Tables& t, Photon& p, const Hit& h, Rng& rng, Acc64* acc = nullptr)
 {
     const unsigned boundary = h.prim_boundary & 0xffffu;
     const unsigned identity = h.iindex_identity & 0xffffu;
@@ -480,7 +497,7 @@ GBO_DEV int propagate(const Tables& t, Photon& p, const Hit& h, Rng& rng)
     State s;
     fill_state(t, s, boundary, p.wavelength, cosTheta);
     unsigned flag = 0;
-    int command = propagate_to_boundary(t, p, s, h.t, rng, flag);
+    int command = propagate_to_boundary(t, p, s, h.t, rng, flag, acc);
     if (command == CMD_BOUNDARY) {
         const int ems = (int)s.optical.y;
         if (ems == GBO_EMS_NOSURFACE) command = propagate_at_boundary(t, p, s, h.normal, rng, flag);

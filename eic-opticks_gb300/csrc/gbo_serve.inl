@@ -170,19 +170,8 @@ int launch_batch(gbo_server* sv, Slot& sl)
     P.ev_pos0 = sl.ev_pos0.ptr;
     P.hit_gidx = sl.hit_gidx.ptr;
     if (N > 0) {
-        if (e->cfg.kernel_mode == 0) {
-            CU(cudaMemsetAsync(sl.bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
-            const long long need = (N + SIM_BLOCK - 1) / SIM_BLOCK;
-            const long long grid = need < e->pool_grid[e->has_tree] ? need : e->pool_grid[e->has_tree];
-            const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
-            const int period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
-            if (e->has_tree) k_simulate_pool<true><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, sl.counters.ptr + 2, refill, period);
-            else k_simulate_pool<false><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, sl.counters.ptr + 2, refill, period);
-        } else {
-            const long long blocks = (N + SIM_BLOCK - 1) / SIM_BLOCK;
-            if (e->has_tree) k_simulate<true><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
-            else k_simulate<false><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P);
-        }
+        if (e->cfg.kernel_mode == 0) CU(cudaMemsetAsync(sl.bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
+        launch_simulate(e, P, N, sl.counters.ptr + 2, s);
         CU(cudaGetLastError());
         k_word_prefix<<<(unsigned)nblk, SCAN_WORDS, 0, s>>>(sl.bitmap.ptr, words, sl.word_prefix.ptr, sl.block_sum.ptr);
         k_block_offsets<<<1, 1024, 0, s>>>(sl.block_sum.ptr, nblk, sl.block_offset.ptr, sl.counters.ptr + 1);

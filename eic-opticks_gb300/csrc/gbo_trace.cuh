@@ -28,6 +28,7 @@ struct Accel {
     const gbo_csgnode* node;
     const float4* plan;
     const gbo_qat4* itra;
+    const double* inst64;       // binary64 inverse columns, 12 per instance (precision mode only)
 };
 
 GBO_DEV bool slab(float4 bmin, float4 bmax, float3 o, float3 inv, float tmin, float tmax, float& tnear)
@@ -61,6 +62,20 @@ GBO_DEV float3 inst_normal(const InstDev& d, float3 n)    // transpose of the in
               d.c0[2] * n.x + d.c1[2] * n.y + d.c2[2] * n.z);
 }
 
+// precision mode: the world -> object transform of the ray in binary64, rounded once to binary32
+GBO_DEV void inst_ray64(const double* c, float3 p, float3 v, float3& op, float3& ov)
+{
+    const double2* q = reinterpret_cast<const double2*>(c);
+    double r[12];
+#pragma unroll
+    for (int k = 0; k < 6; k++) { const double2 x = __ldg(q + k); r[2 * k] = x.x; r[2 * k + 1] = x.y; }
+    const double px = p.x, py = p.y, pz = p.z, vx = v.x, vy = v.y, vz = v.z;
+    op = f3((float)(r[0] * px + r[1] * py + r[2] * pz + r[3]), (float)(r[4] * px + r[5] * py + r[6] * pz + r[7]),
+            (float)(r[8] * px + r[9] * py + r[10] * pz + r[11]));
+    ov = f3((float)(r[0] * vx + r[1] * vy + r[2] * vz), (float)(r[4] * vx + r[5] * vy + r[6] * vz),
+            (float)(r[8] * vx + r[9] * vy + r[10] * vz));
+}
+
 GBO_DEV InstDev load_inst(const InstDev* p)
 {
     const float4* q = reinterpret_cast<const float4*>(p);
@@ -74,12 +89,13 @@ GBO_DEV InstDev load_inst(const InstDev* p)
     return d;
 }
 
-template <bool TREE>
+// POLISH (precision mode): binary64 Newton polish of the quadric roots of sphere, zsphere and cylinder leaves
+template <bool TREE, bool POLISH>
 GBO_DEV bool prim_hit(float4& is, const Accel& a, int node_offset, float t_min, float3 o, float3 d)
 {
     const gbo_csgnode* root = a.node + node_offset;
-    if (TREE) return intersect_prim(is, root, a.plan, a.itra, t_min, o, d);
-    if (node_typecode(root) >= GBO_CSG_LEAF) return intersect_leaf(is, root, a.plan, a.itra, t_min, o, d);
+    if (TREE) return intersect_prim(is, root, a.plan, a.itra, t_min, o, d, POLISH);
+    if (node_typecode(root) >= GBO_CSG_LEAF) return intersect_leaf(is, root, a.plan, a.itra, t_min, o, d, POLISH);
     is = make_float4(0.f, 0.f, 0.f, 0.f);
     return false;
 }
@@ -92,13 +108,17 @@ struct Best {
     unsigned pb;
 };
 
-template <bool TREE>
+template <bool TREE, bool POLISH>
 GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float tmin, Best& b)
 {
     const InstDev d = load_inst(a.inst + ii);
     const float3 oo = d.is_identity ? pos : inst_point(d, pos);
     const float3 od = d.is_identity ? dir : inst_vector(d, dir);
     const float3 oinv = safe_inv(od);
+    // precision mode: the ray handed to the prims is transformed in binary64, once per instance and only when a
+    // prim box is hit (the box test keeps the binary32 ray: boxes are padded far beyond its error)
+    float3 po = oo, pd = od;
+    bool have64 = !POLISH || d.is_identity;
     const int2 so = __ldg(reinterpret_cast<const int2*>(a.solid + d.solid));
     for (int k2 = 0; k2 < so.y; k2++) {
         const float4* pq = reinterpret_cast<const float4*>(a.prim + so.x + k2);
@@ -106,7 +126,8 @@ GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float
         float ptn;
         if (!slab(pb0, pb1, oo, oinv, tmin, b.t, ptn)) continue;
         float4 is;
-        if (!prim_hit<TREE>(is, a, __float_as_int(pb0.w), tmin, oo, od)) continue;
+        if (!have64) { inst_ray64(a.inst64 + 12 * (size_t)ii, pos, dir, po, pd); have64 = true; }
+        if (!prim_hit<TREE, POLISH>(is, a, __float_as_int(pb0.w), tmin, po, pd)) continue;
         const unsigned key = ((unsigned)ii << 16) | (unsigned)k2;
         if (is.w < b.t || (is.w == b.t && b.key != 0xffffffffu && key < b.key)) {
             b.t = is.w; b.key = key; b.is = is; b.inst = ii; b.pb = __float_as_uint(pb1.w);
@@ -120,7 +141,7 @@ constexpr int HINT_FIRST = 0x7fffff;     // leaf item standing for the hint inst
 // work items: an inner node index (>= 0) or a leaf range encoded as -(1 + (first << 8 | count))
 GBO_DEV int leaf_item(int first, int count) { return -(1 + ((first << 8) | count)); }
 
-template <bool TREE>
+template <bool TREE, bool POLISH = false>
 GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tmax, int hint, Hit& h)
 {
     Best b;
@@ -138,7 +159,7 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
 #pragma unroll 1
             for (int k = 0; k < count; k++) {
                 const int ii = first == HINT_FIRST ? hint : __ldg(a.tlas_index + first + k);
-                if (first == HINT_FIRST || ii != hint) test_instance<TREE>(a, ii, pos, dir, tmin, b);
+                if (first == HINT_FIRST || ii != hint) test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b);
             }
         } else {
             const float4* nq = reinterpret_cast<const float4*>(a.tlas + item);

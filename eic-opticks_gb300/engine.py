@@ -43,7 +43,7 @@ class Config(C.Structure):
                 ("tmax", C.c_float), ("debug_tag", C.c_int32), ("record_photon", C.c_int32),
                 ("record_seq", C.c_int32), ("max_photon", C.c_int64), ("kernel_mode", C.c_int32),
                 ("refill_min", C.c_int32), ("blocks_per_sm", C.c_int32), ("refill_period", C.c_int32),
-                ("max_slot", C.c_int64)]
+                ("max_slot", C.c_int64), ("precision", C.c_int32), ("reserved", C.c_int32)]
 
 
 class TuneResult(C.Structure):
@@ -92,6 +92,8 @@ def load(path=LIB):
     lib.gbo_rng_sequence.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_void_p]
     lib.gbo_texture_lookup.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
     lib.gbo_scint_wavelength.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
+    lib.gbo_trace_rays.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.c_float, C.c_void_p,
+                                   C.c_void_p]
     lib.gbo_autotune.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
                                  C.c_void_p]
     _lib = lib
@@ -235,6 +237,16 @@ class Engine:
         _check(self.lib.gbo_texture_lookup(self.handle, int(which), xy.ctypes.data_as(C.c_void_p), len(xy),
                                            out.ctypes.data_as(C.c_void_p)), "gbo_texture_lookup")
         return out if which == 0 else out[:, 0].copy()
+
+    def trace_rays(self, pos, dir, tmin=0.05, tmax=1e6):
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        dir = np.ascontiguousarray(dir, dtype=np.float32)
+        t = np.zeros(len(pos), dtype=np.float32)
+        b = np.zeros(len(pos), dtype=np.uint32)
+        _check(self.lib.gbo_trace_rays(self.handle, pos.ctypes.data_as(C.c_void_p), dir.ctypes.data_as(C.c_void_p),
+                                       len(pos), C.c_float(tmin), C.c_float(tmax), t.ctypes.data_as(C.c_void_p),
+                                       b.ctypes.data_as(C.c_void_p)), "gbo_trace_rays")
+        return t, b
 
     def scint_wavelength(self, u):
         u = np.ascontiguousarray(u, dtype=np.float32)

@@ -81,6 +81,9 @@ typedef struct gbo_config {
     int32_t  blocks_per_sm;         /* pool kernel: resident blocks per SM (0: occupancy maximum) */
     int32_t  refill_period;         /* pool kernel: steps between refill checks (compaction period, >= 1) */
     int64_t  max_slot;              /* OPTICKS_MAX_SLOT: photons per launch, larger events are sliced (0: no slicing) */
+    int32_t  precision;             /* 0: binary32 as the reference (default); 1: binary64 Newton polish of quadric
+                                       roots when |t| 2^-24 > 1e-4 mm and binary64 position/time accumulators */
+    int32_t  reserved;
 } gbo_config;
 
 /* Result of gbo_autotune: the kernel form chosen and the simulate time of every candidate tried. */
@@ -141,6 +144,10 @@ int         gbo_rng_sequence(int device, uint64_t seed, uint64_t subsequence0, u
                              int32_t per_seq, float* out);
 int         gbo_texture_lookup(gbo_engine* e, int32_t which, const float* xy, int32_t n, float* out);
 int         gbo_scint_wavelength(gbo_engine* e, const float* u, int32_t n, float* out);
+/*   gbo_trace_rays        CSGScan (CSG/CSGScan.cu) : closest-hit distance (-1 on a miss) and boundary for n rays
+ *                         (pos, dir: n x float3), with the engine's precision setting */
+int         gbo_trace_rays(gbo_engine* e, const float* pos, const float* dir, int32_t n, float tmin, float tmax,
+                           float* t_out, uint32_t* boundary_out);
 
 /* ---- event server (continuous batching) ----------------------------------------------------------------------
  * The reference simulates one event per synchronous call (G4CXOpticks::simulate, g4cx/G4CXOpticks.cc:466-486;

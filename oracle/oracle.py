@@ -153,6 +153,19 @@ def simulate(cfg, gs, input_photon=None, event_index=0, photon_offset=0, nthread
     return out, sq
 
 
+def trace64(cfg, pos, dirs, tmin=0.05, tmax=1e9, nthreads=None):
+    """Closest-hit distances in binary64 (orc_csg64.c) for rays given as float32 (n,3) arrays; -1 on a miss."""
+    import os as _os
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    dirs = np.ascontiguousarray(dirs, dtype=np.float32)
+    n = len(pos)
+    t = np.zeros(n, dtype=np.float64)
+    b = np.zeros(n, dtype=np.uint32)
+    lib().orc_trace64_batch(C.byref(cfg.sim.geom), _ptr(pos), _ptr(dirs), C.c_int64(n), C.c_double(tmin),
+                            C.c_double(tmax), _ptr(t), _ptr(b), C.c_int(nthreads or _os.cpu_count() or 1))
+    return t, b
+
+
 def philox_uniforms(seed, subsequence, offset, skip, n, use_ref=False):
     out = np.zeros(n, dtype=np.float32)
     if use_ref:

@@ -1,0 +1,55 @@
+"""Intersection distances of the engine against the binary64 oracle on the large instanced geometry.
+
+Geometry: 17.7 m acrylic sphere of liquid scintillator, 20,000 instanced sensors (depth-3 CSG union of an
+ellipsoid and two cylinders, plus the cap prim) on a 19.4 m Fibonacci sphere.  1M rays: half start uniformly inside
+r < 17 m with isotropic directions (the acrylic sphere roots, t up to 35 m), half start in the water between the
+acrylic and the sensors and aim at the sensors in front of them (the CSG sensor roots).  The engine's distances (binary32, with
+and without its binary64 root polish) are compared with orc_csg64.c for the rays whose closest boundary agrees.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rays(n, seed=5):
+    rng = np.random.default_rng(seed)
+    h = n // 2
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    r = np.concatenate([17000.0 * rng.uniform(0, 1, h) ** (1.0 / 3.0), rng.uniform(17900.0, 18900.0, n - h)])
+    pos = r[:, None] * u
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    aim = 19400.0 * u[h:] + rng.normal(scale=300.0, size=(n - h, 3))     # the sensors in front of the start
+    a = aim - pos[h:]
+    d[h:] = a / np.linalg.norm(a, axis=1, keepdims=True)
+    return pos.astype(np.float32), d.astype(np.float32)
+
+
+def test_fp64_intersection_error_large_geometry(oracle):
+    import __graft_entry__ as ge
+    ge.build()
+    from eic_opticks_gb300 import engine as E, geometry as G
+    arrays = G.large_sphere().arrays()
+    pos, d = rays(1_000_000)
+    t64, b64 = oracle.trace64(oracle.SimConfig(arrays), pos, d)
+    h = len(pos) // 2
+    out = {}
+    for precision in (0, 1):
+        eng = E.Engine(arrays, precision=precision)
+        t, b = eng.trace_rays(pos, d)
+        eng.close()
+        for part, sl in (("inside", slice(0, h)), ("sensors", slice(h, None))):
+            ok = (b[sl] == b64[sl]) & (t64[sl] > 0) & (t[sl] > 0)
+            err = np.abs(t[sl][ok].astype(np.float64) - t64[sl][ok])
+            ulp = np.spacing(t64[sl][ok].astype(np.float32)).astype(np.float64)
+            q = np.percentile(err, [50, 99, 99.9, 99.99])
+            out[precision, part] = (ok.mean(), err.max(), q[2], (err / ulp).max())
+            print("precision %d %-7s: same boundary %.6f, |dt| mm p50 %.3g p99 %.3g p99.9 %.3g p99.99 %.3g max %.3g;"
+                  " > 1e-3 mm %.2e; max %.1f ulp(t)" % (precision, part, ok.mean(), q[0], q[1], q[2], q[3], err.max(),
+                                                         (err > 1e-3).mean(), (err / ulp).max()))
+    for part in ("inside", "sensors"):
+        assert out[0, part][0] > 0.999 and out[1, part][0] > 0.999
+        assert out[1, part][1] <= out[0, part][1] and out[1, part][2] <= out[0, part][2]
+    assert out[1, "inside"][3] <= 1.0          # polished sphere roots: within one binary32 ulp of t
