@@ -252,6 +252,17 @@ def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
     run_batched(None)                                       # warm-up of the server buffers
     batched_s, _ = run_batched(None)
     batched_rate = total_photons / batched_s
+    # the same drain with each batch's copies and kernels issued one by one instead of as one CUDA graph
+    graph_stats = {k: s.stats() for k, s in servers.items()}
+    for s in servers.values():
+        s.close()
+    servers = {k: E.Server(e, slots=2, use_graph=0) for k, e in engines.items()}
+    run_batched(None)
+    direct_s, _ = run_batched(None)
+    for s in servers.values():
+        s.close()
+    servers = {k: E.Server(e, slots=2) for k, e in engines.items()}
+    run_batched(None)
     # ---- latency at `load` x plain capacity, Poisson arrivals
     mean_photons = total_photons / len(events)
     rate_events = load * plain_rate / mean_photons
@@ -280,6 +291,9 @@ def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
         "events": len(events), "photons": total_photons, "submitter_threads": submitters,
         "plain_photons_per_s": plain_rate, "batched_photons_per_s": batched_rate,
         "batched_over_plain": batched_rate / plain_rate,
+        "batched_without_graph_photons_per_s": total_photons / direct_s,
+        "graph": {k: {"launches": v["graph_launches"], "instantiations": v["graph_instantiations"]}
+                  for k, v in graph_stats.items()},
         "arrivals": "Poisson at %.0f%% of plain capacity (%.1f events/s)" % (100 * load, rate_events),
         "batched_latency_ms": {"p50": 1e3 * pct(lat_b, 50), "p99": 1e3 * pct(lat_b, 99)},
         "plain_latency_ms": {"p50": 1e3 * pct(lat_p, 50), "p99": 1e3 * pct(lat_p, 99)},

@@ -54,6 +54,7 @@ struct HBuf {                   // pinned host staging
 struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_kernels = nullptr, ev_done = nullptr;
+    cudaGraphExec_t exec = nullptr;     // the slot's executable graph (graph mode)
     int phase = 0;              // 0 idle, 1 kernels running, 2 hit download running
     std::vector<std::shared_ptr<ServerEvent>> events;
     long long num_photon = 0;
@@ -75,6 +76,8 @@ struct Slot {
         hits_unordered.release(); hits.release(); bitmap.release(); word_prefix.release(); block_sum.release();
         h_gs.release(); h_gs_end.release(); h_ev_photon_begin.release(); h_ev_pos0.release(); h_ev_hit.release();
         h_counters.release(); h_ev_gs_begin.release(); h_input.release(); h_hits.release();
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
         if (ev_kernels) cudaEventDestroy(ev_kernels);
         if (ev_done) cudaEventDestroy(ev_done);
         if (stream) cudaStreamDestroy(stream);
@@ -104,6 +107,59 @@ struct gbo_server {
 };
 
 namespace {
+
+// Every copy, memset and kernel of one batch, in stream order on the slot's stream (captured into a graph in
+// graph mode): gensteps and event tables up, the simulate launch, hit compaction, per-event hit ranges and the
+// counters back to pinned host memory.
+int enqueue_batch(gbo_engine* e, Slot& sl, int n_ev, long long n_gs, long long n_input, long long N, long long words,
+                  long long nblk)
+{
+    cudaStream_t s = sl.stream;
+    if (n_gs) {
+        CU(cudaMemcpyAsync(sl.gs.ptr, sl.h_gs.ptr, n_gs * sizeof(gbo_quad6), cudaMemcpyHostToDevice, s));
+        CU(cudaMemcpyAsync(sl.gs_end.ptr, sl.h_gs_end.ptr, n_gs * sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
+    }
+    CU(cudaMemcpyAsync(sl.ev_gs_begin.ptr, sl.h_ev_gs_begin.ptr, (n_ev + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(sl.ev_photon_begin.ptr, sl.h_ev_photon_begin.ptr, (n_ev + 1) * sizeof(unsigned long long),
+                       cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(sl.ev_pos0.ptr, sl.h_ev_pos0.ptr, n_ev * sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
+    if (n_input) CU(cudaMemcpyAsync(sl.input.ptr, sl.h_input.ptr, n_input * sizeof(gbo_sphoton), cudaMemcpyHostToDevice, s));
+    CU(cudaMemsetAsync(sl.counters.ptr, 0, 4 * sizeof(unsigned long long), s));
+
+    Params P = make_params(e);
+    P.gs = reinterpret_cast<const float4*>(sl.gs.ptr);
+    P.gs_end = sl.gs_end.ptr;
+    P.num_gs = (int)n_gs;
+    P.num_photon = N;
+    P.input_photon = n_input ? sl.input.ptr : nullptr;
+    P.hit_unordered = sl.hits_unordered.ptr;
+    P.hit_count = sl.counters.ptr;
+    P.bitmap = sl.bitmap.ptr;
+    P.num_events = n_ev;
+    P.ev_gs_begin = sl.ev_gs_begin.ptr;
+    P.ev_photon_begin = sl.ev_photon_begin.ptr;
+    P.ev_pos0 = sl.ev_pos0.ptr;
+    P.hit_gidx = sl.hit_gidx.ptr;
+    if (N > 0) {
+        if (e->cfg.kernel_mode == 0) CU(cudaMemsetAsync(sl.bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
+        launch_simulate(e, P, N, sl.counters.ptr + 2, s);
+        CU(cudaGetLastError());
+        k_word_prefix<<<(unsigned)nblk, SCAN_WORDS, 0, s>>>(sl.bitmap.ptr, words, sl.word_prefix.ptr, sl.block_sum.ptr);
+        k_block_offsets<<<1, 1024, 0, s>>>(sl.block_sum.ptr, nblk, sl.block_offset.ptr, sl.counters.ptr + 1);
+        k_gather_unordered<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(sl.hits_unordered.ptr, sl.counters.ptr, 0ull,
+                                                                       sl.bitmap.ptr, sl.word_prefix.ptr,
+                                                                       sl.block_offset.ptr, sl.hits.ptr, sl.hit_gidx.ptr);
+        k_event_hit_ranges<<<(n_ev + 1 + 127) / 128, 128, 0, s>>>(sl.ev_photon_begin.ptr, n_ev, N, sl.bitmap.ptr,
+                                                                  sl.word_prefix.ptr, sl.block_offset.ptr,
+                                                                  sl.counters.ptr + 1, sl.ev_hit.ptr);
+        CU(cudaGetLastError());
+        CU(cudaMemcpyAsync(sl.h_ev_hit.ptr, sl.ev_hit.ptr, (n_ev + 1) * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    } else {
+        for (int k = 0; k <= n_ev; k++) sl.h_ev_hit.ptr[k] = 0;
+    }
+    CU(cudaMemcpyAsync(sl.h_counters.ptr, sl.counters.ptr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    return GBO_OK;
+}
 
 int launch_batch(gbo_server* sv, Slot& sl)
 {
@@ -146,47 +202,39 @@ int launch_batch(gbo_server* sv, Slot& sl)
         (rc = sl.block_sum.ensure(nblk)) || (rc = sl.block_offset.ensure(nblk)) || (rc = sl.hits_unordered.ensure(N)) ||
         (rc = sl.hit_gidx.ensure(N)) || (rc = sl.hits.ensure(N)) || (rc = sl.input.ensure(n_input)))
         return rc;
-    CU(cudaMemcpyAsync(sl.gs.ptr, sl.h_gs.ptr, n_gs * sizeof(gbo_quad6), cudaMemcpyHostToDevice, s));
-    CU(cudaMemcpyAsync(sl.gs_end.ptr, sl.h_gs_end.ptr, n_gs * sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
-    CU(cudaMemcpyAsync(sl.ev_gs_begin.ptr, sl.h_ev_gs_begin.ptr, (n_ev + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
-    CU(cudaMemcpyAsync(sl.ev_photon_begin.ptr, sl.h_ev_photon_begin.ptr, (n_ev + 1) * sizeof(unsigned long long),
-                       cudaMemcpyHostToDevice, s));
-    CU(cudaMemcpyAsync(sl.ev_pos0.ptr, sl.h_ev_pos0.ptr, n_ev * sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
-    if (n_input) CU(cudaMemcpyAsync(sl.input.ptr, sl.h_input.ptr, n_input * sizeof(gbo_sphoton), cudaMemcpyHostToDevice, s));
-    CU(cudaMemsetAsync(sl.counters.ptr, 0, 4 * sizeof(unsigned long long), s));
-
-    Params P = make_params(e);
-    P.gs = reinterpret_cast<const float4*>(sl.gs.ptr);
-    P.gs_end = sl.gs_end.ptr;
-    P.num_gs = (int)n_gs;
-    P.num_photon = N;
-    P.input_photon = n_input ? sl.input.ptr : nullptr;
-    P.hit_unordered = sl.hits_unordered.ptr;
-    P.hit_count = sl.counters.ptr;
-    P.bitmap = sl.bitmap.ptr;
-    P.num_events = n_ev;
-    P.ev_gs_begin = sl.ev_gs_begin.ptr;
-    P.ev_photon_begin = sl.ev_photon_begin.ptr;
-    P.ev_pos0 = sl.ev_pos0.ptr;
-    P.hit_gidx = sl.hit_gidx.ptr;
-    if (N > 0) {
-        if (e->cfg.kernel_mode == 0) CU(cudaMemsetAsync(sl.bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
-        launch_simulate(e, P, N, sl.counters.ptr + 2, s);
-        CU(cudaGetLastError());
-        k_word_prefix<<<(unsigned)nblk, SCAN_WORDS, 0, s>>>(sl.bitmap.ptr, words, sl.word_prefix.ptr, sl.block_sum.ptr);
-        k_block_offsets<<<1, 1024, 0, s>>>(sl.block_sum.ptr, nblk, sl.block_offset.ptr, sl.counters.ptr + 1);
-        k_gather_unordered<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(sl.hits_unordered.ptr, sl.counters.ptr, 0ull,
-                                                                       sl.bitmap.ptr, sl.word_prefix.ptr,
-                                                                       sl.block_offset.ptr, sl.hits.ptr, sl.hit_gidx.ptr);
-        k_event_hit_ranges<<<(n_ev + 1 + 127) / 128, 128, 0, s>>>(sl.ev_photon_begin.ptr, n_ev, N, sl.bitmap.ptr,
-                                                                  sl.word_prefix.ptr, sl.block_offset.ptr,
-                                                                  sl.counters.ptr + 1, sl.ev_hit.ptr);
-        CU(cudaGetLastError());
-        CU(cudaMemcpyAsync(sl.h_ev_hit.ptr, sl.ev_hit.ptr, (n_ev + 1) * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    int rc2 = GBO_OK;
+    if (!sv->cfg.use_graph) {
+        rc2 = enqueue_batch(e, sl, n_ev, n_gs, n_input, N, words, nblk);
     } else {
-        for (int k = 0; k <= n_ev; k++) sl.h_ev_hit.ptr[k] = 0;
+        // capture the batch into a graph, then update the slot's executable graph in place (kernel arguments,
+        // grid sizes and copy sizes change from batch to batch; the topology changes only with input photons or
+        // an empty batch, and then the graph is instantiated afresh)
+        CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        rc2 = enqueue_batch(e, sl, n_ev, n_gs, n_input, N, words, nblk);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+        if (!rc2 && ce != cudaSuccess) rc2 = fail(GBO_ERR_CUDA, "batch capture failed: %s", cudaGetErrorString(ce));
+        if (!rc2 && sl.exec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(sl.exec, graph, &info) != cudaSuccess) {
+                (void)cudaGetLastError();
+                cudaGraphExecDestroy(sl.exec);
+                sl.exec = nullptr;
+            }
+        }
+        if (!rc2 && !sl.exec) {
+            const cudaError_t ie = cudaGraphInstantiate(&sl.exec, graph, 0);
+            if (ie != cudaSuccess) { sl.exec = nullptr; rc2 = fail(GBO_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ie)); }
+            else sv->stats.graph_instantiations++;
+        }
+        if (graph) cudaGraphDestroy(graph);
+        if (!rc2) {
+            const cudaError_t le = cudaGraphLaunch(sl.exec, s);
+            if (le != cudaSuccess) rc2 = fail(GBO_ERR_CUDA, "graph launch failed: %s", cudaGetErrorString(le));
+            else sv->stats.graph_launches++;
+        }
     }
-    CU(cudaMemcpyAsync(sl.h_counters.ptr, sl.counters.ptr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    if (rc2) return rc2;
     CU(cudaEventRecord(sl.ev_kernels, s));
     sl.phase = 1;
     return GBO_OK;
@@ -301,6 +349,7 @@ int gbo_server_config_default(gbo_server_config* c)
     c->hbm_budget_bytes = 120ll << 30;
     c->max_batch_events = 4096;
     c->min_batch_photon = 2ll << 20;
+    c->use_graph = 1;
     return GBO_OK;
 }
 

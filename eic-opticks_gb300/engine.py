@@ -258,12 +258,14 @@ class Engine:
 
 class ServerConfig(C.Structure):
     _fields_ = [("slots", C.c_int32), ("max_batch_events", C.c_int32), ("max_batch_photon", C.c_int64),
-                ("hbm_budget_bytes", C.c_int64), ("min_batch_photon", C.c_int64)]
+                ("hbm_budget_bytes", C.c_int64), ("min_batch_photon", C.c_int64), ("use_graph", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [("events_submitted", C.c_int64), ("events_done", C.c_int64), ("batches", C.c_int64),
-                ("photons", C.c_int64), ("max_batch_photon", C.c_int64)]
+                ("photons", C.c_int64), ("max_batch_photon", C.c_int64), ("graph_launches", C.c_int64),
+                ("graph_instantiations", C.c_int64)]
 
 
 def _server_protos(lib):

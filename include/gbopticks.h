@@ -164,9 +164,13 @@ typedef struct gbo_server_config {
     int64_t max_batch_photon;       /* photons per launch (16M); also bounded by the budget */
     int64_t hbm_budget_bytes;       /* device memory the server's launches may hold (120 GB) */
     int64_t min_batch_photon;       /* while a launch is in flight, start another only once this many photons wait (2M) */
+    int32_t use_graph;              /* 1: each batch's copies and kernels go out as one CUDA graph, captured from the
+                                       stream and applied to the slot's executable graph by update (1) */
+    int32_t reserved;
 } gbo_server_config;
 typedef struct gbo_server_stats {
     int64_t events_submitted, events_done, batches, photons, max_batch_photon;
+    int64_t graph_launches, graph_instantiations;   /* instantiations: first batch of a slot, or topology change */
 } gbo_server_stats;
 
 int  gbo_server_config_default(gbo_server_config* cfg);

@@ -53,3 +53,34 @@ def test_fp64_intersection_error_large_geometry(oracle):
         assert out[0, part][0] > 0.999 and out[1, part][0] > 0.999
         assert out[1, part][1] <= out[0, part][1] and out[1, part][2] <= out[0, part][2]
     assert out[1, "inside"][3] <= 1.0          # polished sphere roots: within one binary32 ulp of t
+
+
+@pytest.mark.parametrize("name", ["nested_boxes", "crystal_array", "water_cube"])
+def test_fp64_intersection_error_other_geometries(oracle, name):
+    """1M rays from points uniform in the inner 95% of the world box, isotropic directions; same report and
+    bounds as above (box faces are single-division roots, so both modes sit within a few ulp of t)."""
+    import __graft_entry__ as ge
+    ge.build()
+    from eic_opticks_gb300 import engine as E, geometry as G
+    arrays = getattr(G, name)().arrays()
+    half = np.abs(arrays["prim"].view(np.float32)[0, 2, :3]).min() * 0.95
+    rng = np.random.default_rng(11)
+    n = 1_000_000
+    pos = rng.uniform(-half, half, size=(n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    t64, b64 = oracle.trace64(oracle.SimConfig(arrays), pos, d)
+    out = {}
+    for precision in (0, 1):
+        eng = E.Engine(arrays, precision=precision)
+        t, b = eng.trace_rays(pos, d)
+        eng.close()
+        ok = (b == b64) & (t64 > 0) & (t > 0)
+        err = np.abs(t[ok].astype(np.float64) - t64[ok])
+        ulp = np.spacing(t64[ok].astype(np.float32)).astype(np.float64)
+        q = np.percentile(err, [50, 99, 99.9])
+        out[precision] = (ok.mean(), err.max(), (err / ulp).max())
+        print("%s precision %d: same boundary %.6f, |dt| mm p50 %.3g p99 %.3g p99.9 %.3g max %.3g; max %.1f ulp(t)"
+              % (name, precision, ok.mean(), q[0], q[1], q[2], err.max(), (err / ulp).max()))
+    assert out[0][0] > 0.999 and out[1][0] > 0.999
+    assert out[1][1] <= out[0][1] * 1.0001 + 1e-9

@@ -30,8 +30,8 @@ def make_events(rng, n, geom_kind, wc=None):
     return events
 
 
-@pytest.mark.parametrize("kind", ["crystal", "water"])
-def test_served_events_equal_alone(E, kind):
+@pytest.mark.parametrize("kind,use_graph", [("crystal", 1), ("water", 1), ("crystal", 0)])
+def test_served_events_equal_alone(E, kind, use_graph):
     from eic_opticks_gb300 import geometry as G
     geom = G.crystal_array() if kind == "crystal" else G.water_cube()
     arrays = geom.arrays()
@@ -44,7 +44,7 @@ def test_served_events_equal_alone(E, kind):
     eng_alone.close()
 
     eng = E.Engine(arrays)
-    srv = E.Server(eng, slots=3, max_batch_events=16)
+    srv = E.Server(eng, slots=3, max_batch_events=16, use_graph=use_graph)
     tickets = {}
     lock = threading.Lock()
 
@@ -70,6 +70,10 @@ def test_served_events_equal_alone(E, kind):
         srv.release(t)
     st = srv.stats()
     assert st["events_done"] == len(events) and st["batches"] < len(events)   # events were really packed
+    assert st["graph_launches"] == (st["batches"] if use_graph else 0)
+    if use_graph:       # one instantiation per slot; later batches update it in place
+        print("batches %d, graph instantiations %d" % (st["batches"], st["graph_instantiations"]))
+        assert 1 <= st["graph_instantiations"] <= 3
     srv.close()
     eng.close()
 
