@@ -36,6 +36,11 @@ METRIC = "propagated photons/s, batched vs plain per-event launch on 1 GB300; p9
 UNIT = "photons/s"
 WORKLOAD = "crystal_array_8x8_CsI_scint_2000gs_poisson5000"
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes (read + write) per photon of the simulate kernel from one ncu capture of a 998,319-photon crystal-array
+# event (200 gensteps), scaled to the benchmark event by its photon count: gensteps and hits, the only DRAM traffic,
+# both grow with the photons
+TRAFFIC_B_PER_PHOTON = {"crystal_array": (501248.0 + 27392.0) / 998319}
+TRAFFIC_SOURCE = "profiles/k_simulate_pool_crystal_array.md (ncu, 1M-photon event, scaled by photons)"
 
 
 def peaks():
@@ -102,73 +107,110 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-LARGE_SPHERE = "large_sphere_20000_sensors_scint_100M"
+WORKLOADS = {
+    "nested_boxes": "nested_boxes_torch_100k_input_photons",
+    "crystal_array": WORKLOAD,
+    "water_cube": "water_cube_cerenkov_1000gs",
+    "large_sphere": "large_sphere_20000_sensors_scint_100M",
+}
 
 
 def workload(seed=1, num_gs=2000, kind="crystal_array"):
-    """crystal_array: num_gs Poisson(5000) scintillation gensteps in the 8x8 CsI array (the headline event).
-    large_sphere: 20,000 gensteps of 5,000 photons (100M) uniform in r < 17 m of the 17.7 m liquid-scintillator
-    sphere with 20,000 instanced CSG sensors."""
+    """One event of each benchmark configuration: (geometry arrays, gensteps, input photons or None).
+
+    nested_boxes : 100,000 input photons at the origin, isotropic, 420 nm, in the vacuum/lead/air/water boxes.
+    crystal_array: num_gs Poisson(5000) scintillation gensteps in the 8x8 CsI array (the headline event).
+    water_cube   : 1,000 Frank-Tamm Cerenkov steps (2 mm, beta 0.8-1) in the 1 m dispersive water cube.
+    large_sphere : 20,000 gensteps of 5,000 photons (100M) uniform in r < 17 m of the 17.7 m liquid-scintillator
+                   sphere with 20,000 instanced CSG sensors."""
     ge.load_package()
     from eic_opticks_gb300 import geometry as G, gensteps as GS
+    if kind == "nested_boxes":
+        inp = GS.isotropic_photons(100_000, seed=seed)
+        return G.nested_boxes().arrays(), GS.input_photon_genstep(len(inp)), inp
+    if kind == "water_cube":
+        g = G.water_cube()
+        return g.arrays(), GS.water_cerenkov_gensteps(g, 1000, seed=seed), None
     if kind == "large_sphere":
-        return G.large_sphere().arrays(), GS.sphere_scint_gensteps(20000, 5000, seed=seed)
-    geom = G.crystal_array().arrays()
-    gs = GS.crystal_scint_gensteps(num_gs, 5000, seed=seed)
-    return geom, gs
+        return G.large_sphere().arrays(), GS.sphere_scint_gensteps(20000, 5000, seed=seed), None
+    return G.crystal_array().arrays(), GS.crystal_scint_gensteps(num_gs, 5000, seed=seed), None
 
 
-def cpu_baseline(geom, gs, target_s=12.0, threads=None):
-    """The oracle on a bounded sample (first gensteps of the event) using all host cores."""
+def photon_sample(gs, inp, n):
+    """The first n photons of an event: leading gensteps, the last one cut short (input photons sliced alike)."""
+    counts = gs.view(np.uint32)[:, 0, 3].astype(np.int64)
+    end = np.cumsum(counts)
+    k = int(np.searchsorted(end, n))
+    if k >= len(gs):
+        return gs, inp, int(end[-1]) if len(end) else 0
+    sample = gs[:k + 1].copy()
+    sample.view(np.uint32)[k, 0, 3] = n - (int(end[k - 1]) if k > 0 else 0)
+    return sample, (inp[:n] if inp is not None else None), n
+
+
+def cpu_baseline(geom, gs, target_s=12.0, threads=None, inp=None):
+    """The oracle on a bounded sample (the first photons of the event) using all host cores: the sample grows
+    from 256 photons until one timed run takes about a quarter of target_s."""
     O = ge.load_oracle()
     O.build()
     cfg = O.SimConfig(geom)
     threads = threads or os.cpu_count() or 1
-    n_gs = 4
+    total = int(gs.view(np.uint32)[:, 0, 3].astype(np.int64).sum())
+    want = min(256, total)
     while True:
-        sample = gs[:n_gs]
+        sample, sinp, n = photon_sample(gs, inp, want)
         t0 = time.perf_counter()
-        out, _ = O.simulate(cfg, sample, nthreads=threads, seq=False)
+        out, _ = O.simulate(cfg, sample, input_photon=sinp, nthreads=threads, seq=False)
         dt = time.perf_counter() - t0
-        if dt > target_s / 4 or n_gs >= len(gs):
+        if dt > target_s / 4 or n >= total:
             break
-        n_gs = min(len(gs), max(n_gs + 1, int(n_gs * target_s / 4 / max(dt, 1e-3))))
-    n = len(out)
+        want = min(total, max(want + 1, int(want * target_s / 4 / max(dt, 1e-3))))
     return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d of %d gensteps (%d photons), %.1f s" % (n_gs, len(gs), n, dt)}
+            "sample": "first %d of %d photons of the event, %.1f s" % (n, total, dt)}
 
 
 def reference_arm(args):
-    """--impl reference : the reference's CPU implementation of the path on the host cores."""
-    geom, gs = workload()
+    """--impl reference : the reference's CPU implementation of the path on the host cores.
+
+    oracle/_ref/libref.so (the reference's own headers compiled for the host) when it was built on this machine,
+    else the oracle port.  Each step simulates the next `threads` gensteps of the crystal-array event, one genstep
+    per host thread, each with its event photon offset, so the photons are exactly those of the full event."""
+    from concurrent.futures import ThreadPoolExecutor
+    geom, gs, _ = workload()
     O = ge.load_oracle()
     O.build()
     use_ref = O.reflib() is not None
     kind = "reference" if use_ref else "port"
     cfg = O.SimConfig(geom)
     threads = os.cpu_count() or 1
-    sample_gs = 2
+    counts = gs.view(np.uint32)[:, 0, 3].astype(np.int64)
+    begin = np.concatenate([[0], np.cumsum(counts)])
+    sample_gs = threads
     times, photons = [], 0
-    for step in range(args.warmup + args.steps):
-        sample = gs[step * sample_gs % len(gs):][:sample_gs]
-        t0 = time.perf_counter()
-        if use_ref:
-            out, _ = O.simulate(cfg, sample, seq=False, use_ref=True)          # single-threaded driver
-        else:
-            out, _ = O.simulate(cfg, sample, nthreads=threads, seq=False)
-        dt = time.perf_counter() - t0
-        if step >= args.warmup:
-            times.append(dt)
-            photons += len(out)
+
+    def one(k):
+        out, _ = O.simulate(cfg, gs[k:k + 1], photon_offset=int(begin[k]), seq=False, use_ref=use_ref)
+        return len(out)
+
+    with ThreadPoolExecutor(max_workers=threads) as pool:
+        for step in range(args.warmup + args.steps):
+            first = step * sample_gs % len(gs)
+            ks = [(first + j) % len(gs) for j in range(sample_gs)]
+            t0 = time.perf_counter()
+            n = sum(pool.map(one, ks))
+            dt = time.perf_counter() - t0
+            if step >= args.warmup:
+                times.append(dt)
+                photons += n
     total = sum(times)
     value = photons / total
-    cores = 1 if use_ref else threads
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / max(1, len(times)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "sample_gensteps_per_step": sample_gs},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
-                             "sample": "%d gensteps per step (~%d photons)" % (sample_gs, photons // max(1, len(times)))},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": "%d gensteps per step, one per thread (~%d photons)"
+                                       % (sample_gs, photons // max(1, len(times)))},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -209,6 +251,15 @@ def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
     from eic_opticks_gb300 import engine as E
     arrays, events = mixed_events(num_events, lo=lo, hi=hi)
     engines = {k: E.Engine(a) for k, a in arrays.items()}
+    # kernel form of each engine picked by the autotuner on a sample event of its kind (setup)
+    tuned = {}
+    for kind, eng in engines.items():
+        from eic_opticks_gb300 import geometry as G, gensteps as GS
+        sample = (GS.crystal_scint_gensteps(200, 5000, seed=99) if kind == "crystal" else
+                  GS.water_cerenkov_gensteps(G.water_cube(), 2000, seed=99))
+        r = eng.autotune(0, sample, trials=2)
+        tuned[kind] = {"mode": "photon pool" if r["kernel_mode"] == 0 else "one thread per photon",
+                       "refill_min": r["refill_min"], "refill_period": r["refill_period"]}
     photons = {id(ev[2]): int(ev[2].view(np.uint32)[:, 0, 3].astype(np.int64).sum()) for ev in events}
     total_photons = sum(photons.values())
     for kind, eid, gs in events[:4]:                          # warm-up
@@ -298,7 +349,59 @@ def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
         "batched_latency_ms": {"p50": 1e3 * pct(lat_b, 50), "p99": 1e3 * pct(lat_b, 99)},
         "plain_latency_ms": {"p50": 1e3 * pct(lat_p, 50), "p99": 1e3 * pct(lat_p, 99)},
         "batches": {k: v["batches"] for k, v in stats.items()},
+        "kernel": tuned,
+        "server": {"slots": 2, "target_batch_photon": 4 << 20, "min_batch_photon": 2 << 20,
+                   "hbm_budget_bytes": 120 << 30},
     }
+
+
+def same_config_batching(geom, kind, n_events, tune, submitters=16):
+    """n_events events of one configuration (seeds differ): one synchronous gbo_simulate + hit download per event,
+    against the server draining all of them submitted at once (continuous batching, graph mode)."""
+    import threading
+    from eic_opticks_gb300 import engine as E
+    events = [workload(seed=100 + k, kind=kind)[1:] for k in range(n_events)]
+    photons = sum(int(g.view(np.uint32)[:, 0, 3].astype(np.int64).sum()) for g, _ in events)
+    eng = E.Engine(geom, kernel_mode=tune["kernel_mode"], refill_min=tune["refill_min"],
+                   refill_period=tune["refill_period"])
+    eng.simulate(0, *events[0])
+    t0 = time.perf_counter()
+    for k, (g, inp) in enumerate(events):
+        eng.simulate(500 + k, g, inp)
+        eng.hits()
+    plain_s = time.perf_counter() - t0
+    srv = E.Server(eng, slots=2)
+
+    def drain():
+        tickets = [None] * n_events
+        start = time.perf_counter()
+
+        def producer(idx):
+            for i in idx:
+                tickets[i] = srv.submit(500 + i, *events[i])
+
+        th = [threading.Thread(target=producer, args=(range(j, n_events, submitters),)) for j in range(submitters)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        for t in tickets:
+            srv.wait(t)
+        el = time.perf_counter() - start
+        lat = []
+        for t in tickets:
+            lat.append(srv.info(t)["latency_s"])
+            srv.release(t)
+        return el, lat
+
+    drain()
+    batched_s, lat = drain()
+    st = srv.stats()
+    srv.close()
+    eng.close()
+    return {"events": n_events, "photons": photons, "plain_photons_per_s": photons / plain_s,
+            "batched_photons_per_s": photons / batched_s, "batched_over_plain": plain_s / batched_s,
+            "batches": st["batches"], "drain_latency_ms": {"p50": 1e3 * pct(lat, 50), "p99": 1e3 * pct(lat, 99)}}
 
 
 def dist_init(args):
@@ -319,7 +422,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the batched-serving comparison")
     ap.add_argument("--gensteps", type=int, default=2000, help="gensteps per event (2000 is the benchmark workload)")
-    ap.add_argument("--workload", default="crystal_array", choices=["crystal_array", "large_sphere"])
+    ap.add_argument("--workload", default="crystal_array", choices=sorted(WORKLOADS))
+    ap.add_argument("--batch-events", type=int, default=None,
+                    help="events of the workload for the same-configuration plain vs batched comparison")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
                     help="1: binary64 root polish and position/time accumulators")
     args = ap.parse_args()
@@ -341,19 +446,25 @@ def main():
         dist.barrier()
     ge.load_package()
     from eic_opticks_gb300 import engine as E
-    geom, gs = workload(seed=1 + rank, num_gs=args.gensteps, kind=args.workload)
+    geom, gs, inp = workload(seed=1 + rank, num_gs=args.gensteps, kind=args.workload)
     n_photon = int(gs.view(np.uint32)[:, 0, 3].astype(np.int64).sum())
+    n_inp = 0 if inp is None else len(inp)
     eng = E.Engine(geom, device=local, precision=args.precision)
     # kernel form picked by the autotuner on a 10% sample of the workload (setup, outside the timed region)
-    tune = eng.autotune(0, gs[: max(1, len(gs) // 10)], trials=2)
+    if inp is None:
+        tune = eng.autotune(0, gs[: max(1, len(gs) // 10)], trials=2)
+    else:
+        tune = eng.autotune(0, gs, inp, trials=2)
 
     d_gs = torch.from_numpy(gs.copy()).to(f"cuda:{local}")
+    d_inp = torch.from_numpy(inp.view(np.uint8).copy()).to(f"cuda:{local}") if inp is not None else None
+    inp_ptr = d_inp.data_ptr() if d_inp is not None else 0
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     # ---- device-resident throughput (value) ----
     for w in range(args.warmup):
-        eng.simulate_device(w, d_gs.data_ptr(), len(gs))
+        eng.simulate_device(w, d_gs.data_ptr(), len(gs), inp_ptr, n_inp)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -363,7 +474,7 @@ def main():
             flush.zero_()
             torch.cuda.synchronize()
             start.record()
-            hits = eng.simulate_device(1000 + k, d_gs.data_ptr(), len(gs))
+            hits = eng.simulate_device(1000 + k, d_gs.data_ptr(), len(gs), inp_ptr, n_inp)
             end.record()
             end.synchronize()
             ms.append(start.elapsed_time(end))
@@ -381,12 +492,12 @@ def main():
     # ---- end to end through the C ABI with host buffers (e2e) ----
     hits_host = None
     e2e_ms = []
-    h2d = gs.nbytes
+    h2d = gs.nbytes + (inp.nbytes if inp is not None else 0)
     for k in range(args.warmup + args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        nh = eng.simulate(2000 + k, gs)
+        nh = eng.simulate(2000 + k, gs, inp)
         if hits_host is None or len(hits_host) < nh:
             hits_host = np.zeros(max(nh, 1) * 2, dtype=E.L.PHOTON)
         eng.hits(out=hits_host[:nh])
@@ -408,7 +519,7 @@ def main():
 
     hbm, peak_kind = peaks()
     f_hit = hits / n_photon
-    b_alg = 96.0 / (n_photon / len(gs)) + 4 + 64 + 64 + 64 * f_hit
+    b_alg = 96.0 / (n_photon / len(gs)) + 4 + 64 + 64 + 64 * f_hit + (64.0 if inp is not None else 0.0)
     sim_mean = float(np.mean(sim_ms))
     achieved = b_alg * n_photon / (sim_mean * 1e-3) / 1e9
     line = {
@@ -416,8 +527,8 @@ def main():
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if not args.precision else "f32+f64",
         "data": "synthetic (seeded numpy gensteps with the reference genstep layout)",
-        "config": {"workload": (LARGE_SPHERE if args.workload == "large_sphere" else
-                                WORKLOAD if args.gensteps == 2000 else WORKLOAD + "_%dgs" % args.gensteps),
+        "config": {"workload": (WORKLOADS[args.workload] if args.workload != "crystal_array" or args.gensteps == 2000
+                                else WORKLOAD + "_%dgs" % args.gensteps),
                    "precision": "binary64 root polish + accumulators" if args.precision else "binary32",
                    "photons_per_step": n_photon, "gensteps_per_step": len(gs),
                    "hits_per_step": hits, "path": "plain: one event per launch", "l2": "flushed (256 MB write) between timed steps",
@@ -428,15 +539,23 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "kernel": "k_simulate", "bytes_per_photon": b_alg,
+                     "traffic": (TRAFFIC_B_PER_PHOTON[args.workload] * n_photon
+                                 if args.workload in TRAFFIC_B_PER_PHOTON and not args.precision else None),
+                     "traffic_source": TRAFFIC_SOURCE if args.workload in TRAFFIC_B_PER_PHOTON else None,
+                     "kernel": "k_simulate_pool" if tune["kernel_mode"] == 0 else "k_simulate",
+                     "bytes_per_photon": b_alg,
                      "kernel_ms": sim_mean, "peak_source": peak_kind},
         "clocks": clk.summary(),
     }
     if not args.no_serving and world == 1:
         line["serving"] = serving_bench()                                   # the 1e3-1e7 serving stream
         line["serving_small_events"] = serving_bench(num_events=1500, lo=3.0, hi=5.0)
+    n_batch = args.batch_events if args.batch_events is not None else (
+        {"nested_boxes": 64, "water_cube": 16, "crystal_array": 8, "large_sphere": 2}[args.workload])
+    if n_batch > 0 and world == 1 and not args.precision:
+        line["same_config_batching"] = same_config_batching(geom, args.workload, n_batch, tune)
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(geom, gs)
+        line["cpu_baseline"] = cpu_baseline(geom, gs, inp=inp)
     print(json.dumps(line))
     if dist:
         dist.barrier()

@@ -32,6 +32,9 @@ namespace gbo {
 #ifndef GBO_SIM_MINB
 #define GBO_SIM_MINB 1              // minimum resident blocks per SM asked of ptxas for the simulate kernels
 #endif
+#ifndef GBO_POOL_MINB
+#define GBO_POOL_MINB 1             // the same for the persistent photon-pool kernel
+#endif
 constexpr int SIM_BLOCK = 128;
 constexpr int SCAN_WORDS = 256;     // words per block in k_word_prefix
 
@@ -59,6 +62,8 @@ struct Params {
     const int* ev_gs_begin;
     const unsigned long long* ev_photon_begin;
     const unsigned long long* ev_pos0;
+    const unsigned long long* ev_photon_offset;     // event-local index of each entry's first photon (a piece of a
+                                                    // sliced event starts past 0); nullptr: all 0
     unsigned long long* hit_gidx;           // launch index of each unordered hit (batched launches)
 };
 
@@ -141,6 +146,7 @@ GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng)
             if (__ldg(P.ev_gs_begin + m) <= lo) a = m; else z = m - 1;
         }
         photon_idx = (unsigned long long)idx - __ldg(P.ev_photon_begin + a);
+        if (P.ev_photon_offset) photon_idx += __ldg(P.ev_photon_offset + a);
         pos0 = __ldg(P.ev_pos0 + a);
     }
     rng_init(rng, P.seed, photon_idx, pos0);
@@ -161,7 +167,7 @@ GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng)
 }
 
 template <bool TREE, bool PRECISE>
-__global__ void __launch_bounds__(SIM_BLOCK) k_simulate_pool(const __grid_constant__ Params P,
+__global__ void __launch_bounds__(SIM_BLOCK, GBO_POOL_MINB) k_simulate_pool(const __grid_constant__ Params P,
                                                              unsigned long long* pool, int refill_min, int period)
 {
     const unsigned lane = threadIdx.x & 31u;

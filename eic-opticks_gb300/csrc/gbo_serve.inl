@@ -7,9 +7,11 @@
 // simulate kernel, events kept apart by their genstep and photon ranges), runs up to `slots` such batches at once
 // on separate CUDA streams so a new batch fills the SMs that the previous one's tail leaves idle, admits events
 // only while the batch's device buffers fit the HBM budget, and hands back each event's hits in photon order with
-// its submit-to-hits latency.  Each event's results are those it gets alone: its photons keep their event-local
-// indices and the event's own Philox stream positions.
+// its submit-to-hits latency.  An event larger than a batch runs as genstep-aligned pieces in successive batches
+// (the reference slices a large event the same way, qudarap/QSim.cc:481-529).  Each event's results are those it
+// gets alone: its photons keep their event-local indices and the event's own Philox stream positions.
 
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -31,6 +33,20 @@ struct ServerEvent {
     int status = 0;             // 0 waiting, 1 on the GPU, 2 done, 3 failed
     std::vector<gbo_sphoton> hits;
     std::string error;
+    // an event larger than a batch runs as several pieces (genstep ranges), possibly in several slots at once
+    int64_t next_gs = 0;                // first genstep not yet handed to a batch
+    long long next_photon = 0;          // event-local index of that genstep's first photon
+    int pieces_launched = 0, pieces_done = 0;
+    bool all_launched = false;
+    std::vector<std::vector<gbo_sphoton>> piece_hits;
+};
+
+// One batch entry: gensteps [g0, g1) of an event, whose photons are the event's [photon_offset, +num_photon)
+struct Piece {
+    std::shared_ptr<ServerEvent> ev;
+    int64_t g0 = 0, g1 = 0;
+    long long photon_offset = 0, num_photon = 0;
+    int index = 0;
 };
 
 template <typename T>
@@ -56,26 +72,28 @@ struct Slot {
     cudaEvent_t ev_kernels = nullptr, ev_done = nullptr;
     cudaGraphExec_t exec = nullptr;     // the slot's executable graph (graph mode)
     int phase = 0;              // 0 idle, 1 kernels running, 2 hit download running
-    std::vector<std::shared_ptr<ServerEvent>> events;
+    std::vector<Piece> pieces;
     long long num_photon = 0;
+    bool big = false;           // holds a piece of at least target_batch_photon photons
     unsigned long long num_hit = 0;
     DBuf<gbo_quad6> gs;
-    DBuf<unsigned long long> gs_end, ev_photon_begin, ev_pos0, block_offset, counters, hit_gidx, ev_hit;
+    DBuf<unsigned long long> gs_end, ev_photon_begin, ev_pos0, ev_photon_offset, block_offset, counters, hit_gidx, ev_hit;
     DBuf<int> ev_gs_begin;
     DBuf<gbo_sphoton> input, hits_unordered, hits;
     DBuf<uint32_t> bitmap, word_prefix, block_sum;
     HBuf<gbo_quad6> h_gs;
-    HBuf<unsigned long long> h_gs_end, h_ev_photon_begin, h_ev_pos0, h_ev_hit, h_counters;
+    HBuf<unsigned long long> h_gs_end, h_ev_photon_begin, h_ev_pos0, h_ev_photon_offset, h_ev_hit, h_counters;
     HBuf<int> h_ev_gs_begin;
-    HBuf<gbo_sphoton> h_input, h_hits;
+    HBuf<gbo_sphoton> h_hits;
 
     void release()
     {
-        gs.release(); gs_end.release(); ev_photon_begin.release(); ev_pos0.release(); block_offset.release();
-        counters.release(); hit_gidx.release(); ev_hit.release(); ev_gs_begin.release(); input.release();
-        hits_unordered.release(); hits.release(); bitmap.release(); word_prefix.release(); block_sum.release();
-        h_gs.release(); h_gs_end.release(); h_ev_photon_begin.release(); h_ev_pos0.release(); h_ev_hit.release();
-        h_counters.release(); h_ev_gs_begin.release(); h_input.release(); h_hits.release();
+        gs.release(); gs_end.release(); ev_photon_begin.release(); ev_pos0.release(); ev_photon_offset.release();
+        block_offset.release(); counters.release(); hit_gidx.release(); ev_hit.release(); ev_gs_begin.release();
+        input.release(); hits_unordered.release(); hits.release(); bitmap.release(); word_prefix.release();
+        block_sum.release(); h_gs.release(); h_gs_end.release(); h_ev_photon_begin.release(); h_ev_pos0.release();
+        h_ev_photon_offset.release(); h_ev_hit.release(); h_counters.release(); h_ev_gs_begin.release();
+        h_hits.release();
         if (exec) cudaGraphExecDestroy(exec);
         exec = nullptr;
         if (ev_kernels) cudaEventDestroy(ev_kernels);
@@ -85,6 +103,12 @@ struct Slot {
         stream = nullptr;
     }
 };
+
+// big batches in flight per GPU, over every server of the process (one server per geometry shares the GPU)
+constexpr int SERVE_MAX_DEVICES = 64;
+std::atomic<int> g_big_in_flight[SERVE_MAX_DEVICES];
+
+std::atomic<int>& big_counter(int device) { return g_big_in_flight[device >= 0 && device < SERVE_MAX_DEVICES ? device : 0]; }
 
 // device bytes per photon slot of a batch: bitmap + prefix bits, unordered + ordered hit capacity, hit index
 constexpr double SERVE_BYTES_PER_PHOTON = 0.25 + 64.0 + 64.0 + 8.0;
@@ -109,9 +133,9 @@ struct gbo_server {
 namespace {
 
 // Every copy, memset and kernel of one batch, in stream order on the slot's stream (captured into a graph in
-// graph mode): gensteps and event tables up, the simulate launch, hit compaction, per-event hit ranges and the
-// counters back to pinned host memory.
-int enqueue_batch(gbo_engine* e, Slot& sl, int n_ev, long long n_gs, long long n_input, long long N, long long words,
+// graph mode): gensteps and entry tables up, the simulate launch, hit compaction, per-entry hit ranges and the
+// counters back to pinned host memory.  Input photons are already on the device (copied before, see launch_batch).
+int enqueue_batch(gbo_engine* e, Slot& sl, int n_ev, long long n_gs, bool has_input, long long N, long long words,
                   long long nblk)
 {
     cudaStream_t s = sl.stream;
@@ -123,7 +147,8 @@ int enqueue_batch(gbo_engine* e, Slot& sl, int n_ev, long long n_gs, long long n
     CU(cudaMemcpyAsync(sl.ev_photon_begin.ptr, sl.h_ev_photon_begin.ptr, (n_ev + 1) * sizeof(unsigned long long),
                        cudaMemcpyHostToDevice, s));
     CU(cudaMemcpyAsync(sl.ev_pos0.ptr, sl.h_ev_pos0.ptr, n_ev * sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
-    if (n_input) CU(cudaMemcpyAsync(sl.input.ptr, sl.h_input.ptr, n_input * sizeof(gbo_sphoton), cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(sl.ev_photon_offset.ptr, sl.h_ev_photon_offset.ptr, n_ev * sizeof(unsigned long long),
+                       cudaMemcpyHostToDevice, s));
     CU(cudaMemsetAsync(sl.counters.ptr, 0, 4 * sizeof(unsigned long long), s));
 
     Params P = make_params(e);
@@ -131,7 +156,7 @@ int enqueue_batch(gbo_engine* e, Slot& sl, int n_ev, long long n_gs, long long n
     P.gs_end = sl.gs_end.ptr;
     P.num_gs = (int)n_gs;
     P.num_photon = N;
-    P.input_photon = n_input ? sl.input.ptr : nullptr;
+    P.input_photon = has_input ? sl.input.ptr : nullptr;
     P.hit_unordered = sl.hits_unordered.ptr;
     P.hit_count = sl.counters.ptr;
     P.bitmap = sl.bitmap.ptr;
@@ -139,6 +164,7 @@ int enqueue_batch(gbo_engine* e, Slot& sl, int n_ev, long long n_gs, long long n
     P.ev_gs_begin = sl.ev_gs_begin.ptr;
     P.ev_photon_begin = sl.ev_photon_begin.ptr;
     P.ev_pos0 = sl.ev_pos0.ptr;
+    P.ev_photon_offset = sl.ev_photon_offset.ptr;
     P.hit_gidx = sl.hit_gidx.ptr;
     if (N > 0) {
         if (e->cfg.kernel_mode == 0) CU(cudaMemsetAsync(sl.bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
@@ -165,30 +191,31 @@ int launch_batch(gbo_server* sv, Slot& sl)
 {
     gbo_engine* e = sv->e;
     cudaStream_t s = sl.stream;
-    const int n_ev = (int)sl.events.size();
-    long long n_gs = 0, n_input = 0;
-    for (auto& ev : sl.events) { n_gs += (long long)ev->gs.size(); n_input += (long long)ev->input.size(); }
+    const int n_ev = (int)sl.pieces.size();
+    long long n_gs = 0;
+    bool has_input = false;
+    for (const Piece& pc : sl.pieces) { n_gs += pc.g1 - pc.g0; has_input |= !pc.ev->input.empty(); }
     int rc;
     if ((rc = sl.h_gs.ensure(n_gs)) || (rc = sl.h_gs_end.ensure(n_gs)) || (rc = sl.h_ev_gs_begin.ensure(n_ev + 1)) ||
         (rc = sl.h_ev_photon_begin.ensure(n_ev + 1)) || (rc = sl.h_ev_pos0.ensure(n_ev)) ||
-        (rc = sl.h_ev_hit.ensure(n_ev + 1)) || (rc = sl.h_counters.ensure(4)) || (rc = sl.h_input.ensure(n_input)))
+        (rc = sl.h_ev_photon_offset.ensure(n_ev)) || (rc = sl.h_ev_hit.ensure(n_ev + 1)) || (rc = sl.h_counters.ensure(4)))
         return rc;
-    long long g = 0, p = 0, ip = 0;
+    long long g = 0;
     unsigned long long total = 0;
     for (int k = 0; k < n_ev; k++) {
-        ServerEvent& ev = *sl.events[k];
+        const Piece& pc = sl.pieces[k];
+        const ServerEvent& ev = *pc.ev;
         sl.h_ev_gs_begin.ptr[k] = (int)g;
-        sl.h_ev_photon_begin.ptr[k] = (unsigned long long)p;
+        sl.h_ev_photon_begin.ptr[k] = total;
         sl.h_ev_pos0.ptr[k] = e->cfg.rng_offset + e->cfg.event_skipahead * (uint64_t)(ev.event_id < 0 ? 0 : ev.event_id);
-        for (const gbo_quad6& q : ev.gs) {
+        sl.h_ev_photon_offset.ptr[k] = (unsigned long long)pc.photon_offset;
+        for (int64_t i = pc.g0; i < pc.g1; i++) {
+            const gbo_quad6& q = ev.gs[(size_t)i];
             sl.h_gs.ptr[g] = q;
             total += q.q[0].u[3];
             sl.h_gs_end.ptr[g] = total;
             g++;
         }
-        if (!ev.input.empty()) std::memcpy(sl.h_input.ptr + ip, ev.input.data(), ev.input.size() * sizeof(gbo_sphoton));
-        ip += (long long)ev.input.size();
-        p = (long long)total;
     }
     sl.h_ev_gs_begin.ptr[n_ev] = (int)g;
     sl.h_ev_photon_begin.ptr[n_ev] = total;
@@ -197,20 +224,34 @@ int launch_batch(gbo_server* sv, Slot& sl)
     const long long words = (N + 31) / 32;
     const long long nblk = (words + SCAN_WORDS - 1) / SCAN_WORDS;
     if ((rc = sl.gs.ensure(n_gs)) || (rc = sl.gs_end.ensure(n_gs)) || (rc = sl.ev_gs_begin.ensure(n_ev + 1)) ||
-        (rc = sl.ev_photon_begin.ensure(n_ev + 1)) || (rc = sl.ev_pos0.ensure(n_ev)) || (rc = sl.ev_hit.ensure(n_ev + 1)) ||
+        (rc = sl.ev_photon_begin.ensure(n_ev + 1)) || (rc = sl.ev_pos0.ensure(n_ev)) ||
+        (rc = sl.ev_photon_offset.ensure(n_ev)) || (rc = sl.ev_hit.ensure(n_ev + 1)) ||
         (rc = sl.counters.ensure(4)) || (rc = sl.bitmap.ensure(words)) || (rc = sl.word_prefix.ensure(words)) ||
         (rc = sl.block_sum.ensure(nblk)) || (rc = sl.block_offset.ensure(nblk)) || (rc = sl.hits_unordered.ensure(N)) ||
-        (rc = sl.hit_gidx.ensure(N)) || (rc = sl.hits.ensure(N)) || (rc = sl.input.ensure(n_input)))
+        (rc = sl.hit_gidx.ensure(N)) || (rc = sl.hits.ensure(N)) || (has_input && (rc = sl.input.ensure(N))))
         return rc;
+    // input photons go up straight from each event's own copy, one copy per piece at the piece's launch position
+    // (outside any graph: the source is pageable host memory)
+    if (has_input) {
+        for (int k = 0; k < n_ev; k++) {
+            const Piece& pc = sl.pieces[k];
+            const std::vector<gbo_sphoton>& in = pc.ev->input;
+            const long long avail = (long long)in.size() - pc.photon_offset;
+            const long long n = avail < pc.num_photon ? avail : pc.num_photon;
+            if (n > 0)
+                CU(cudaMemcpyAsync(sl.input.ptr + sl.h_ev_photon_begin.ptr[k], in.data() + pc.photon_offset,
+                                   (size_t)n * sizeof(gbo_sphoton), cudaMemcpyHostToDevice, s));
+        }
+    }
     int rc2 = GBO_OK;
     if (!sv->cfg.use_graph) {
-        rc2 = enqueue_batch(e, sl, n_ev, n_gs, n_input, N, words, nblk);
+        rc2 = enqueue_batch(e, sl, n_ev, n_gs, has_input, N, words, nblk);
     } else {
         // capture the batch into a graph, then update the slot's executable graph in place (kernel arguments,
         // grid sizes and copy sizes change from batch to batch; the topology changes only with input photons or
         // an empty batch, and then the graph is instantiated afresh)
         CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        rc2 = enqueue_batch(e, sl, n_ev, n_gs, n_input, N, words, nblk);
+        rc2 = enqueue_batch(e, sl, n_ev, n_gs, has_input, N, words, nblk);
         cudaGraph_t graph = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(s, &graph);
         if (!rc2 && ce != cudaSuccess) rc2 = fail(GBO_ERR_CUDA, "batch capture failed: %s", cudaGetErrorString(ce));
@@ -244,22 +285,41 @@ void finish_slot(gbo_server* sv, Slot& sl, int rc)
 {
     std::lock_guard<std::mutex> lock(sv->mu);
     const Clock::time_point now = Clock::now();
-    for (size_t k = 0; k < sl.events.size(); k++) {
-        ServerEvent& ev = *sl.events[k];
-        if (rc == GBO_OK) {
-            const unsigned long long a = sl.h_ev_hit.ptr[k], b = sl.h_ev_hit.ptr[k + 1];
-            ev.hits.assign(sl.h_hits.ptr + a, sl.h_hits.ptr + b);
-            ev.status = 2;
-        } else {
+    for (size_t k = 0; k < sl.pieces.size(); k++) {
+        const Piece& pc = sl.pieces[k];
+        ServerEvent& ev = *pc.ev;
+        ev.pieces_done++;
+        if (ev.status == 3) continue;                   // an earlier piece failed
+        if (rc != GBO_OK) {
             ev.status = 3;
             ev.error = g_last_error;
+            ev.t_done = now;
+            sv->stats.events_done++;
+            continue;
         }
-        ev.t_done = now;
-        sv->stats.events_done++;
+        const unsigned long long a = sl.h_ev_hit.ptr[k], b = sl.h_ev_hit.ptr[k + 1];
+        if ((int)ev.piece_hits.size() <= pc.index) ev.piece_hits.resize((size_t)pc.index + 1);
+        ev.piece_hits[(size_t)pc.index].assign(sl.h_hits.ptr + a, sl.h_hits.ptr + b);
+        if (ev.all_launched && ev.pieces_done == ev.pieces_launched) {
+            if (ev.piece_hits.size() == 1) {
+                ev.hits.swap(ev.piece_hits[0]);
+            } else {
+                size_t n = 0;
+                for (auto& h : ev.piece_hits) n += h.size();
+                ev.hits.reserve(n);
+                for (auto& h : ev.piece_hits) ev.hits.insert(ev.hits.end(), h.begin(), h.end());
+            }
+            ev.piece_hits.clear();
+            ev.status = 2;
+            ev.t_done = now;
+            sv->stats.events_done++;
+        }
     }
     sv->stats.batches++;
     sv->stats.photons += sl.num_photon;
-    sl.events.clear();
+    if (sl.big) big_counter(sv->e->device)--;
+    sl.big = false;
+    sl.pieces.clear();
     sl.phase = 0;
     sv->cv_done.notify_all();
 }
@@ -292,31 +352,67 @@ void serve_loop(gbo_server* sv)
             }
         }
         // admit waiting events into idle slots: at once when the GPU has nothing in flight, otherwise only once
-        // enough photons wait to fill the GPU (min_batch_photon), so that batches do not degenerate to single events
+        // enough photons wait to fill the GPU (min_batch_photon), so that batches do not degenerate to single events.
+        // A big event (at least target_batch_photon photons, enough to fill the GPU alone) never starts beside
+        // another big one, where the two would share the SMs and each take twice as long; small events may pass a
+        // waiting big one into the free slot.
         for (Slot& sl : sv->slots) {
             if (sl.phase != 0) continue;
             int in_flight = 0;
+            bool big_in_flight = false;
             for (Slot& x : sv->slots) in_flight += x.phase != 0;
+            big_in_flight = big_counter(sv->e->device).load() > 0;
             {
                 std::lock_guard<std::mutex> lock(sv->mu);
+                auto admissible = [&](const ServerEvent& ev) {
+                    return !big_in_flight || ev.num_photon - ev.next_photon < sv->cfg.target_batch_photon;
+                };
                 if (in_flight > 0) {
                     long long waiting = 0;
-                    for (auto& ev : sv->pending) { waiting += ev->num_photon; if (waiting >= sv->cfg.min_batch_photon) break; }
+                    for (auto& ev : sv->pending) {
+                        if (!admissible(*ev)) continue;
+                        waiting += ev->num_photon - ev->next_photon;
+                        if (waiting >= sv->cfg.min_batch_photon) break;
+                    }
                     if (waiting < sv->cfg.min_batch_photon) continue;
                 }
                 long long photons = 0;
-                while (!sv->pending.empty()) {
-                    auto& ev = sv->pending.front();
-                    if (!sl.events.empty() && (photons + ev->num_photon > sv->max_batch_photon ||
-                                               (int)sl.events.size() >= sv->cfg.max_batch_events))
+                sl.big = false;
+                for (auto it = sv->pending.begin(); it != sv->pending.end();) {
+                    std::shared_ptr<ServerEvent> ev = *it;
+                    const long long rest = ev->num_photon - ev->next_photon;
+                    if (!admissible(*ev)) { ++it; continue; }
+                    if (!sl.pieces.empty() && (photons + rest > sv->max_batch_photon ||
+                                               photons >= sv->cfg.target_batch_photon ||
+                                               (int)sl.pieces.size() >= sv->cfg.max_batch_events))
                         break;
-                    photons += ev->num_photon;
+                    // the rest of the event, or, when it does not fit an empty batch, its next genstep-aligned piece
+                    // of at most max_batch_photon photons (a single larger genstep goes alone)
+                    Piece pc;
+                    pc.ev = ev;
+                    pc.g0 = ev->next_gs;
+                    pc.photon_offset = ev->next_photon;
+                    int64_t g1 = pc.g0;
+                    long long n = 0;
+                    const int64_t ng = (int64_t)ev->gs.size();
+                    while (g1 < ng && (g1 == pc.g0 || n + (long long)ev->gs[(size_t)g1].q[0].u[3] <= sv->max_batch_photon - photons))
+                        n += ev->gs[(size_t)g1++].q[0].u[3];
+                    pc.g1 = g1;
+                    pc.num_photon = n;
+                    pc.index = ev->pieces_launched++;
+                    ev->next_gs = g1;
+                    ev->next_photon += n;
                     ev->status = 1;
-                    sl.events.push_back(ev);
-                    sv->pending.pop_front();
+                    photons += n;
+                    sl.big |= n >= sv->cfg.target_batch_photon;
+                    sl.pieces.push_back(pc);
+                    if (g1 < ng) break;                 // the event goes on in a later batch
+                    ev->all_launched = true;
+                    it = sv->pending.erase(it);
                 }
             }
-            if (sl.events.empty()) continue;
+            if (sl.pieces.empty()) continue;
+            if (sl.big) big_counter(sv->e->device)++;
             busy = true;
             int rc = launch_batch(sv, sl);
             if (rc) finish_slot(sv, sl, rc);
@@ -350,6 +446,7 @@ int gbo_server_config_default(gbo_server_config* c)
     c->max_batch_events = 4096;
     c->min_batch_photon = 2ll << 20;
     c->use_graph = 1;
+    c->target_batch_photon = 4ll << 20;
     return GBO_OK;
 }
 
@@ -361,6 +458,7 @@ int gbo_server_create(gbo_engine* e, const gbo_server_config* cfg, gbo_server** 
     if (cfg) c = *cfg; else gbo_server_config_default(&c);
     if (c.slots < 1 || c.slots > 8) return fail(GBO_ERR_ARG, "gbo_server_create: slots %d not in 1..8", c.slots);
     if (c.max_batch_events < 1) return fail(GBO_ERR_ARG, "gbo_server_create: max_batch_events must be positive");
+    if (c.target_batch_photon <= 0) c.target_batch_photon = INT64_MAX;     // no target: max_batch_photon alone
     CU(cudaSetDevice(e->device));
     auto* sv = new gbo_server();
     sv->e = e;
@@ -398,8 +496,6 @@ int gbo_server_submit(gbo_server* sv, int32_t event_id, const gbo_quad6* gs, int
     for (const gbo_quad6& q : ev->gs) { n += q.q[0].u[3]; has_input_gs |= q.q[0].i[0] == GBO_GS_INPUT_PHOTON; }
     if (has_input_gs && num_input_photon < n)
         return fail(GBO_ERR_ARG, "gbo_server_submit: INPUT_PHOTON gensteps need %lld photons, %lld given", n, (long long)num_input_photon);
-    if (n > sv->max_batch_photon)
-        return fail(GBO_ERR_CAPACITY, "gbo_server_submit: event of %lld photons above the batch limit %lld", n, sv->max_batch_photon);
     ev->num_photon = n;
     ev->t_submit = Clock::now();
     {

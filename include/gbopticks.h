@@ -155,18 +155,21 @@ int         gbo_trace_rays(gbo_engine* e, const float* pos, const float* dir, in
  * multi-threaded producers: gbo_server_submit copies an event's gensteps (and input photons) and returns a ticket
  * at once (thread-safe); a worker thread packs waiting events into one simulate launch, runs up to `slots` launches
  * at once on separate streams, admits events while the launches' device buffers fit hbm_budget_bytes, and keeps
- * each finished event's hits on the host until gbo_server_release.  Results equal those of gbo_simulate for the
- * same event id. */
+ * each finished event's hits on the host until gbo_server_release.  An event above max_batch_photon runs as
+ * genstep-aligned pieces over several launches (as OPTICKS_MAX_SLOT slices an event in the reference,
+ * qudarap/QSim.cc:481-529).  Results equal those of gbo_simulate for the same event id. */
 typedef struct gbo_server gbo_server;
 typedef struct gbo_server_config {
     int32_t slots;                  /* launches in flight at once (1..8, 2) */
     int32_t max_batch_events;       /* events per launch (4096) */
-    int64_t max_batch_photon;       /* photons per launch (16M); also bounded by the budget */
+    int64_t max_batch_photon;       /* photons per launch (16M); also bounded by the budget; larger events are sliced */
     int64_t hbm_budget_bytes;       /* device memory the server's launches may hold (120 GB) */
     int64_t min_batch_photon;       /* while a launch is in flight, start another only once this many photons wait (2M) */
     int32_t use_graph;              /* 1: each batch's copies and kernels go out as one CUDA graph, captured from the
                                        stream and applied to the slot's executable graph by update (1) */
     int32_t reserved;
+    int64_t target_batch_photon;    /* a batch stops taking events once it holds this many photons (4M): enough to
+                                       fill the GPU, small enough that small events do not wait on a long launch */
 } gbo_server_config;
 typedef struct gbo_server_stats {
     int64_t events_submitted, events_done, batches, photons, max_batch_photon;

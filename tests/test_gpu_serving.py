@@ -78,11 +78,56 @@ def test_served_events_equal_alone(E, kind, use_graph):
     eng.close()
 
 
-def test_server_rejects_oversized_event(E):
+@pytest.mark.parametrize("max_batch_photon", [1200, 400])
+def test_server_slices_events_larger_than_a_batch(E, max_batch_photon):
+    """Events above max_batch_photon run as genstep-aligned pieces (several batches, both slots); each event's hits
+    equal those it gets alone.  At 400 every 500-photon genstep is a piece of its own."""
     from eic_opticks_gb300 import geometry as G, gensteps as GS
-    eng = E.Engine(G.crystal_array().arrays())
-    srv = E.Server(eng, max_batch_photon=1000)
-    with pytest.raises(E.GBOError):
-        srv.submit(0, GS.crystal_scint_gensteps(4, 500, seed=1, poisson=False))
+    arrays = G.crystal_array().arrays()
+    events = [(300 + k, GS.crystal_scint_gensteps(10, 500, seed=70 + k, poisson=False)) for k in range(6)]
+    eng = E.Engine(arrays)
+    alone = {}
+    for eid, gs in events:
+        eng.simulate(eid, gs)
+        alone[eid] = eng.hits()
+    srv = E.Server(eng, slots=2, max_batch_photon=max_batch_photon)
+    tickets = {eid: srv.submit(eid, gs) for eid, gs in events}
+    for eid, t in tickets.items():
+        assert srv.wait(t, timeout_us=60_000_000)
+        got = srv.hits(t)
+        assert np.array_equal(got.view(np.uint32), alone[eid].view(np.uint32)), eid
+        assert srv.info(t)["num_photon"] == 5000
+        srv.release(t)
+    st = srv.stats()
+    assert st["events_done"] == len(events) and st["photons"] == 5000 * len(events)
+    assert st["batches"] >= len(events) * 5000 // 1200
+    srv.close()
+    eng.close()
+
+
+@pytest.mark.parametrize("max_batch_photon", [16 << 20, 3000])
+def test_server_input_photons(E, max_batch_photon):
+    """INPUT_PHOTON events (nested boxes with the sensor surface): batched, and sliced into pieces, each event's
+    hits equal those it gets alone."""
+    from eic_opticks_gb300 import geometry as G, gensteps as GS
+    arrays = G.nested_boxes(sensor=True).arrays()
+    events = []
+    for k in range(8):
+        inp = GS.isotropic_photons(2000 + 500 * k, seed=40 + k)
+        q = len(inp) // 4                       # four INPUT_PHOTON gensteps, so that slicing can cut the event
+        gs = np.concatenate([GS.input_photon_genstep(q)] * 3 + [GS.input_photon_genstep(len(inp) - 3 * q)])
+        events.append((400 + k, gs, inp))
+    eng = E.Engine(arrays)
+    alone = {}
+    for eid, gs, inp in events:
+        eng.simulate(eid, gs, inp)
+        alone[eid] = eng.hits()
+    assert sum(len(h) for h in alone.values()) > 0
+    srv = E.Server(eng, slots=2, max_batch_photon=max_batch_photon)
+    tickets = {eid: srv.submit(eid, gs, inp) for eid, gs, inp in events}
+    for eid, t in tickets.items():
+        assert srv.wait(t, timeout_us=60_000_000)
+        assert np.array_equal(srv.hits(t).view(np.uint32), alone[eid].view(np.uint32)), eid
+        srv.release(t)
     srv.close()
     eng.close()
