@@ -39,8 +39,8 @@ def build(verbose=False, force=False, ptxas_verbose=False):
         o = os.path.join(BUILD, f + ".o")
         cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", inc, "-c",
                os.path.join(CSRC, f), "-o", o]
-        extra = os.environ.get("GBO_NVCC_DEFINES", "").split()      # e.g. -DGBO_SIM_MINB=5 for tuning builds
-        cmd[1:1] = [x for x in extra if x.startswith("-D")]
+        extra = os.environ.get("GBO_NVCC_DEFINES", "").split()      # tuning builds: -DGBO_SIM_MINB=5, --fmad=false
+        cmd[1:1] = [x for x in extra if x.startswith("-D") or x.startswith("--fmad=")]
         if ptxas_verbose:
             cmd[1:1] = ["-Xptxas", "-v"]
         procs.append(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT))

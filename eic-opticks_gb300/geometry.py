@@ -37,6 +37,8 @@ def _on_domain(v):
     arr = np.asarray(v, dtype=np.float64)
     if arr.ndim == 0:
         return np.full(DOMAIN.shape, float(arr))
+    if arr.ndim == 1 and arr.shape == DOMAIN.shape:      # already sampled on the domain
+        return arr
     if arr.ndim == 2:                      # (n, 2) table of (wavelength_nm, value): clamp outside its range
         order = np.argsort(arr[:, 0])
         return np.interp(DOMAIN, arr[order, 0], arr[order, 1])
@@ -171,6 +173,14 @@ def cone(r1, z1, r2, z2):
     return _node(L.CSG_CONE, (r1, z1, r2, z2), bbox=(-rm, -rm, z1, rm, rm, z2))
 
 
+def convexpolyhedron(planes, bbox):
+    """Convex polyhedron leaf: planes (n, 4) as (outward normal, distance from the origin); the planes go into the
+    geometry's plan array when the solid is added (CSG/csg_intersect_leaf_convexpolyhedron.h:40-106)."""
+    nd = _node(L.CSG_CONVEXPOLYHEDRON, bbox=tuple(float(v) for v in bbox))
+    nd["planes"] = np.asarray(planes, dtype=np.float64).reshape(-1, 4)
+    return nd
+
+
 def with_transform(node, m):
     node = dict(node)
     node["transform"] = np.asarray(m, dtype=np.float64) if node.get("transform") is None else node["transform"] @ m
@@ -267,6 +277,10 @@ class Geometry:
                 else:
                     rec[0, :] = nd["q0"]
                     rec[1, 0:2] = nd["q1xy"]
+                    if nd.get("planes") is not None:             # planeIdx, planeNum (CSGNode::setPlaneIdx/Num)
+                        ints[0, 0] = len(self.plan)
+                        ints[0, 1] = len(nd["planes"])
+                        self.plan = np.concatenate([self.plan, nd["planes"].astype(np.float32)])
                     ints[1, 2] = bnd
                     ints[3, 2] = nd["typecode"]
                     tidx = 0
@@ -372,7 +386,15 @@ def scint_icdf(emission, num_bins=4096, hd_factor=20, num_table=256, lo=200.0, h
     """
     wl = np.linspace(lo, hi, num_table)
     e = HC_EVNM / wl[::-1]                           # increasing energy
-    f = emission(wl[::-1])
+    return scint_icdf_table(e, emission(wl[::-1]), num_bins, hd_factor)
+
+
+def scint_icdf_table(energy_ev, intensity, num_bins=4096, hd_factor=20):
+    """Inverse CDF of an emission spectrum tabulated at increasing photon energies (eV): the trapezoid running
+    integral on the table's own points (u4/U4Scint.h:218-256, Geant4's ScintillationIntegral) inverted by linear
+    interpolation, in the three-row hd_factor layout."""
+    e = np.asarray(energy_ev, dtype=np.float64)
+    f = np.asarray(intensity, dtype=np.float64)
     integ = np.concatenate([[0.0], np.cumsum(0.5 * (f[1:] + f[:-1]) * np.diff(e))])
     mx = integ[-1]
     j = np.arange(num_bins, dtype=np.float64)

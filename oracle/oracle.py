@@ -153,6 +153,23 @@ def simulate(cfg, gs, input_photon=None, event_index=0, photon_offset=0, nthread
     return out, sq
 
 
+def trace(cfg, pos, dirs, tmin=0.05, tmax=1e9):
+    """Closest hit of each ray by the binary32 brute-force oracle (orc_csg.c): (t, boundary), t = -1 on a miss."""
+    pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+    dirs = np.ascontiguousarray(dirs, dtype=np.float32).reshape(-1, 3)
+    t = np.full(len(pos), -1.0, dtype=np.float32)
+    b = np.full(len(pos), 0xffffffff, dtype=np.uint32)
+    prd = np.zeros(8, dtype=np.float32)
+    for i in range(len(pos)):
+        lib().orc_trace_c(C.byref(cfg.sim.geom), _ptr(pos[i]), _ptr(dirs[i]), C.c_float(tmin), C.c_float(tmax),
+                          _ptr(prd))
+        bnd = int(prd.view(np.uint32)[7]) & 0xffff
+        if bnd != 0xffff:
+            t[i] = prd[3]
+            b[i] = bnd
+    return t, b
+
+
 def trace64(cfg, pos, dirs, tmin=0.05, tmax=1e9, nthreads=None):
     """Closest-hit distances in binary64 (orc_csg64.c) for rays given as float32 (n,3) arrays; -1 on a miss."""
     import os as _os
