@@ -554,6 +554,15 @@ def main():
         {"nested_boxes": 64, "water_cube": 16, "crystal_array": 8, "large_sphere": 2}[args.workload])
     if n_batch > 0 and world == 1 and not args.precision:
         line["same_config_batching"] = same_config_batching(geom, args.workload, n_batch, tune)
+    # hit merge (identity, 1 ns bucket) of the last event's hits, as the reference's per-launch merge does
+    import ctypes as C
+    nm = C.c_int64()
+    eng.simulate(3000, gs, inp)
+    E._check(eng.lib.gbo_merge_hits(eng.handle, C.c_float(1.0), C.byref(nm)), "gbo_merge_hits")    # warm-up
+    t0 = time.perf_counter()
+    E._check(eng.lib.gbo_merge_hits(eng.handle, C.c_float(1.0), C.byref(nm)), "gbo_merge_hits")
+    line["hit_merge"] = {"time_window_ns": 1.0, "hits": eng.num_hit(), "merged": nm.value,
+                         "ms": 1e3 * (time.perf_counter() - t0)}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(geom, gs, inp=inp)
     print(json.dumps(line))

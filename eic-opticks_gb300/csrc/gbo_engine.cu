@@ -534,6 +534,8 @@ struct gbo_engine {
     DBuf<gbo_seq> seq;
     DBuf<gbo_sphoton> hits_unordered;
     DBuf<gbo_sphoton> hits;
+    DBuf<gbo_sphoton> merged;               // hits merged by (identity, time bucket), gbo_merge_hits
+    long long num_merged = -1;
     DBuf<uint32_t> bitmap, word_prefix, block_sum;
     DBuf<unsigned long long> block_offset;
     DBuf<unsigned long long> counters;      // [0] unordered hit count, [1] total hits, [2] photons
@@ -649,7 +651,7 @@ void gbo_engine_destroy(gbo_engine* e)
     e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->prim.release(); e->solid.release();
     e->node.release(); e->plan.release(); e->itra.release(); e->optical.release();
     e->gs.release(); e->gs_end.release(); e->input.release(); e->photon.release(); e->seq.release();
-    e->hits_unordered.release(); e->hits.release(); e->bitmap.release(); e->word_prefix.release();
+    e->hits_unordered.release(); e->hits.release(); e->merged.release(); e->bitmap.release(); e->word_prefix.release();
     e->block_sum.release(); e->block_offset.release(); e->counters.release();
     if (e->host_counters) cudaFreeHost(e->host_counters);
     for (auto& v : e->ev) if (v) cudaEventDestroy(v);
@@ -866,6 +868,7 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     CU(cudaStreamSynchronize(s));
     e->num_photon = at.photon_base + num_photon;
     e->num_hit = at.hit_base + (long long)e->host_counters[1];
+    e->num_merged = -1;
     e->event_id = event_id;
     e->stats.num_photon = e->num_photon;
     e->stats.num_hit = e->num_hit;
@@ -1010,6 +1013,35 @@ int gbo_copy_hits(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64_t count
     return GBO_OK;
 }
 
+int gbo_merge_hits(gbo_engine* e, float time_window, int64_t* num_merged)
+{
+    if (!e || !num_merged) return fail(GBO_ERR_ARG, "gbo_merge_hits: null argument");
+    if (e->num_photon < 0) return fail(GBO_ERR_STATE, "gbo_merge_hits: no event simulated");
+    if (!(time_window >= 0.f)) return fail(GBO_ERR_ARG, "gbo_merge_hits: time window %g", (double)time_window);
+    CU(cudaSetDevice(e->device));
+    int rc;
+    if ((rc = e->merged.ensure(e->num_hit > 0 ? e->num_hit : 1))) return rc;
+    int64_t n = 0;
+    rc = gbo_merge_hits_device(e->hits.ptr, e->num_hit, time_window, e->merged.ptr, &n, e->stream);
+    if (rc) return fail(rc, "gbo_merge_hits: merge of %lld hits failed", e->num_hit);
+    e->num_merged = n;
+    *num_merged = n;
+    return GBO_OK;
+}
+
+int gbo_copy_merged_hits(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64_t count)
+{
+    if (!e || (!dst && count > 0)) return fail(GBO_ERR_ARG, "gbo_copy_merged_hits: null argument");
+    if (e->num_merged < 0) return fail(GBO_ERR_STATE, "gbo_copy_merged_hits: gbo_merge_hits not called");
+    if (offset < 0 || count < 0 || offset + count > e->num_merged)
+        return fail(GBO_ERR_ARG, "gbo_copy_merged_hits: range outside %lld merged hits", e->num_merged);
+    if (count == 0) return GBO_OK;
+    CU(cudaSetDevice(e->device));
+    CU(cudaMemcpyAsync(dst, e->merged.ptr + offset, (size_t)count * sizeof(gbo_sphoton), cudaMemcpyDeviceToHost, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+    return GBO_OK;
+}
+
 int gbo_copy_photons(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64_t count)
 {
     if (!e || (!dst && count > 0)) return fail(GBO_ERR_ARG, "gbo_copy_photons: null argument");
@@ -1042,6 +1074,7 @@ int gbo_reset(gbo_engine* e, int32_t event_id)
     (void)event_id;
     e->num_photon = -1;
     e->num_hit = 0;
+    e->num_merged = -1;
     e->event_id = -1;
     return GBO_OK;
 }

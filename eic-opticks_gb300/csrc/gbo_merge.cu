@@ -1,0 +1,253 @@
+// gbo_merge.cu : hit merging by (sensor identity, time bucket), the reference's SPM::merge_partial_select
+// (sysrap/SPM.cu) with sphoton::key_functor / reduce_op (sysrap/sphoton.h:277-304).
+//
+// key = identity << 48 | (unsigned)(time / tw); hits are stably sorted by key and each run of equal keys becomes one
+// hit: the earliest-time member (the earlier in input order on a tie) with the run's flagmasks ORed and hitcounts
+// (16 bits) summed.  The reference sorts with thrust and reduces with reduce_by_key; here:
+//
+//   k_merge_keys      key and input index per hit, OR of all keys (to skip radix passes over all-zero bytes)
+//   k_radix_hist      per-tile histogram of one key byte (256 bins in shared memory), digit-major layout
+//   k_scan_exclusive  one-block exclusive scan of the digit x tile counts (or of the run-head flags)
+//   k_radix_scatter   stable scatter: each warp owns a contiguous sub-tile, ranks equal digits with
+//                     __match_any_sync and a per-warp running offset, so input order survives every pass
+//   k_run_heads       1 where a key differs from its predecessor
+//   k_run_reduce      one thread per run folds its members in sorted (= input) order
+//
+// Memory is stream-ordered (cudaMallocAsync / cudaFreeAsync) on the caller's stream.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbopticks.h"
+
+namespace {
+
+constexpr int MB_THREADS = 256;                 // threads per block of the sort kernels
+constexpr int MB_WARPS = MB_THREADS / 32;
+constexpr int MB_TILE = 4096;                   // keys per block tile
+constexpr int MB_WARP_TILE = MB_TILE / MB_WARPS;
+constexpr int SCAN_THREADS = 1024;
+
+__device__ __forceinline__ uint64_t merge_key(const gbo_sphoton& p, float tw)
+{
+    const unsigned id = p.identity & 0x00ffffffu;
+    const unsigned bucket = (unsigned)(p.time / tw);
+    return ((uint64_t)id << 48) | (uint64_t)bucket;
+}
+
+__global__ void k_merge_keys(const gbo_sphoton* in, long long n, float tw, uint64_t* keys, uint32_t* idx,
+                             unsigned long long* key_or)
+{
+    __shared__ unsigned long long s_or;
+    if (threadIdx.x == 0) s_or = 0ull;
+    __syncthreads();
+    unsigned long long acc = 0ull;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const uint64_t k = merge_key(in[i], tw);
+        keys[i] = k;
+        idx[i] = (uint32_t)i;
+        acc |= k;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc |= __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicOr(&s_or, acc);
+    __syncthreads();
+    if (threadIdx.x == 0) atomicOr(key_or, s_or);
+}
+
+__global__ void k_radix_hist(const uint64_t* keys, long long n, int shift, int ntiles, uint32_t* hist)
+{
+    __shared__ uint32_t h[256];
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) h[d] = 0u;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * MB_TILE;
+    for (int j = threadIdx.x; j < MB_TILE; j += blockDim.x) {
+        const long long i = base + j;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xffu], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(size_t)d * ntiles + blockIdx.x] = h[d];
+}
+
+// exclusive scan of n uint32 in place by one block: each thread scans a contiguous chunk; total in *total
+__global__ void k_scan_exclusive(uint32_t* v, long long n, unsigned long long* total)
+{
+    __shared__ unsigned long long part[SCAN_THREADS];
+    const long long per = (n + SCAN_THREADS - 1) / SCAN_THREADS;
+    const long long lo = (long long)threadIdx.x * per;
+    const long long hi = lo + per < n ? lo + per : n;
+    unsigned long long s = 0ull;
+    for (long long i = lo; i < hi; i++) s += v[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < SCAN_THREADS; off <<= 1) {          // Hillis-Steele over the chunk sums
+        const unsigned long long x = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0ull;
+        __syncthreads();
+        part[threadIdx.x] += x;
+        __syncthreads();
+    }
+    unsigned long long run = threadIdx.x ? part[threadIdx.x - 1] : 0ull;
+    for (long long i = lo; i < hi; i++) {
+        const uint32_t x = v[i];
+        v[i] = (uint32_t)run;
+        run += x;
+    }
+    if (threadIdx.x == SCAN_THREADS - 1 && total) *total = part[SCAN_THREADS - 1];
+}
+
+__global__ void __launch_bounds__(MB_THREADS) k_radix_scatter(const uint64_t* keys, const uint32_t* idx, long long n,
+                                                              int shift, int ntiles, const uint32_t* offsets,
+                                                              uint64_t* keys_out, uint32_t* idx_out)
+{
+    __shared__ uint32_t cnt[MB_WARPS][256];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int d = threadIdx.x; d < MB_WARPS * 256; d += blockDim.x) (&cnt[0][0])[d] = 0u;
+    __syncthreads();
+    const long long wbase = (long long)blockIdx.x * MB_TILE + (long long)warp * MB_WARP_TILE;
+    // 1. digit counts of each warp's sub-tile
+    for (int c = 0; c < MB_WARP_TILE; c += 32) {
+        const long long i = wbase + c + lane;
+        const bool ok = i < n;
+        const unsigned d = ok ? (unsigned)((keys[i] >> shift) & 0xffu) : 0u;
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const unsigned peers = __match_any_sync(act, d);
+            if ((peers & lt) == 0u) cnt[warp][d] += __popc(peers);
+        }
+        __syncwarp();                                   // the next chunk's leader may be another lane
+    }
+    __syncthreads();
+    // 2. running bases: the block's offset for the digit, then the earlier warps' counts
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+        uint32_t run = offsets[(size_t)d * ntiles + blockIdx.x];
+        for (int w = 0; w < MB_WARPS; w++) {
+            const uint32_t c = cnt[w][d];
+            cnt[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    // 3. stable scatter in sub-tile order
+    for (int c = 0; c < MB_WARP_TILE; c += 32) {
+        const long long i = wbase + c + lane;
+        const bool ok = i < n;
+        const uint64_t k = ok ? keys[i] : 0ull;
+        const unsigned d = (unsigned)((k >> shift) & 0xffu);
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        unsigned peers = 0u, pos = 0u;
+        if (ok) {
+            peers = __match_any_sync(act, d);
+            pos = cnt[warp][d] + __popc(peers & lt);
+        }
+        __syncwarp();
+        if (ok) {
+            keys_out[pos] = k;
+            idx_out[pos] = idx[i];
+            if ((peers & lt) == 0u) cnt[warp][d] += __popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void k_run_heads(const uint64_t* keys, long long n, uint32_t* head)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        head[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+__global__ void k_run_starts(const uint64_t* keys, long long n, const uint32_t* run_index, uint32_t* start)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        if (i == 0 || keys[i] != keys[i - 1]) start[run_index[i]] = (uint32_t)i;
+}
+
+__global__ void k_run_reduce(const gbo_sphoton* in, const uint32_t* order, const uint32_t* start, long long runs,
+                             long long n, gbo_sphoton* out)
+{
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < runs; r += (long long)gridDim.x * blockDim.x) {
+        const long long b = start[r];
+        const long long e = r + 1 < runs ? (long long)start[r + 1] : n;
+        gbo_sphoton acc = in[order[b]];
+        for (long long j = b + 1; j < e; j++) {
+            const gbo_sphoton x = in[order[j]];
+            const bool a_first = fminf(acc.time, x.time) == acc.time;
+            const unsigned fm = acc.flagmask | x.flagmask;
+            const unsigned hc = ((acc.hitcount_iindex >> 16) + (x.hitcount_iindex >> 16)) & 0xffffu;
+            if (!a_first) acc = x;
+            acc.flagmask = fm;
+            acc.hitcount_iindex = (acc.hitcount_iindex & 0x0000ffffu) | (hc << 16);
+        }
+        out[r] = acc;
+    }
+}
+
+#define MCU(x) do { cudaError_t err_ = (x); if (err_ != cudaSuccess) { rc = GBO_ERR_CUDA; goto done; } } while (0)
+
+}  // namespace
+
+// Merge n device hits into d_out (room for n); *num_out receives the merged count.  Synchronous on `stream`.
+extern "C" int gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float time_window, gbo_sphoton* d_out,
+                                     int64_t* num_out, void* stream_)
+{
+    if (!num_out || n < 0 || (n > 0 && (!d_in || !d_out))) return GBO_ERR_ARG;
+    if (n > 0xffffffffll) return GBO_ERR_CAPACITY;
+    cudaStream_t s = (cudaStream_t)stream_;
+    *num_out = 0;
+    if (n == 0) return GBO_OK;
+    if (time_window == 0.f) {                                   // NOMERGE_TIME_WINDOW: the hits as they are
+        if (cudaMemcpyAsync(d_out, d_in, (size_t)n * sizeof(gbo_sphoton), cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return GBO_ERR_CUDA;
+        *num_out = n;
+        return GBO_OK;
+    }
+    int rc = GBO_OK;
+    const int ntiles = (int)((n + MB_TILE - 1) / MB_TILE);
+    uint64_t *k0 = nullptr, *k1 = nullptr;
+    uint32_t *i0 = nullptr, *i1 = nullptr, *hist = nullptr;
+    unsigned long long* scal = nullptr;                         // [0] key OR, [1] scan total
+    unsigned long long h_scal[2] = {0ull, 0ull};
+    const int grid = (int)((n + MB_THREADS - 1) / MB_THREADS < 4096 ? (n + MB_THREADS - 1) / MB_THREADS : 4096);
+    MCU(cudaMallocAsync((void**)&k0, (size_t)n * 8, s));
+    MCU(cudaMallocAsync((void**)&k1, (size_t)n * 8, s));
+    MCU(cudaMallocAsync((void**)&i0, (size_t)n * 4, s));
+    MCU(cudaMallocAsync((void**)&i1, (size_t)n * 4, s));
+    MCU(cudaMallocAsync((void**)&hist, (size_t)256 * ntiles * 4 > (size_t)n * 4 ? (size_t)256 * ntiles * 4 : (size_t)n * 4, s));
+    MCU(cudaMallocAsync((void**)&scal, 2 * sizeof(unsigned long long), s));
+    MCU(cudaMemsetAsync(scal, 0, 2 * sizeof(unsigned long long), s));
+    k_merge_keys<<<grid, MB_THREADS, 0, s>>>(d_in, n, time_window, k0, i0, scal);
+    MCU(cudaGetLastError());
+    MCU(cudaMemcpyAsync(h_scal, scal, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    MCU(cudaStreamSynchronize(s));
+    for (int byte = 0; byte < 8; byte++) {
+        if (((h_scal[0] >> (8 * byte)) & 0xffull) == 0ull) continue;       // every key has a zero byte here
+        k_radix_hist<<<ntiles, MB_THREADS, 0, s>>>(k0, n, 8 * byte, ntiles, hist);
+        k_scan_exclusive<<<1, SCAN_THREADS, 0, s>>>(hist, (long long)256 * ntiles, nullptr);
+        k_radix_scatter<<<ntiles, MB_THREADS, 0, s>>>(k0, i0, n, 8 * byte, ntiles, hist, k1, i1);
+        MCU(cudaGetLastError());
+        uint64_t* tk = k0; k0 = k1; k1 = tk;
+        uint32_t* ti = i0; i0 = i1; i1 = ti;
+    }
+    {
+        // runs of equal keys: heads -> exclusive scan (run index of each head) -> run starts -> fold
+        uint32_t* head = hist;                                  // n words (hist was sized for max(n, 256 ntiles))
+        k_run_heads<<<grid, MB_THREADS, 0, s>>>(k0, n, head);
+        k_scan_exclusive<<<1, SCAN_THREADS, 0, s>>>(head, n, scal + 1);
+        MCU(cudaGetLastError());
+        MCU(cudaMemcpyAsync(h_scal + 1, scal + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        MCU(cudaStreamSynchronize(s));
+        const long long runs = (long long)h_scal[1];
+        uint32_t* start = i1;                                   // free after the last pass
+        k_run_starts<<<grid, MB_THREADS, 0, s>>>(k0, n, head, start);
+        const int rgrid = (int)((runs + MB_THREADS - 1) / MB_THREADS < 4096 ? (runs + MB_THREADS - 1) / MB_THREADS : 4096);
+        k_run_reduce<<<rgrid > 0 ? rgrid : 1, MB_THREADS, 0, s>>>(d_in, i0, start, runs, n, d_out);
+        MCU(cudaGetLastError());
+        MCU(cudaStreamSynchronize(s));
+        *num_out = runs;
+    }
+done:
+    void* bufs[6] = {k0, k1, i0, i1, hist, scal};
+    for (void* b : bufs)
+        if (b) cudaFreeAsync(b, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess && rc == GBO_OK) rc = GBO_ERR_CUDA;
+    return rc;
+}

@@ -85,8 +85,11 @@ def load(path=LIB):
     lib.gbo_num_hit.argtypes = [C.c_void_p]
     lib.gbo_num_photon.argtypes = [C.c_void_p]
     lib.gbo_device_hits.argtypes = [C.c_void_p]
-    for f in ("gbo_copy_hits", "gbo_copy_photons", "gbo_copy_seq"):
+    for f in ("gbo_copy_hits", "gbo_copy_photons", "gbo_copy_seq", "gbo_copy_merged_hits"):
         getattr(lib, f).argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64]
+    lib.gbo_merge_hits.argtypes = [C.c_void_p, C.c_float, C.POINTER(C.c_int64)]
+    lib.gbo_merge_hits_device.argtypes = [C.c_void_p, C.c_int64, C.c_float, C.c_void_p, C.POINTER(C.c_int64),
+                                          C.c_void_p]
     lib.gbo_reset.argtypes = [C.c_void_p, C.c_int32]
     lib.gbo_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     lib.gbo_rng_sequence.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_void_p]
@@ -196,6 +199,15 @@ class Engine:
             _check(self.lib.gbo_copy_hits(self.handle, None, 0, 0), "gbo_copy_hits")
         out = np.zeros(n, dtype=L.PHOTON) if out is None else out
         _check(self.lib.gbo_copy_hits(self.handle, out.ctypes.data_as(C.c_void_p), 0, n), "gbo_copy_hits")
+        return out
+
+    def merge_hits(self, time_window=1.0):
+        """The current event's hits merged by (sensor identity, time bucket of time_window ns): gbo_merge_hits."""
+        n = C.c_int64()
+        _check(self.lib.gbo_merge_hits(self.handle, C.c_float(time_window), C.byref(n)), "gbo_merge_hits")
+        out = np.zeros(n.value, dtype=L.PHOTON)
+        _check(self.lib.gbo_copy_merged_hits(self.handle, out.ctypes.data_as(C.c_void_p), 0, n.value),
+               "gbo_copy_merged_hits")
         return out
 
     def photons(self):

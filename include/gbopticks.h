@@ -122,6 +122,16 @@ int         gbo_copy_hits(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64
 int         gbo_copy_photons(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64_t count);
 int         gbo_copy_seq(gbo_engine* e, gbo_seq* dst, int64_t offset, int64_t count);
 const void* gbo_device_hits(const gbo_engine* e);
+/* Hit merging, the reference's per-launch SPM::merge_partial_select (sysrap/SPM.cu, called from QEvt::PerLaunchMerge
+ * qudarap/QEvt.cc:1170-1210) with sphoton::key_functor / reduce_op (sysrap/sphoton.h:277-304): the current event's
+ * hits grouped by (sensor identity, floor(time / time_window)), each group becoming its earliest hit with the
+ * group's flagmasks ORed and hitcounts summed, in ascending key order.  time_window 0 keeps the hits unmerged
+ * (NOMERGE_TIME_WINDOW); the reference's OPTICKS_MERGE_WINDOW is typically 1 ns.
+ * gbo_merge_hits_device does the same for any device array of n hits into d_out (room for n), on `stream`. */
+int         gbo_merge_hits(gbo_engine* e, float time_window, int64_t* num_merged);
+int         gbo_copy_merged_hits(gbo_engine* e, gbo_sphoton* dst, int64_t offset, int64_t count);
+int         gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float time_window, gbo_sphoton* d_out,
+                                  int64_t* num_out, void* stream);
 int         gbo_reset(gbo_engine* e, int32_t event_id);
 int         gbo_get_stats(const gbo_engine* e, gbo_stats* out);
 const char* gbo_last_error(void);

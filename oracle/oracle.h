@@ -64,6 +64,7 @@ int64_t orc_fill_seed(const gbo_quad6* gs, int num_gs, int32_t* seed, int64_t ma
 
 /* hit selection : (flagmask & hitmask) == hitmask (sysrap/sphoton.h:1219-1225), order preserved */
 int64_t orc_select_hits(const gbo_sphoton* p, int64_t n, uint32_t hitmask, gbo_sphoton* hits);
+int64_t orc_merge_hits(const gbo_sphoton* in, int64_t n, float tw, gbo_sphoton* out);
 
 /* unit pieces exposed for known-answer tests */
 void  orc_philox_uniforms(uint64_t seed, uint64_t subsequence, uint64_t offset, uint64_t skip, int n, float* out);

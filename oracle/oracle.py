@@ -116,6 +116,7 @@ def lib():
         _oracle.orc_fill_seed.restype = C.c_int64
         _oracle.orc_select_hits.restype = C.c_int64
         _oracle.orc_intersect_prim_c.restype = C.c_int
+        _oracle.orc_merge_hits.restype = C.c_int64
     return _oracle
 
 
@@ -181,6 +182,14 @@ def trace64(cfg, pos, dirs, tmin=0.05, tmax=1e9, nthreads=None):
     lib().orc_trace64_batch(C.byref(cfg.sim.geom), _ptr(pos), _ptr(dirs), C.c_int64(n), C.c_double(tmin),
                             C.c_double(tmax), _ptr(t), _ptr(b), C.c_int(nthreads or _os.cpu_count() or 1))
     return t, b
+
+
+def merge_hits(hits, time_window):
+    """Hits merged by (identity, time bucket) as the reference's SPM::merge_partial_select does (orc_qsim.c)."""
+    hits = np.ascontiguousarray(hits)
+    out = np.zeros_like(hits)
+    m = lib().orc_merge_hits(_ptr(hits), C.c_int64(len(hits)), C.c_float(time_window), _ptr(out))
+    return out[:m]
 
 
 def philox_uniforms(seed, subsequence, offset, skip, n, use_ref=False):

@@ -712,3 +712,54 @@ int64_t orc_select_hits(const gbo_sphoton* p, int64_t n, uint32_t hitmask, gbo_s
     }
     return h;
 }
+
+/* ---- hit merge (sysrap/sphoton.h:277-304 key_functor / reduce_op, sysrap/SPM.cu merge_partial_select) ----------
+ * key = identity << 48 | (unsigned)(time / tw), stable sort by key, then each run of equal keys becomes the hit
+ * with the earliest time (the earlier one in photon order on a tie), flagmasks ORed, hitcounts (16 bits) summed.
+ * tw = 0 returns the hits unmerged (NOMERGE_TIME_WINDOW). */
+typedef struct { uint64_t key; int64_t idx; } orc_keyidx;
+
+static int cmp_keyidx(const void* a, const void* b)
+{
+    const orc_keyidx* x = (const orc_keyidx*)a;
+    const orc_keyidx* y = (const orc_keyidx*)b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->idx < y->idx ? -1 : (x->idx > y->idx ? 1 : 0);
+}
+
+static uint64_t merge_key(const gbo_sphoton* p, float tw)
+{
+    const unsigned id = p->identity & 0x00ffffffu;
+    const unsigned bucket = (unsigned)(p->time / tw);
+    return ((uint64_t)id << 48) | (uint64_t)bucket;
+}
+
+int64_t orc_merge_hits(const gbo_sphoton* in, int64_t n, float tw, gbo_sphoton* out)
+{
+    if (n <= 0) return 0;
+    if (tw == 0.f) {
+        for (int64_t i = 0; i < n; i++) out[i] = in[i];
+        return n;
+    }
+    orc_keyidx* k = (orc_keyidx*)malloc(sizeof(orc_keyidx) * (size_t)n);
+    for (int64_t i = 0; i < n; i++) { k[i].key = merge_key(&in[i], tw); k[i].idx = i; }
+    qsort(k, (size_t)n, sizeof(orc_keyidx), cmp_keyidx);
+    int64_t m = 0;
+    for (int64_t i = 0; i < n;) {
+        gbo_sphoton r = in[k[i].idx];
+        int64_t j = i + 1;
+        for (; j < n && k[j].key == k[i].key; j++) {
+            const gbo_sphoton* b = &in[k[j].idx];
+            const int a_first = fminf(r.time, b->time) == r.time;
+            const unsigned fm = r.flagmask | b->flagmask;
+            const unsigned hc = ((r.hitcount_iindex >> 16) + (b->hitcount_iindex >> 16)) & 0xffffu;
+            if (!a_first) r = *b;
+            r.flagmask = fm;
+            r.hitcount_iindex = (r.hitcount_iindex & 0x0000ffffu) | (hc << 16);
+        }
+        out[m++] = r;
+        i = j;
+    }
+    free(k);
+    return m;
+}
