@@ -167,3 +167,22 @@ def test_expression_evaluator_refuses_code():
     for bad in ("__import__('os')", "open('x')", "(1).__class__", "[1,2]", "lambda: 1"):
         with pytest.raises((ValueError, SyntaxError)):
             ex(bad)
+
+
+def test_csgfoundry_round_trip(oracle, tmp_path):
+    """A CSGFoundry folder in the reference's layout (CSGFoundry/*.npy + SSim/stree/standard) loads back to the same
+    arrays and the same simulation."""
+    from eic_opticks_gb300 import csgfoundry, geometry as G, gensteps as GS
+    g, _ = __import__("eic_opticks_gb300.gdml", fromlist=["load"]).load(DOC)
+    for arrays in (g.arrays(), G.crystal_array().arrays()):
+        d = csgfoundry.save(arrays, str(tmp_path / ("x%d" % len(arrays["inst"]))))
+        assert os.path.exists(os.path.join(d, "SSim", "stree", "standard", "bnd.npy"))
+        back = csgfoundry.load(os.path.dirname(d))
+        for k in ("node", "prim", "inst", "itra", "plan", "bnd", "optical", "icdf"):
+            assert np.array_equal(np.asarray(back[k]).view(np.uint8), np.asarray(arrays[k]).view(np.uint8)), k
+        assert np.array_equal(back["solid"].view(np.uint8), arrays["solid"].view(np.uint8))
+        assert back["hd_factor"] == arrays["hd_factor"] and tuple(back["domain"]) == tuple(arrays["domain"])
+    gs = GS.crystal_scint_gensteps(4, 100, seed=2)
+    a, _ = oracle.simulate(oracle.SimConfig(arrays), gs)
+    b, _ = oracle.simulate(oracle.SimConfig(back), gs)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
