@@ -1,0 +1,163 @@
+// gbo_gensteps.hh : header-only C++ genstep producers for a Geant4 application's stepping actions, without Geant4
+// types in the signatures.
+//
+// The reference fills its gensteps from G4Track / G4Step inside U4::CollectGenstep_DsG4Scintillation_r4695 and
+// U4::CollectGenstep_G4Cerenkov_modified (u4/U4.cc:82-305) and appends them with SEvt::AddGenstep.  The same
+// quad6 payloads (sysrap/sscint.h:34-62, sysrap/scerenkov.h:29-58) are produced here from plain values a stepping
+// action reads off its G4Step:
+//
+//     gbo::StepPoints sp;                      // pre/post position (mm), global time (ns), velocity (mm/ns)
+//     sp.pre = {{x0.x(), x0.y(), x0.z()}, pre->GetGlobalTime(), pre->GetVelocity()};  ...
+//     gbo::SEvt::AddGenstep(gbo::MakeGenstep_DsG4Scintillation_r4695(track, sp, matline, n, scnt, tau));
+//
+// `matline` is the boundary-texture line of the step's material (4 * boundary + 3 for a boundary whose inner
+// material it is); the reference maps Geant4 material indices to those lines in SEvt::setGenstep.
+// CerenkovMeanPhotonsPerMM restates the Cerenkov yield of u4/Local_G4Cerenkov_modified.cc
+// (GetAverageNumberOfPhotons): 369.81 photons / (eV cm) x charge^2 x the integral over photon energy of
+// (1 - 1/(beta n)^2) where beta n > 1, with n(E) linear between the table points and the threshold crossings
+// solved on each segment (n need not be monotonic).
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "gbopticks.h"
+
+namespace gbo {
+
+struct StepPoint {
+    double pos[3];      // mm
+    double time;        // global time, ns
+    double velocity;    // mm/ns
+};
+
+struct StepPoints {
+    StepPoint pre, post;
+};
+
+struct TrackInfo {
+    int32_t trackid = 0;
+    int32_t pdg_code = 0;
+    double charge = 0.0;    // units of the positron charge
+    double weight = 1.0;
+};
+
+constexpr double HC_EVNM = 1239.8418754200;       // h c in eV nm (sysrap/smath.h)
+
+namespace detail {
+inline void put_f(gbo_quad6& g, int q, int c, double v) { g.q[q].f[c] = (float)v; }
+inline void put_u(gbo_quad6& g, int q, int c, uint32_t v) { g.q[q].u[c] = v; }
+inline void put_i(gbo_quad6& g, int q, int c, int32_t v) { g.q[q].i[c] = v; }
+
+inline void common(gbo_quad6& g, uint32_t gentype, const TrackInfo& t, const StepPoints& s, uint32_t matline,
+                   int32_t numphoton)
+{
+    std::memset(&g, 0, sizeof(g));
+    put_u(g, 0, 0, gentype);
+    put_u(g, 0, 1, (uint32_t)t.trackid);
+    put_u(g, 0, 2, matline);
+    put_u(g, 0, 3, (uint32_t)numphoton);
+    for (int k = 0; k < 3; k++) put_f(g, 1, k, s.pre.pos[k]);
+    put_f(g, 1, 3, s.pre.time);
+    double len2 = 0.0;
+    for (int k = 0; k < 3; k++) {
+        const double d = s.post.pos[k] - s.pre.pos[k];       // G4Step::GetDeltaPosition, not normalized
+        put_f(g, 2, k, d);
+        len2 += d * d;
+    }
+    put_f(g, 2, 3, std::sqrt(len2));                         // step_length
+    put_i(g, 3, 0, t.pdg_code);
+    put_f(g, 3, 1, t.charge);
+    put_f(g, 3, 2, t.weight);
+}
+}  // namespace detail
+
+// sscint layout: q3.w meanVelocity, q4.x scnt, q5.x ScintillationTime (u4/U4.cc:82-140)
+inline gbo_quad6 MakeGenstep_DsG4Scintillation_r4695(const TrackInfo& t, const StepPoints& s, uint32_t matline,
+                                                      int32_t numPhotons, int32_t scnt, double ScintillationTime)
+{
+    gbo_quad6 g;
+    detail::common(g, GBO_GS_DsG4Scintillation_r4695, t, s, matline, numPhotons);
+    detail::put_f(g, 3, 3, 0.5 * (s.pre.velocity + s.post.velocity));
+    detail::put_i(g, 4, 0, scnt);
+    detail::put_f(g, 5, 0, ScintillationTime);
+    return g;
+}
+
+// scerenkov layout: q3.w preVelocity, q4 (BetaInverse, Wmin, Wmax, maxCos), q5 (maxSin2, MeanNumberOfPhotons1,
+// MeanNumberOfPhotons2, postVelocity); Wmin/Wmax in nm from the photon energy range pmin/pmax in eV (u4/U4.cc:200-260)
+inline gbo_quad6 MakeGenstep_G4Cerenkov_modified(const TrackInfo& t, const StepPoints& s, uint32_t matline,
+                                                  int32_t numPhotons, double betaInverse, double pmin_eV,
+                                                  double pmax_eV, double maxCos, double maxSin2,
+                                                  double meanNumberOfPhotons1, double meanNumberOfPhotons2)
+{
+    gbo_quad6 g;
+    detail::common(g, GBO_GS_G4Cerenkov_modified, t, s, matline, numPhotons);
+    detail::put_f(g, 3, 3, s.pre.velocity);
+    detail::put_f(g, 4, 0, betaInverse);
+    detail::put_f(g, 4, 1, HC_EVNM / pmax_eV);
+    detail::put_f(g, 4, 2, HC_EVNM / pmin_eV);
+    detail::put_f(g, 4, 3, maxCos);
+    detail::put_f(g, 5, 0, maxSin2);
+    detail::put_f(g, 5, 1, meanNumberOfPhotons1);
+    detail::put_f(g, 5, 2, meanNumberOfPhotons2);
+    detail::put_f(g, 5, 3, s.post.velocity);
+    return g;
+}
+
+// Mean Cerenkov photons per mm for a particle of `charge` and `beta` in a medium with refractive index n(E) given at
+// increasing photon energies (eV).
+inline double CerenkovMeanPhotonsPerMM(double charge, double beta, const double* energy_eV, const double* rindex,
+                                       int n)
+{
+    if (beta <= 0.0 || n < 2) return 0.0;
+    const double bi2 = 1.0 / (beta * beta);
+    double integral = 0.0;
+    for (int i = 0; i + 1 < n; i++) {
+        const double e0 = energy_eV[i], e1 = energy_eV[i + 1];
+        const double n0 = rindex[i], n1 = rindex[i + 1];
+        if (e1 <= e0) continue;
+        // f(E) = 1 - bi2 / n(E)^2 over the part of [e0, e1] where n(E) > 1/beta (n linear in E)
+        const double thr = 1.0 / beta;
+        double a = e0, b = e1;
+        const bool in0 = n0 > thr, in1 = n1 > thr;
+        if (!in0 && !in1) continue;
+        if (in0 != in1) {
+            const double ec = e0 + (thr - n0) * (e1 - e0) / (n1 - n0);      // crossing of n = 1/beta
+            if (in0) b = ec; else a = ec;
+        }
+        // exact integral of 1 - bi2 / (p + q E)^2 with n = p + q E on [a, b]
+        const double q = (n1 - n0) / (e1 - e0);
+        const double p = n0 - q * e0;
+        const double na = p + q * a, nb = p + q * b;
+        const double inv = std::fabs(q) > 0.0 ? (1.0 / na - 1.0 / nb) / q : (b - a) / (na * na);
+        integral += (b - a) - bi2 * inv;
+    }
+    return 36.981 * charge * charge * integral;            // 369.81 / (eV cm) = 36.981 / (eV mm)
+}
+
+// Cerenkov step quantities from the medium's n(E) and the pre/post velocities, as G4Cerenkov_modified prepares them:
+// BetaInverse at the pre point, maxCos = BetaInverse / nMax, maxSin2 = (1 - maxCos)(1 + maxCos), the mean photon
+// numbers at the pre and post betas for the step length, energy range of the table.
+inline gbo_quad6 MakeGenstep_Cerenkov_FromTable(const TrackInfo& t, const StepPoints& s, uint32_t matline,
+                                                int32_t numPhotons, const double* energy_eV, const double* rindex,
+                                                int n)
+{
+    const double c = 299.792458;
+    const double beta_pre = s.pre.velocity / c, beta_post = s.post.velocity / c;
+    double nmax = rindex[0];
+    for (int i = 1; i < n; i++) nmax = rindex[i] > nmax ? rindex[i] : nmax;
+    const double bi = 1.0 / beta_pre;
+    const double maxCos = bi / nmax;
+    double len2 = 0.0;
+    for (int k = 0; k < 3; k++) len2 += (s.post.pos[k] - s.pre.pos[k]) * (s.post.pos[k] - s.pre.pos[k]);
+    const double step = std::sqrt(len2);
+    const double m1 = CerenkovMeanPhotonsPerMM(t.charge, beta_pre, energy_eV, rindex, n) * step;
+    const double m2 = CerenkovMeanPhotonsPerMM(t.charge, beta_post, energy_eV, rindex, n) * step;
+    return MakeGenstep_G4Cerenkov_modified(t, s, matline, numPhotons, bi, energy_eV[0], energy_eV[n - 1], maxCos,
+                                           (1.0 - maxCos) * (1.0 + maxCos), m1, m2);
+}
+
+}  // namespace gbo
