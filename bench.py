@@ -115,7 +115,7 @@ WORKLOADS = {
 }
 
 
-def workload(seed=1, num_gs=2000, kind="crystal_array"):
+def workload(seed=1, num_gs=None, kind="crystal_array"):
     """One event of each benchmark configuration: (geometry arrays, gensteps, input photons or None).
 
     nested_boxes : 100,000 input photons at the origin, isotropic, 420 nm, in the vacuum/lead/air/water boxes.
@@ -132,8 +132,8 @@ def workload(seed=1, num_gs=2000, kind="crystal_array"):
         g = G.water_cube()
         return g.arrays(), GS.water_cerenkov_gensteps(g, 1000, seed=seed), None
     if kind == "large_sphere":
-        return G.large_sphere().arrays(), GS.sphere_scint_gensteps(20000, 5000, seed=seed), None
-    return G.crystal_array().arrays(), GS.crystal_scint_gensteps(num_gs, 5000, seed=seed), None
+        return G.large_sphere().arrays(), GS.sphere_scint_gensteps(num_gs or 20000, 5000, seed=seed), None
+    return G.crystal_array().arrays(), GS.crystal_scint_gensteps(num_gs or 2000, 5000, seed=seed), None
 
 
 def photon_sample(gs, inp, n):
@@ -421,7 +421,8 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the batched-serving comparison")
-    ap.add_argument("--gensteps", type=int, default=2000, help="gensteps per event (2000 is the benchmark workload)")
+    ap.add_argument("--gensteps", type=int, default=None,
+                    help="gensteps per event (default: the workload's own, 2000 for the crystal array)")
     ap.add_argument("--workload", default="crystal_array", choices=sorted(WORKLOADS))
     ap.add_argument("--batch-events", type=int, default=None,
                     help="events of the workload for the same-configuration plain vs batched comparison")
@@ -527,8 +528,8 @@ def main():
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if not args.precision else "f32+f64",
         "data": "synthetic (seeded numpy gensteps with the reference genstep layout)",
-        "config": {"workload": (WORKLOADS[args.workload] if args.workload != "crystal_array" or args.gensteps == 2000
-                                else WORKLOAD + "_%dgs" % args.gensteps),
+        "config": {"workload": (WORKLOADS[args.workload] if args.gensteps is None
+                                else WORKLOADS[args.workload] + "_%dgs" % args.gensteps),
                    "precision": "binary64 root polish + accumulators" if args.precision else "binary32",
                    "photons_per_step": n_photon, "gensteps_per_step": len(gs),
                    "hits_per_step": hits, "path": "plain: one event per launch", "l2": "flushed (256 MB write) between timed steps",

@@ -14,6 +14,10 @@
 
 namespace gbo {
 
+// Leaf types the benchmark and test geometries use rarely stay out of line, to keep the traversal loop's code (and
+// the instruction cache it needs) small; the common ones (sphere, zsphere, cylinder, box3) are inlined.
+#define GBO_COLD __device__ __noinline__
+
 constexpr float RT_DEFAULT_MAX = 1.e27f;
 
 struct NodeView {            // the parts of a CSGNode the intersectors read
@@ -268,7 +272,7 @@ GBO_DEV bool leaf_box3(float4& is, float4 q0, float t_min, float3 ro, float3 rd)
 GBO_DEV float fmin4(float a, float b, float c, float d) { return fminf(fminf(a, b), fminf(c, d)); }
 
 // csg_intersect_leaf_newcone.h:38-121
-GBO_DEV bool leaf_cone(float4& is, float4 q0, float t_min, float3 o, float3 d)
+GBO_COLD bool leaf_cone(float4& is, float4 q0, float t_min, float3 o, float3 d)
 {
     const float r1 = q0.x, z1 = q0.y, r2 = q0.z, z2 = q0.w;
     const float r1r1 = r1 * r1, r2r2 = r2 * r2;
@@ -306,7 +310,7 @@ GBO_DEV bool leaf_cone(float4& is, float4 q0, float t_min, float3 o, float3 d)
 }
 
 // csg_intersect_leaf_convexpolyhedron.h:40-106
-GBO_DEV bool leaf_convexpolyhedron(float4& is, float4 q0, const float4* plan, float t_min, float3 ro, float3 rd)
+GBO_COLD bool leaf_convexpolyhedron(float4& is, float4 q0, const float4* plan, float t_min, float3 ro, float3 rd)
 {
     float t0 = -__int_as_float(0x7f800000), t1 = __int_as_float(0x7f800000);
     float3 t0n = f3(0.f, 0.f, 0.f), t1n = f3(0.f, 0.f, 0.f);
@@ -334,7 +338,7 @@ GBO_DEV bool leaf_convexpolyhedron(float4& is, float4 q0, const float4* plan, fl
 }
 
 // csg_intersect_leaf_hyperboloid.h:36-106
-GBO_DEV bool leaf_hyperboloid(float4& is, float4 q0, float t_min, float3 ro, float3 rd)
+GBO_COLD bool leaf_hyperboloid(float4& is, float4 q0, float t_min, float3 ro, float3 rd)
 {
     const float zero = 0.f, one = 1.f;
     const float r0 = q0.x, zf = q0.y, z1 = q0.z, z2 = q0.w;
@@ -379,7 +383,7 @@ GBO_DEV bool leaf_hyperboloid(float4& is, float4 q0, float t_min, float3 ro, flo
 }
 
 // csg_intersect_leaf_halfspace.h
-GBO_DEV bool leaf_halfspace(float4& is, float4 q0, float t_min, float3 o, float3 d)
+GBO_COLD bool leaf_halfspace(float4& is, float4 q0, float t_min, float3 o, float3 d)
 {
     const float3 n = f3(q0.x, q0.y, q0.z);
     const float on = dot(o, n), dn = dot(d, n);
@@ -394,7 +398,7 @@ GBO_DEV bool leaf_halfspace(float4& is, float4 q0, float t_min, float3 o, float3
 }
 
 // csg_intersect_leaf_phicut.h:580-640
-GBO_DEV bool leaf_phicut(float4& is, float4 q0, float t_min, float3 o, float3 d)
+GBO_COLD bool leaf_phicut(float4& is, float4 q0, float t_min, float3 o, float3 d)
 {
     const float cosPhi0 = q0.x, sinPhi0 = q0.y, cosPhi1 = q0.z, sinPhi1 = q0.w;
     const float d_n0 = d.x * sinPhi0 + d.y * (-cosPhi0);

@@ -33,7 +33,13 @@ namespace gbo {
 #define GBO_SIM_MINB 1              // minimum resident blocks per SM asked of ptxas for the simulate kernels
 #endif
 #ifndef GBO_POOL_MINB
-#define GBO_POOL_MINB 1             // the same for the persistent photon-pool kernel
+#define GBO_POOL_MINB 4             // the same for the persistent photon-pool kernel: 4 x 128 threads per SM (128
+                                    // registers) measured 12 % faster than ptxas' unbounded choice on the crystal event
+#endif
+#ifdef GBO_POOL_MAXNREG                // register budget of the pool kernel instead of its launch bounds
+#define GBO_POOL_BOUNDS __maxnreg__(GBO_POOL_MAXNREG)
+#else
+#define GBO_POOL_BOUNDS __launch_bounds__(SIM_BLOCK, GBO_POOL_MINB)
 #endif
 constexpr int SIM_BLOCK = 128;
 constexpr int SCAN_WORDS = 256;     // words per block in k_word_prefix
@@ -167,7 +173,7 @@ GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng)
 }
 
 template <bool TREE, bool PRECISE>
-__global__ void __launch_bounds__(SIM_BLOCK, GBO_POOL_MINB) k_simulate_pool(const __grid_constant__ Params P,
+__global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P,
                                                              unsigned long long* pool, int refill_min, int period)
 {
     const unsigned lane = threadIdx.x & 31u;

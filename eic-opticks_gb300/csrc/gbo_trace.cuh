@@ -149,19 +149,14 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
     const float3 inv = safe_inv(dir);
     int stack[TRAVERSAL_STACK];
     int sp = 0;
+    constexpr int NONE = -0x7fffffff;
     int item = 0;
     if (hint >= 0) { stack[sp++] = 0; item = leaf_item(HINT_FIRST, 1); }
-    for (;;) {
-        int next = -0x7fffffff;
-        if (item < 0) {
-            const int code = -item - 1;
-            const int first = code >> 8, count = code & 0xff;
-#pragma unroll 1
-            for (int k = 0; k < count; k++) {
-                const int ii = first == HINT_FIRST ? hint : __ldg(a.tlas_index + first + k);
-                if (first == HINT_FIRST || ii != hint) test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b);
-            }
-        } else {
+    // while-while traversal (Aila & Laine 2009): every lane first descends inner nodes until it holds a leaf, then
+    // the lanes process their leaves together, so the expensive instance / CSG work runs with the warp converged;
+    // each lane still visits its items in the same order as a one-item-per-iteration loop
+    while (item != NONE) {
+        while (item >= 0) {
             const float4* nq = reinterpret_cast<const float4*>(a.tlas + item);
             const float4 l0 = __ldg(nq), h0 = __ldg(nq + 1), l1 = __ldg(nq + 2), h1 = __ldg(nq + 3);
             float t0, t1;
@@ -172,17 +167,26 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
             const int it1 = c1 > 0 ? leaf_item(__float_as_int(l1.w), c1) : __float_as_int(l1.w);
             if (v0 && v1) {                         // nearer child next, the other on the stack
                 const bool near0 = t0 <= t1;
-                next = near0 ? it0 : it1;
+                item = near0 ? it0 : it1;
                 if (sp < TRAVERSAL_STACK) stack[sp++] = near0 ? it1 : it0;
             } else if (v0) {
-                next = it0;
+                item = it0;
             } else if (v1) {
-                next = it1;
+                item = it1;
+            } else {
+                item = sp ? stack[--sp] : NONE;
             }
         }
-        if (next != -0x7fffffff) { item = next; continue; }
-        if (sp == 0) break;
-        item = stack[--sp];
+        while (item < 0 && item != NONE) {
+            const int code = -item - 1;
+            const int first = code >> 8, count = code & 0xff;
+#pragma unroll 1
+            for (int k = 0; k < count; k++) {
+                const int ii = first == HINT_FIRST ? hint : __ldg(a.tlas_index + first + k);
+                if (first == HINT_FIRST || ii != hint) test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b);
+            }
+            item = sp ? stack[--sp] : NONE;
+        }
     }
 
     if (b.inst < 0) {
