@@ -223,6 +223,47 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
         pad(wb);
         inst_box[i] = wb;
     }
+    // overlap lists: sort and sweep along x over the padded world boxes (closed intervals)
+    {
+        std::vector<int> by_x(num_inst);
+        for (int i = 0; i < num_inst; i++) by_x[i] = i;
+        std::sort(by_x.begin(), by_x.end(), [&](int a, int c) { return inst_box[a].lo[0] < inst_box[c].lo[0]; });
+        std::vector<std::vector<int>> ov(num_inst);
+        std::vector<char> full(num_inst, 0);
+        for (int a = 0; a < num_inst; a++) {
+            const int i = by_x[a];
+            const Box& bi = inst_box[i];
+            for (int c = a + 1; c < num_inst && inst_box[by_x[c]].lo[0] <= bi.hi[0]; c++) {
+                const int j = by_x[c];
+                const Box& bj = inst_box[j];
+                if (bj.lo[1] > bi.hi[1] || bi.lo[1] > bj.hi[1] || bj.lo[2] > bi.hi[2] || bi.lo[2] > bj.hi[2]) continue;
+                for (int e : {i, j}) {
+                    const int other = e == i ? j : i;
+                    if (full[e]) continue;
+                    if ((int)ov[e].size() >= MAX_OVERLAP) { full[e] = 1; ov[e].clear(); continue; }
+                    ov[e].push_back(other);
+                }
+            }
+        }
+        out.inst_box.resize(num_inst);
+        for (int i = 0; i < num_inst; i++) {
+            InstBox& ib = out.inst_box[i];
+            for (int k = 0; k < 3; k++) {
+                // binary32 box inside the binary64 one, so that a point found inside it is inside the box the
+                // overlaps were computed with
+                float lo = (float)inst_box[i].lo[k], hi = (float)inst_box[i].hi[k];
+                if ((double)lo < inst_box[i].lo[k]) lo = std::nextafter(lo, INFINITY);
+                if ((double)hi > inst_box[i].hi[k]) hi = std::nextafter(hi, -INFINITY);
+                ib.lo[k] = lo;
+                ib.hi[k] = hi;
+            }
+            std::sort(ov[i].begin(), ov[i].end());
+            ib.overlap_first = (int32_t)out.overlap.size();
+            ib.overlap_count = full[i] ? -1 : (int32_t)ov[i].size();
+            if (!full[i]) out.overlap.insert(out.overlap.end(), ov[i].begin(), ov[i].end());
+        }
+        if (out.overlap.empty()) out.overlap.push_back(0);
+    }
     out.tlas_index.resize(num_inst);
     for (int i = 0; i < num_inst; i++) out.tlas_index[i] = i;
     Builder b(out.tlas_index, out.tlas);

@@ -52,6 +52,17 @@ struct PrimDev {
 };
 static_assert(sizeof(PrimDev) == 32, "PrimDev is 32 bytes");
 
+// World box of an instance (padded, rounded inward to binary32) and its overlap list: the other instances whose
+// boxes meet it, as a range of AccelHost::overlap (count -1: more than MAX_OVERLAP, use the TLAS).
+struct InstBox {
+    float lo[3];
+    int32_t overlap_first;
+    float hi[3];
+    int32_t overlap_count;
+};
+static_assert(sizeof(InstBox) == 32, "InstBox is 32 bytes");
+constexpr int MAX_OVERLAP = 8;
+
 struct SolidDev {
     int32_t prim_offset;
     int32_t num_prim;
@@ -65,6 +76,8 @@ struct AccelHost {
     std::vector<double> inst64;          // the same inverse columns in binary64, 12 per instance (precision mode)
     std::vector<PrimDev> prim;
     std::vector<SolidDev> solid;
+    std::vector<InstBox> inst_box;
+    std::vector<int32_t> overlap;
     int max_depth = 0;
 };
 

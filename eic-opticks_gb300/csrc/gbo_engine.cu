@@ -520,6 +520,8 @@ struct gbo_engine {
     DBuf<int32_t> tlas_index;
     DBuf<InstDev> inst;
     DBuf<double> inst64;                   // precision mode only
+    DBuf<InstBox> inst_box;
+    DBuf<int32_t> overlap;
     DBuf<PrimDev> prim;
     DBuf<SolidDev> solid;
     DBuf<gbo_csgnode> node;
@@ -654,7 +656,7 @@ void gbo_engine_destroy(gbo_engine* e)
     if (e->icdf_tex) cudaDestroyTextureObject(e->icdf_tex);
     if (e->bnd_array) cudaFreeArray(e->bnd_array);
     if (e->icdf_array) cudaFreeArray(e->icdf_array);
-    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->prim.release(); e->solid.release();
+    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->inst_box.release(); e->overlap.release(); e->prim.release(); e->solid.release();
     e->node.release(); e->plan.release(); e->itra.release(); e->optical.release();
     e->gs.release(); e->gs_end.release(); e->input.release(); e->photon.release(); e->seq.release();
     e->hits_unordered.release(); e->hits.release(); e->merged.release(); e->bitmap.release(); e->word_prefix.release();
@@ -718,6 +720,8 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     TRY(upload(e->tlas_index, acc.tlas_index.data(), acc.tlas_index.size(), e->stream));
     TRY(upload(e->inst, acc.inst.data(), acc.inst.size(), e->stream));
     if (e->cfg.precision) TRY(upload(e->inst64, acc.inst64.data(), acc.inst64.size(), e->stream));
+    TRY(upload(e->inst_box, acc.inst_box.data(), acc.inst_box.size(), e->stream));
+    TRY(upload(e->overlap, acc.overlap.data(), acc.overlap.size(), e->stream));
     TRY(upload(e->prim, acc.prim.data(), acc.prim.size(), e->stream));
     TRY(upload(e->solid, acc.solid.data(), acc.solid.size(), e->stream));
     TRY(upload(e->node, g->node, (size_t)g->num_node, e->stream));
@@ -766,6 +770,8 @@ static Params make_params(gbo_engine* e)
     P.acc.tlas_index = e->tlas_index.ptr;
     P.acc.inst = e->inst.ptr;
     P.acc.inst64 = e->inst64.ptr;
+    P.acc.inst_box = reinterpret_cast<const float4*>(e->inst_box.ptr);
+    P.acc.overlap = e->overlap.ptr;
     P.acc.prim = e->prim.ptr;
     P.acc.solid = e->solid.ptr;
     P.acc.node = e->node.ptr;

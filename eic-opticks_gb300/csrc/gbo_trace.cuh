@@ -29,7 +29,21 @@ struct Accel {
     const float4* plan;
     const gbo_qat4* itra;
     const double* inst64;       // binary64 inverse columns, 12 per instance (precision mode only)
+    const float4* inst_box;     // InstBox per instance (2 x float4): world box, overlap list range
+    const int* overlap;         // overlap lists
 };
+
+// p inside the box by a margin of ~30 binary32 ulp of the coordinates involved: far above the rounding of p and of
+// pos + t dir, far below the boxes' padding (1e-5 x extent + 1e-3 mm), so photons sitting on a face of their
+// instance's solid still pass
+GBO_DEV bool inside_box(float4 lo, float4 hi, float3 p)
+{
+    const float mx = 2e-6f * (fabsf(p.x) + fabsf(lo.x) + fabsf(hi.x)) + 1e-5f;
+    const float my = 2e-6f * (fabsf(p.y) + fabsf(lo.y) + fabsf(hi.y)) + 1e-5f;
+    const float mz = 2e-6f * (fabsf(p.z) + fabsf(lo.z) + fabsf(hi.z)) + 1e-5f;
+    return p.x > lo.x + mx && p.x < hi.x - mx && p.y > lo.y + my && p.y < hi.y - my && p.z > lo.z + mz &&
+           p.z < hi.z - mz;
+}
 
 GBO_DEV bool slab(float4 bmin, float4 bmax, float3 o, float3 inv, float tmin, float tmax, float& tnear)
 {
@@ -136,7 +150,9 @@ GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float
 }
 
 constexpr int TRAVERSAL_STACK = 64;
-constexpr int HINT_FIRST = 0x7fffff;     // leaf item standing for the hint instance
+
+constexpr int HINT_FIRST = 0x7fffff;     // leaf item standing for the photon's previous instance
+constexpr int OVERLAP_FIRST = 0x7ffffe;  // leaf item standing for that instance's overlap list
 
 // work items: an inner node index (>= 0) or a leaf range encoded as -(1 + (first << 8 | count))
 GBO_DEV int leaf_item(int first, int count) { return -(1 + ((first << 8) | count)); }
@@ -151,10 +167,13 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
     int sp = 0;
     constexpr int NONE = -0x7fffffff;
     int item = 0;
+    int ov_first = 0;
     if (hint >= 0) { stack[sp++] = 0; item = leaf_item(HINT_FIRST, 1); }
     // while-while traversal (Aila & Laine 2009): every lane first descends inner nodes until it holds a leaf, then
     // the lanes process their leaves together, so the expensive instance / CSG work runs with the warp converged;
-    // each lane still visits its items in the same order as a one-item-per-iteration loop
+    // each lane still visits its items in the same order as a one-item-per-iteration loop.  Leaf items are TLAS
+    // leaves, the photon's previous instance (HINT_FIRST) or that instance's overlap list (OVERLAP_FIRST), all
+    // tested at the single test_instance call site.
     while (item != NONE) {
         while (item >= 0) {
             const float4* nq = reinterpret_cast<const float4*>(a.tlas + item);
@@ -182,8 +201,21 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
             const int first = code >> 8, count = code & 0xff;
 #pragma unroll 1
             for (int k = 0; k < count; k++) {
-                const int ii = first == HINT_FIRST ? hint : __ldg(a.tlas_index + first + k);
-                if (first == HINT_FIRST || ii != hint) test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b);
+                const int ii = first == HINT_FIRST ? hint
+                             : first == OVERLAP_FIRST ? __ldg(a.overlap + ov_first + k) : __ldg(a.tlas_index + first + k);
+                if (first >= OVERLAP_FIRST || ii != hint) test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b);
+            }
+            if (first == HINT_FIRST) {
+                // when the previous instance's closest hit keeps the whole segment inside its box, only the instances
+                // whose boxes overlap that box can hold a closer hit: their short list replaces the TLAS
+                const float4 blo = __ldg(a.inst_box + 2 * hint), bhi = __ldg(a.inst_box + 2 * hint + 1);
+                const int ocount = __float_as_int(bhi.w);
+                if (ocount >= 0 && inside_box(blo, bhi, pos) && inside_box(blo, bhi, pos + b.t * dir)) {
+                    ov_first = __float_as_int(blo.w);
+                    sp = 0;
+                    item = ocount > 0 ? leaf_item(OVERLAP_FIRST, ocount) : NONE;
+                    continue;
+                }
             }
             item = sp ? stack[--sp] : NONE;
         }

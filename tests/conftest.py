@@ -39,3 +39,23 @@ def golden_arrays(z):
 
 SIM_FIXTURES = ["nested_boxes", "nested_boxes_sensor", "crystal_array", "water_cube", "torch", "large_sphere_small",
                 "gdml_raindrop", "gdml_sipm8x8", "gdml_sphere_leak", "gdml_basic_detector"]
+
+
+INT_WORDS = [7, 12, 13, 14, 15]            # hitcount_iindex, orient_boundary_flag, identity, index, flagmask
+
+
+def assert_photons_agree(a, b, pos_mm=1e-2, time_ns=1e-3, unit=1e-4):
+    """Two kernels' photon records for the same photons: integer words identical, float words within bounds.
+
+    Different kernels (one thread per photon, photon pool, no-allocation) are fused mul+add by ptxas differently
+    under their own register budgets, so their binary32 results can differ in the last bits, which later steps
+    can grow; the bounds are those of the reference parity (positions, times) and of a unit vector's rounding.
+    Returns the largest differences seen."""
+    wa, wb = a.view(np.uint32).reshape(-1, 16), b.view(np.uint32).reshape(-1, 16)
+    assert np.array_equal(wa[:, INT_WORDS], wb[:, INT_WORDS])
+    dpos = np.abs(a["pos"] - b["pos"]).max(initial=0.0)
+    dt = np.abs(a["time"] - b["time"]).max(initial=0.0)
+    dvec = max(np.abs(a["mom"] - b["mom"]).max(initial=0.0), np.abs(a["pol"] - b["pol"]).max(initial=0.0))
+    dwl = np.abs(a["wavelength"] - b["wavelength"]).max(initial=0.0)
+    assert dpos <= pos_mm and dt <= time_ns and dvec <= unit and dwl <= unit, (dpos, dt, dvec, dwl)
+    return dpos, dt, dvec, dwl

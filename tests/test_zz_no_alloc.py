@@ -1,14 +1,17 @@
 """gbo_simulate_noalloc : the simulation entry point for callers that cannot allocate device memory per event.
 
-Its hits must equal those of the allocating device entry point (gbo_simulate_device) for the same event, bit for
-bit (the photon program is deterministic), on two calls in a row so that state left in the shared scratch array
-by the first call cannot leak into the second.  This file is collected last so that a run stopping at the first
-failure has already run every other test; it also passes alone in a fresh process.
+Its hits must equal those of the allocating device entry point (gbo_simulate_device) for the same event: the same
+photons, indices, flags and histories, float words within a few ulp (the no-allocation kernel is a separate kernel,
+and ptxas fuses mul+add per kernel), and a repeated call must give the same bytes again, so that state left in the
+shared scratch array by one call cannot leak into the next.  This file is collected last so that a run stopping at
+the first failure has already run every other test; it also passes alone in a fresh process.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
+
+from conftest import assert_photons_agree
 
 pytestmark = pytest.mark.gpu
 
@@ -45,14 +48,19 @@ def test_scratch_is_modest(setup):
 
 def test_noalloc_matches_device_entry_point_twice(setup):
     torch, E, lib, eng, gs, d_gs = setup
-    for event_id in (5, 6):
+    first = {}
+    for event_id in (5, 6, 5):
         want_n = eng.simulate_device(event_id, d_gs.data_ptr(), len(gs))
         want = eng.hits()
         rc, n, d_hits = noalloc_hits(torch, E, lib, eng, d_gs, len(gs), event_id, 2 * want_n + 16)
         assert rc == 0, lib.gbo_last_error()
         assert n == want_n
         got = d_hits[:n].cpu().numpy().view(E.L.PHOTON).reshape(-1)
-        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+        print("no-alloc vs device entry point, event %d: max |dpos| %.3g mm, |dt| %.3g ns, |dvec| %.3g, |dwl| %.3g"
+              % ((event_id,) + assert_photons_agree(got, want)))
+        if event_id in first:
+            assert np.array_equal(got.view(np.uint32), first[event_id])       # repeated call: same bytes
+        first[event_id] = got.view(np.uint32).copy()
 
 
 def test_noalloc_rejects_sizes_beyond_limits(setup):
