@@ -143,6 +143,10 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
     }
     out.solid.resize(num_solid);
     std::vector<Box> solid_box(num_solid);
+    // per solid: the object-space boxes of its prims when every prim is a single untransformed, uncomplemented
+    // box3 (its surface is then exactly its box's boundary); empty otherwise
+    std::vector<std::vector<Box>> exact(num_solid);
+    std::vector<char> all_exact(num_solid, 1);
     out.prim.resize(num_prim);
     for (int s = 0; s < num_solid; s++) {
         const gbo_csgsolid& so = solid[s];
@@ -173,6 +177,18 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
             const unsigned gpi = pr.q3.u[3];
             pd.prim_boundary = ((gpi & 0xffffu) << 16) | (boundary & 0xffffu);
             solid_box[s].grow(b);
+            const gbo_csgnode& nd = node[noff];
+            const bool box_leaf = nn == 1 && nd.q3.u[2] == GBO_CSG_BOX3 && nd.q3.u[3] == 0u;
+            if (box_leaf) {
+                Box e;
+                double lo2[3] = {-0.5 * nd.q0.f[0], -0.5 * nd.q0.f[1], -0.5 * nd.q0.f[2]};
+                double hi2[3] = {0.5 * nd.q0.f[0], 0.5 * nd.q0.f[1], 0.5 * nd.q0.f[2]};
+                e.grow(lo2);
+                e.grow(hi2);
+                exact[s].push_back(e);
+            } else {
+                all_exact[s] = 0;
+            }
         }
     }
     out.inst.resize(num_inst);
@@ -223,6 +239,40 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
         pad(wb);
         inst_box[i] = wb;
     }
+    // instances made only of exact boxes under a translation: their world boxes, for the containment rule below
+    std::vector<std::vector<Box>> inst_exact(num_inst);
+    for (int i = 0; i < num_inst; i++) {
+        const gbo_qat4& q = inst[i];
+        const int s = q.q1.i[3];
+        const bool translation_only = q.q0.f[0] == 1.f && q.q0.f[1] == 0.f && q.q0.f[2] == 0.f && q.q1.f[0] == 0.f &&
+                                      q.q1.f[1] == 1.f && q.q1.f[2] == 0.f && q.q2.f[0] == 0.f && q.q2.f[1] == 0.f &&
+                                      q.q2.f[2] == 1.f;
+        if (!translation_only || !all_exact[s]) continue;
+        for (const Box& e : exact[s]) {
+            Box w;
+            double lo[3], hi[3];
+            for (int k = 0; k < 3; k++) { lo[k] = e.lo[k] + q.q3.f[k]; hi[k] = e.hi[k] + q.q3.f[k]; }
+            w.grow(lo);
+            w.grow(hi);
+            inst_exact[i].push_back(w);
+        }
+    }
+    // j cannot hold a hit inside i's box when each of j's prims is an exact box that either misses i's box or
+    // contains it strictly (its surface, the box boundary, then lies outside i's box)
+    auto cannot_hit_inside = [&](int j, const Box& bi) {
+        if (inst_exact[j].empty()) return false;
+        for (const Box& e : inst_exact[j]) {
+            const double m = 1e-6 * (std::fabs(e.lo[0]) + std::fabs(e.hi[0]) + std::fabs(e.lo[1]) + std::fabs(e.hi[1]) +
+                                     std::fabs(e.lo[2]) + std::fabs(e.hi[2])) + 1e-4;
+            bool misses = false, contains = true;
+            for (int k = 0; k < 3; k++) {
+                if (e.hi[k] < bi.lo[k] || e.lo[k] > bi.hi[k]) misses = true;
+                if (!(e.lo[k] + m < bi.lo[k] && bi.hi[k] < e.hi[k] - m)) contains = false;
+            }
+            if (!misses && !contains) return false;
+        }
+        return true;
+    };
     // overlap lists: sort and sweep along x over the padded world boxes (closed intervals)
     {
         std::vector<int> by_x(num_inst);
@@ -239,7 +289,7 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
                 if (bj.lo[1] > bi.hi[1] || bi.lo[1] > bj.hi[1] || bj.lo[2] > bi.hi[2] || bi.lo[2] > bj.hi[2]) continue;
                 for (int e : {i, j}) {
                     const int other = e == i ? j : i;
-                    if (full[e]) continue;
+                    if (full[e] || cannot_hit_inside(other, inst_box[e])) continue;
                     if ((int)ov[e].size() >= MAX_OVERLAP) { full[e] = 1; ov[e].clear(); continue; }
                     ov[e].push_back(other);
                 }
