@@ -424,6 +424,8 @@ def main():
     ap.add_argument("--gensteps", type=int, default=None,
                     help="gensteps per event (default: the workload's own, 2000 for the crystal array)")
     ap.add_argument("--workload", default="crystal_array", choices=sorted(WORKLOADS))
+    ap.add_argument("--form", default=None,
+                    help="kernel form MODE,REFILL,PERIOD instead of the autotuner's choice (MODE 0: photon pool)")
     ap.add_argument("--batch-events", type=int, default=None,
                     help="events of the workload for the same-configuration plain vs batched comparison")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
@@ -452,7 +454,13 @@ def main():
     n_inp = 0 if inp is None else len(inp)
     eng = E.Engine(geom, device=local, precision=args.precision)
     # kernel form picked by the autotuner on a 10% sample of the workload (setup, outside the timed region)
-    if inp is None:
+    if args.form:
+        mode, refill, period = (int(x) for x in args.form.split(","))
+        eng.close()
+        eng = E.Engine(geom, device=local, precision=args.precision, kernel_mode=mode, refill_min=refill,
+                       refill_period=period)
+        tune = {"kernel_mode": mode, "refill_min": refill, "refill_period": period}
+    elif inp is None:
         tune = eng.autotune(0, gs[: max(1, len(gs) // 10)], trials=2)
     else:
         tune = eng.autotune(0, gs, inp, trials=2)
@@ -535,7 +543,7 @@ def main():
                    "hits_per_step": hits, "path": "plain: one event per launch", "l2": "flushed (256 MB write) between timed steps",
                    "kernel": {"mode": "photon pool" if tune["kernel_mode"] == 0 else "one thread per photon",
                               "refill_min": tune["refill_min"], "refill_period": tune["refill_period"],
-                              "chosen_by": "autotuner on 10% sample"},
+                              "chosen_by": "--form" if args.form else "autotuner on 10% sample"},
                    "max_bounce": 31, "parallelism": "replicas" if world > 1 else "1 GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

@@ -41,6 +41,11 @@ namespace gbo {
 #else
 #define GBO_POOL_BOUNDS __launch_bounds__(SIM_BLOCK, GBO_POOL_MINB)
 #endif
+#ifdef GBO_GENERATE_INLINE
+#define GBO_GEN GBO_DEV
+#else
+#define GBO_GEN __device__ __noinline__   // photon generation runs once per photon: kept out of the bounce loop's code
+#endif
 constexpr int SIM_BLOCK = 128;
 constexpr int SCAN_WORDS = 256;     // words per block in k_word_prefix
 
@@ -73,7 +78,7 @@ struct Params {
     unsigned long long* hit_gidx;           // launch index of each unordered hit (batched launches)
 };
 
-GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng);
+GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng);
 
 // Kernel forms: TREE when any prim is a CSG tree; PRECISE for the precision mode (binary64 root polish in the
 // quadric leaves, binary64 position / time accumulators).  The default form compiles none of the latter.
@@ -132,7 +137,7 @@ __global__ void __launch_bounds__(SIM_BLOCK, GBO_SIM_MINB) k_simulate(const __gr
 
 // ---- persistent form: lanes refill from a photon pool so a warp never idles behind its longest photon --------
 
-GBO_DEV void generate(const Params& P, long long idx, Photon& p, Rng& rng)
+GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng)
 {
     int lo = 0, hi = P.num_gs - 1;
     while (lo < hi) {
