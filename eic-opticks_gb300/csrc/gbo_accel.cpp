@@ -313,6 +313,32 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
             if (!full[i]) out.overlap.insert(out.overlap.end(), ov[i].begin(), ov[i].end());
         }
         if (out.overlap.empty()) out.overlap.push_back(0);
+        // clear balls for the instances whose overlap lists overflowed (containers such as a world volume):
+        // centred on the box centre, radius the distance to the nearest other box, a little less for rounding
+        out.clear.assign(4 * (size_t)num_inst, 0.f);
+        int done = 0;
+        for (int i = 0; i < num_inst && done < 64; i++) {
+            if (!full[i]) continue;
+            done++;
+            double c[3];
+            for (int k = 0; k < 3; k++) c[k] = 0.5 * (inst_box[i].lo[k] + inst_box[i].hi[k]);
+            double r2 = 1e300;
+            for (int j = 0; j < num_inst; j++) {
+                if (j == i) continue;
+                double d2 = 0.0;
+                for (int k = 0; k < 3; k++) {
+                    const double d = c[k] < inst_box[j].lo[k] ? inst_box[j].lo[k] - c[k]
+                                   : (c[k] > inst_box[j].hi[k] ? c[k] - inst_box[j].hi[k] : 0.0);
+                    d2 += d * d;
+                }
+                r2 = std::min(r2, d2);
+            }
+            if (r2 >= 1e300) continue;                          // a single instance: its overlap list is empty
+            const double r = std::sqrt(r2) * (1.0 - 1e-6) - 1e-3;
+            if (r <= 0.0) continue;
+            for (int k = 0; k < 3; k++) out.clear[4 * (size_t)i + k] = (float)c[k];
+            out.clear[4 * (size_t)i + 3] = (float)(r * r);
+        }
     }
     out.tlas_index.resize(num_inst);
     for (int i = 0; i < num_inst; i++) out.tlas_index[i] = i;

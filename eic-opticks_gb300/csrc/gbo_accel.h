@@ -78,6 +78,9 @@ struct AccelHost {
     std::vector<SolidDev> solid;
     std::vector<InstBox> inst_box;
     std::vector<int32_t> overlap;
+    // per instance (cx, cy, cz, r^2): a ball no other instance's box enters, for instances whose overlap list is
+    // too long (r^2 = 0: none)
+    std::vector<float> clear;
     int max_depth = 0;
 };
 

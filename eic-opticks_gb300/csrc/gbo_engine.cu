@@ -36,10 +36,13 @@ namespace gbo {
 #define GBO_POOL_MINB 4             // the same for the persistent photon-pool kernel: 4 x 128 threads per SM (128
                                     // registers) measured 12 % faster than ptxas' unbounded choice on the crystal event
 #endif
+#ifndef GBO_POOL_MINB_TREE
+#define GBO_POOL_MINB_TREE GBO_POOL_MINB   // the pool kernel's form for geometries with CSG trees
+#endif
 #ifdef GBO_POOL_MAXNREG                // register budget of the pool kernel instead of its launch bounds
 #define GBO_POOL_BOUNDS __maxnreg__(GBO_POOL_MAXNREG)
 #else
-#define GBO_POOL_BOUNDS __launch_bounds__(SIM_BLOCK, GBO_POOL_MINB)
+#define GBO_POOL_BOUNDS __launch_bounds__(SIM_BLOCK, TREE ? GBO_POOL_MINB_TREE : GBO_POOL_MINB)
 #endif
 #ifdef GBO_GENERATE_INLINE
 #define GBO_GEN GBO_DEV
@@ -527,6 +530,7 @@ struct gbo_engine {
     DBuf<double> inst64;                   // precision mode only
     DBuf<InstBox> inst_box;
     DBuf<int32_t> overlap;
+    DBuf<float> clear;
     DBuf<PrimDev> prim;
     DBuf<SolidDev> solid;
     DBuf<gbo_csgnode> node;
@@ -661,7 +665,7 @@ void gbo_engine_destroy(gbo_engine* e)
     if (e->icdf_tex) cudaDestroyTextureObject(e->icdf_tex);
     if (e->bnd_array) cudaFreeArray(e->bnd_array);
     if (e->icdf_array) cudaFreeArray(e->icdf_array);
-    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->inst_box.release(); e->overlap.release(); e->prim.release(); e->solid.release();
+    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->inst_box.release(); e->overlap.release(); e->clear.release(); e->prim.release(); e->solid.release();
     e->node.release(); e->plan.release(); e->itra.release(); e->optical.release();
     e->gs.release(); e->gs_end.release(); e->input.release(); e->photon.release(); e->seq.release();
     e->hits_unordered.release(); e->hits.release(); e->merged.release(); e->bitmap.release(); e->word_prefix.release();
@@ -727,6 +731,7 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     if (e->cfg.precision) TRY(upload(e->inst64, acc.inst64.data(), acc.inst64.size(), e->stream));
     TRY(upload(e->inst_box, acc.inst_box.data(), acc.inst_box.size(), e->stream));
     TRY(upload(e->overlap, acc.overlap.data(), acc.overlap.size(), e->stream));
+    TRY(upload(e->clear, acc.clear.data(), acc.clear.size(), e->stream));
     TRY(upload(e->prim, acc.prim.data(), acc.prim.size(), e->stream));
     TRY(upload(e->solid, acc.solid.data(), acc.solid.size(), e->stream));
     TRY(upload(e->node, g->node, (size_t)g->num_node, e->stream));
@@ -777,6 +782,7 @@ static Params make_params(gbo_engine* e)
     P.acc.inst64 = e->inst64.ptr;
     P.acc.inst_box = reinterpret_cast<const float4*>(e->inst_box.ptr);
     P.acc.overlap = e->overlap.ptr;
+    P.acc.clear = reinterpret_cast<const float4*>(e->clear.ptr);
     P.acc.prim = e->prim.ptr;
     P.acc.solid = e->solid.ptr;
     P.acc.node = e->node.ptr;

@@ -31,7 +31,15 @@ struct Accel {
     const double* inst64;       // binary64 inverse columns, 12 per instance (precision mode only)
     const float4* inst_box;     // InstBox per instance (2 x float4): world box, overlap list range
     const int* overlap;         // overlap lists
+    const float4* clear;        // per instance: ball (centre, r^2) that no other instance's box enters
 };
+
+// p inside the ball (c, r^2) by a relative margin far above the rounding of p
+GBO_DEV bool inside_ball(float4 c, float3 p)
+{
+    const float dx = p.x - c.x, dy = p.y - c.y, dz = p.z - c.z;
+    return dx * dx + dy * dy + dz * dz < c.w * 0.9999f;
+}
 
 // p inside the box by a margin of ~30 binary32 ulp of the coordinates involved: far above the rounding of p and of
 // pos + t dir, far below the boxes' padding (1e-5 x extent + 1e-3 mm), so photons sitting on a face of their
@@ -210,11 +218,21 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
                 // whose boxes overlap that box can hold a closer hit: their short list replaces the TLAS
                 const float4 blo = __ldg(a.inst_box + 2 * hint), bhi = __ldg(a.inst_box + 2 * hint + 1);
                 const int ocount = __float_as_int(bhi.w);
-                if (ocount >= 0 && inside_box(blo, bhi, pos) && inside_box(blo, bhi, pos + b.t * dir)) {
+                const float3 e = pos + b.t * dir;
+                if (ocount >= 0 && inside_box(blo, bhi, pos) && inside_box(blo, bhi, e)) {
                     ov_first = __float_as_int(blo.w);
                     sp = 0;
                     item = ocount > 0 ? leaf_item(OVERLAP_FIRST, ocount) : NONE;
                     continue;
+                }
+                // a container (long overlap list): a segment inside its clear ball meets no other instance
+                if (ocount < 0) {
+                    const float4 cb = __ldg(a.clear + hint);
+                    if (cb.w > 0.f && inside_ball(cb, pos) && inside_ball(cb, e)) {
+                        sp = 0;
+                        item = NONE;
+                        continue;
+                    }
                 }
             }
             item = sp ? stack[--sp] : NONE;
