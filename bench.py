@@ -37,10 +37,10 @@ UNIT = "photons/s"
 WORKLOAD = "crystal_array_8x8_CsI_scint_2000gs_poisson5000"
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) per photon of the simulate kernel from one ncu capture of a 998,319-photon crystal-array
-# event (200 gensteps), scaled to the benchmark event by its photon count: gensteps and hits, the only DRAM traffic,
-# both grow with the photons
-TRAFFIC_B_PER_PHOTON = {"crystal_array": (501248.0 + 27392.0) / 998319}
-TRAFFIC_SOURCE = "profiles/k_simulate_pool_crystal_array.md (ncu, 1M-photon event, scaled by photons)"
+# event (200 gensteps), scaled to the benchmark event by its photon count: gensteps in, hits and hit bitmap out,
+# the only DRAM traffic, all grow with the photons
+TRAFFIC_B_PER_PHOTON = {"crystal_array": (443392.0 + 840192.0) / 998319}
+TRAFFIC_SOURCE = "profiles/k_simulate_crystal_array.md (ncu, 1M-photon event, scaled by photons)"
 
 
 def peaks():
