@@ -16,12 +16,19 @@
 #include <condition_variable>
 #include <deque>
 #include <memory>
+#include <new>
 #include <thread>
 #include <unordered_map>
 
 namespace {
 
 using Clock = std::chrono::steady_clock;
+
+// One piece's hits in host memory, left uninitialised until the device copy fills it
+struct HitPiece {
+    std::unique_ptr<gbo_sphoton[]> data;
+    size_t n = 0;
+};
 
 struct ServerEvent {
     uint64_t ticket = 0;
@@ -31,14 +38,14 @@ struct ServerEvent {
     long long num_photon = 0;
     Clock::time_point t_submit, t_done;
     int status = 0;             // 0 waiting, 1 on the GPU, 2 done, 3 failed
-    std::vector<gbo_sphoton> hits;
     std::string error;
     // an event larger than a batch runs as several pieces (genstep ranges), possibly in several slots at once
     int64_t next_gs = 0;                // first genstep not yet handed to a batch
     long long next_photon = 0;          // event-local index of that genstep's first photon
     int pieces_launched = 0, pieces_done = 0;
     bool all_launched = false;
-    std::vector<std::vector<gbo_sphoton>> piece_hits;
+    std::vector<HitPiece> piece_hits;   // hits of each piece, in photon order; the event's hits are their concatenation
+    long long num_hit = 0;
 };
 
 // One batch entry: gensteps [g0, g1) of an event, whose photons are the event's [photon_offset, +num_photon)
@@ -84,7 +91,9 @@ struct Slot {
     HBuf<gbo_quad6> h_gs;
     HBuf<unsigned long long> h_gs_end, h_ev_photon_begin, h_ev_pos0, h_ev_photon_offset, h_ev_hit, h_counters;
     HBuf<int> h_ev_gs_begin;
-    HBuf<gbo_sphoton> h_hits;
+    std::vector<HitPiece> staged;       // the current batch's hits per piece, copied from the device
+    HBuf<gbo_sphoton> h_hits;           // pinned staging of a batch's hits when they are few
+    bool direct = false;                // this batch's hits went straight into `staged`
 
     void release()
     {
@@ -93,6 +102,7 @@ struct Slot {
         input.release(); hits_unordered.release(); hits.release(); bitmap.release(); word_prefix.release();
         block_sum.release(); h_gs.release(); h_gs_end.release(); h_ev_photon_begin.release(); h_ev_pos0.release();
         h_ev_photon_offset.release(); h_ev_hit.release(); h_counters.release(); h_ev_gs_begin.release();
+        staged.clear();
         h_hits.release();
         if (exec) cudaGraphExecDestroy(exec);
         exec = nullptr;
@@ -109,6 +119,9 @@ constexpr int SERVE_MAX_DEVICES = 64;
 std::atomic<int> g_big_in_flight[SERVE_MAX_DEVICES];
 
 std::atomic<int>& big_counter(int device) { return g_big_in_flight[device >= 0 && device < SERVE_MAX_DEVICES ? device : 0]; }
+
+// a batch's hits above this size go straight from the device into per-piece host buffers
+constexpr size_t SERVE_DIRECT_HIT_BYTES = 64ull << 20;
 
 // device bytes per photon slot of a batch: bitmap + prefix bits, unordered + ordered hit capacity, hit index
 constexpr double SERVE_BYTES_PER_PHOTON = 0.25 + 64.0 + 64.0 + 8.0;
@@ -297,19 +310,25 @@ void finish_slot(gbo_server* sv, Slot& sl, int rc)
             sv->stats.events_done++;
             continue;
         }
-        const unsigned long long a = sl.h_ev_hit.ptr[k], b = sl.h_ev_hit.ptr[k + 1];
-        if ((int)ev.piece_hits.size() <= pc.index) ev.piece_hits.resize((size_t)pc.index + 1);
-        ev.piece_hits[(size_t)pc.index].assign(sl.h_hits.ptr + a, sl.h_hits.ptr + b);
-        if (ev.all_launched && ev.pieces_done == ev.pieces_launched) {
-            if (ev.piece_hits.size() == 1) {
-                ev.hits.swap(ev.piece_hits[0]);
-            } else {
-                size_t n = 0;
-                for (auto& h : ev.piece_hits) n += h.size();
-                ev.hits.reserve(n);
-                for (auto& h : ev.piece_hits) ev.hits.insert(ev.hits.end(), h.begin(), h.end());
+        if (!sl.direct) {                               // split the pinned staging into the pieces
+            const unsigned long long a = sl.h_ev_hit.ptr[k], n = sl.h_ev_hit.ptr[k + 1] - a;
+            sl.staged[k].n = (size_t)n;
+            if (n) {
+                sl.staged[k].data.reset(new (std::nothrow) gbo_sphoton[n]);
+                if (!sl.staged[k].data) {
+                    ev.status = 3;
+                    ev.error = "host memory for hits";
+                    ev.t_done = now;
+                    sv->stats.events_done++;
+                    continue;
+                }
+                std::memcpy(sl.staged[k].data.get(), sl.h_hits.ptr + a, (size_t)n * sizeof(gbo_sphoton));
             }
-            ev.piece_hits.clear();
+        }
+        if ((int)ev.piece_hits.size() <= pc.index) ev.piece_hits.resize((size_t)pc.index + 1);
+        ev.num_hit += (long long)sl.staged[k].n;
+        ev.piece_hits[(size_t)pc.index] = std::move(sl.staged[k]);
+        if (ev.all_launched && ev.pieces_done == ev.pieces_launched) {
             ev.status = 2;
             ev.t_done = now;
             sv->stats.events_done++;
@@ -336,11 +355,29 @@ void serve_loop(gbo_server* sv)
                 if (q == cudaErrorNotReady) continue;
                 if (q != cudaSuccess) { fail(GBO_ERR_CUDA, "batch failed: %s", cudaGetErrorString(q)); finish_slot(sv, sl, GBO_ERR_CUDA); continue; }
                 sl.num_hit = sl.h_counters.ptr[1];
-                int rc = sl.h_hits.ensure(sl.num_hit);
-                if (!rc && sl.num_hit &&
-                    cudaMemcpyAsync(sl.h_hits.ptr, sl.hits.ptr, sl.num_hit * sizeof(gbo_sphoton), cudaMemcpyDeviceToHost,
-                                    sl.stream) != cudaSuccess)
-                    rc = fail(GBO_ERR_CUDA, "hit download failed");
+                // few hits: one asynchronous copy into pinned staging, split per piece when the batch finishes;
+                // many hits: each piece's hits straight into host memory of its own (no second copy, no zero fill)
+                int rc = GBO_OK;
+                sl.staged.clear();
+                sl.staged.resize(sl.pieces.size());
+                sl.direct = sl.num_hit * sizeof(gbo_sphoton) > SERVE_DIRECT_HIT_BYTES;
+                if (!sl.direct) {
+                    rc = sl.h_hits.ensure(sl.num_hit);
+                    if (!rc && sl.num_hit &&
+                        cudaMemcpyAsync(sl.h_hits.ptr, sl.hits.ptr, sl.num_hit * sizeof(gbo_sphoton), cudaMemcpyDeviceToHost,
+                                        sl.stream) != cudaSuccess)
+                        rc = fail(GBO_ERR_CUDA, "hit download failed");
+                }
+                for (size_t k = 0; k < sl.pieces.size() && !rc && sl.direct; k++) {
+                    const unsigned long long a = sl.h_ev_hit.ptr[k], n = sl.h_ev_hit.ptr[k + 1] - a;
+                    sl.staged[k].n = (size_t)n;
+                    if (!n) continue;
+                    sl.staged[k].data.reset(new (std::nothrow) gbo_sphoton[n]);
+                    if (!sl.staged[k].data) { rc = fail(GBO_ERR_CAPACITY, "host memory for %llu hits", n); break; }
+                    if (cudaMemcpyAsync(sl.staged[k].data.get(), sl.hits.ptr + a, (size_t)n * sizeof(gbo_sphoton),
+                                        cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+                        rc = fail(GBO_ERR_CUDA, "hit download failed");
+                }
                 if (!rc && cudaEventRecord(sl.ev_done, sl.stream) != cudaSuccess) rc = fail(GBO_ERR_CUDA, "event record failed");
                 if (rc) { finish_slot(sv, sl, rc); continue; }
                 sl.phase = 2;
@@ -441,7 +478,7 @@ int gbo_server_config_default(gbo_server_config* c)
     if (!c) return fail(GBO_ERR_ARG, "gbo_server_config_default: null config");
     std::memset(c, 0, sizeof(*c));
     c->slots = 2;
-    c->max_batch_photon = 16ll << 20;
+    c->max_batch_photon = 64ll << 20;
     c->hbm_budget_bytes = 120ll << 30;
     c->max_batch_events = 4096;
     c->min_batch_photon = 2ll << 20;
@@ -535,7 +572,7 @@ int gbo_server_event_info(gbo_server* sv, uint64_t ticket, int64_t* num_photon, 
     ServerEvent& ev = *it->second;
     if (ev.status < 2) return fail(GBO_ERR_STATE, "gbo_server_event_info: event not done");
     if (num_photon) *num_photon = ev.num_photon;
-    if (num_hit) *num_hit = (int64_t)ev.hits.size();
+    if (num_hit) *num_hit = (int64_t)ev.num_hit;
     if (latency_s) *latency_s = std::chrono::duration<double>(ev.t_done - ev.t_submit).count();
     return GBO_OK;
 }
@@ -548,8 +585,14 @@ int gbo_server_copy_hits(gbo_server* sv, uint64_t ticket, gbo_sphoton* dst, int6
     if (it == sv->events.end()) return fail(GBO_ERR_ARG, "gbo_server_copy_hits: unknown ticket");
     ServerEvent& ev = *it->second;
     if (ev.status != 2) return fail(GBO_ERR_STATE, "gbo_server_copy_hits: event not done");
-    if (offset < 0 || count < 0 || offset + count > (int64_t)ev.hits.size()) return fail(GBO_ERR_ARG, "gbo_server_copy_hits: range outside hits");
-    if (count) std::memcpy(dst, ev.hits.data() + offset, (size_t)count * sizeof(gbo_sphoton));
+    if (offset < 0 || count < 0 || offset + count > (int64_t)ev.num_hit) return fail(GBO_ERR_ARG, "gbo_server_copy_hits: range outside hits");
+    int64_t base = 0;                                   // concatenation of the pieces, in piece order
+    for (const HitPiece& pc : ev.piece_hits) {
+        const int64_t n = (int64_t)pc.n;
+        const int64_t lo = offset > base ? offset : base, hi = offset + count < base + n ? offset + count : base + n;
+        if (hi > lo) std::memcpy(dst + (lo - offset), pc.data.get() + (lo - base), (size_t)(hi - lo) * sizeof(gbo_sphoton));
+        base += n;
+    }
     return GBO_OK;
 }
 

@@ -172,7 +172,7 @@ typedef struct gbo_server gbo_server;
 typedef struct gbo_server_config {
     int32_t slots;                  /* launches in flight at once (1..8, 2) */
     int32_t max_batch_events;       /* events per launch (4096) */
-    int64_t max_batch_photon;       /* photons per launch (16M); also bounded by the budget; larger events are sliced */
+    int64_t max_batch_photon;       /* photons per launch (64M); also bounded by the budget; larger events are sliced */
     int64_t hbm_budget_bytes;       /* device memory the server's launches may hold (120 GB) */
     int64_t min_batch_photon;       /* while a launch is in flight, start another only once this many photons wait (2M) */
     int32_t use_graph;              /* 1: each batch's copies and kernels go out as one CUDA graph, captured from the
