@@ -30,7 +30,11 @@
 namespace gbo {
 
 #ifndef GBO_SIM_MINB
-#define GBO_SIM_MINB 1              // minimum resident blocks per SM asked of ptxas for the simulate kernels
+#define GBO_SIM_MINB 5              // minimum resident blocks per SM asked of ptxas for the one-thread simulate kernel
+                                    // (binary32, no CSG trees): 5 x 128 threads (96 registers) measured fastest
+#endif
+#ifndef GBO_SIM_MINB_WIDE
+#define GBO_SIM_MINB_WIDE 1         // the same for its CSG-tree and precision forms, which need their registers
 #endif
 #ifndef GBO_POOL_MINB
 #define GBO_POOL_MINB 4             // the same for the persistent photon-pool kernel: 4 x 128 threads per SM (128
@@ -86,7 +90,8 @@ GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng);
 // Kernel forms: TREE when any prim is a CSG tree; PRECISE for the precision mode (binary64 root polish in the
 // quadric leaves, binary64 position / time accumulators).  The default form compiles none of the latter.
 template <bool TREE, bool PRECISE>
-__global__ void __launch_bounds__(SIM_BLOCK, GBO_SIM_MINB) k_simulate(const __grid_constant__ Params P)
+__global__ void __launch_bounds__(SIM_BLOCK, (TREE || PRECISE) ? GBO_SIM_MINB_WIDE : GBO_SIM_MINB)
+k_simulate(const __grid_constant__ Params P)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = idx < P.num_photon;
