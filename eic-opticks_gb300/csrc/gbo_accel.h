@@ -4,11 +4,17 @@
 // (CSGOptiX/SBT.cc:247-495, GAS_Builder.cc, IAS_Builder.cc), then lets OptiX traverse them.  Here:
 //   * level 1 (TLAS): a binned-SAH BVH over the world-space AABBs of all instances, built on the host;
 //   * level 2: the prims of the instance's solid, each with an object-space AABB test before intersect_prim
-//     (solids in these geometries hold a handful of prims).
+//     (solids in these geometries hold a handful of prims);
+//   * per instance, the list of other instances whose padded world boxes meet its own (at most MAX_OVERLAP;
+//     instances made only of axis-aligned boxes that strictly contain it are left out, as their surfaces lie
+//     outside it), and for instances with longer lists a clear ball no other instance's box enters: the
+//     traversal uses them to skip the TLAS for steps that stay inside the photon's previous instance.
 // Device layouts (all 16-byte aligned, read as float4/int4):
 //   BvhNode  32 B : bmin.xyz, left-child-or-first-index ; bmax.xyz, count (0 for inner nodes)
 //   InstDev  64 B : inverse transform as three float4 columns + (solid, identity, is_identity, iindex)
 //   PrimDev  32 B : object AABB min.xyz + node offset ; AABB max.xyz + (globalPrimIdx<<16 | boundary)
+//   InstBox  32 B : world box min.xyz + overlap list start ; max.xyz + overlap count (-1: use the TLAS)
+//   clear    16 B : ball centre.xyz + radius^2 (0: none)
 #pragma once
 #include <cstdint>
 #include <vector>

@@ -10,8 +10,13 @@
 //     (optixTransformNormalFromObjectToWorldSpace); identity instances skip both transforms;
 //   * iindex|identity and globalPrimIdx|boundary packed in 16-bit halves (CSGOptiX7.cu:753, :929);
 //   * a miss returns boundary 0xffff (__miss__ms).
-// Traversal: the instance the photon last hit is intersected first (photons mostly stay inside one solid), then
-// the TLAS is walked front to back with nodes that carry both child boxes, pruning boxes beyond the current best.
+// Traversal: the instance the photon last hit (the hint) is intersected first, since photons mostly stay inside
+// one solid.  If that hit keeps the whole segment inside the hint's box, only the instances whose boxes overlap
+// that box can hold a closer hit, and their short precomputed list replaces the TLAS.  For a container whose list
+// is too long, a segment inside its clear ball (entered by no other instance's box) meets no other instance at all.
+// Otherwise the TLAS is walked front to back (while-while: descend inner nodes, then process leaves), with nodes
+// that carry both child boxes, pruning boxes beyond the current best.  Every path tests every instance that could
+// hold a hit at t <= the best, so the result is the same whichever path runs.
 #pragma once
 #include "gbo_csg.cuh"
 #include "gbo_physics.cuh"
