@@ -172,7 +172,20 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
             pad(b);
             PrimDev& pd = out.prim[pi];
             for (int j = 0; j < 3; j++) { pd.bmin[j] = (float)b.lo[j]; pd.bmax[j] = (float)b.hi[j]; }
-            pd.node_offset = noff;
+            if (noff >= (1 << 30)) {
+                std::snprintf(err, errlen, "prim %d node offset %d above 2^30", pi, noff);
+                return 1;
+            }
+            // pure union trees of plain leaves (no complement, no phicut / halfspace) take the union fast path
+            bool pure_union = nn > 1;
+            for (int k = 0; k < nn && pure_union; k++) {
+                const gbo_csgnode& nk = node[noff + k];
+                const unsigned tc = nk.q3.u[2];
+                if (tc == GBO_CSG_ZERO || tc == GBO_CSG_UNION) continue;
+                if (tc < GBO_CSG_LEAF || tc == GBO_CSG_PHICUT || tc == GBO_CSG_HALFSPACE || (nk.q3.u[3] & 0x80000000u))
+                    pure_union = false;
+            }
+            pd.node_offset = noff | (pure_union ? (1 << 30) : 0);
             const unsigned boundary = node[noff].q1.u[2];
             const unsigned gpi = pr.q3.u[3];
             pd.prim_boundary = ((gpi & 0xffffu) << 16) | (boundary & 0xffffu);

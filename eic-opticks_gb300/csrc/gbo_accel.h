@@ -12,7 +12,8 @@
 // Device layouts (all 16-byte aligned, read as float4/int4):
 //   BvhNode  32 B : bmin.xyz, left-child-or-first-index ; bmax.xyz, count (0 for inner nodes)
 //   InstDev  64 B : inverse transform as three float4 columns + (solid, identity, is_identity, iindex)
-//   PrimDev  32 B : object AABB min.xyz + node offset ; AABB max.xyz + (globalPrimIdx<<16 | boundary)
+//   PrimDev  32 B : object AABB min.xyz + node offset (bit 30: pure union tree) ; AABB max.xyz +
+//                   (globalPrimIdx<<16 | boundary)
 //   InstBox  32 B : world box min.xyz + overlap list start ; max.xyz + overlap count (-1: use the TLAS)
 //   clear    16 B : ball centre.xyz + radius^2 (0: none)
 #pragma once

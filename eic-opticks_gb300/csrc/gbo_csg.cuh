@@ -586,6 +586,37 @@ GBO_DEV bool intersect_tree(float4& isect, const gbo_csgnode* node, const float4
     return isect.w > 0.f;
 }
 
+// Union fast path for trees whose internal nodes are all unions and whose leaves are plain: evaluate every leaf
+// once at t_min, in postorder (left to right).  While every leaf's first hit enters it (the ray starts outside all
+// of them), Kensler's union table returns the nearest entering hit, the left one on a tie (ReturnAIfCloser with
+// leftIsCloser = tA <= tB), which is what the loop below keeps.  A leaf hit that exits (the ray starts inside that
+// leaf) needs the table's loop cases: the function then returns -1 and the caller runs intersect_tree.
+GBO_DEV int intersect_union_enter(float4& isect, const gbo_csgnode* node, const float4* plan, const gbo_qat4* itra,
+                                  float t_min, float3 ro, float3 rd, bool polish)
+{
+    const int numNode = (int)__ldg(&node->q0.u[0]);
+    const unsigned height = (unsigned)(__ffs(numNode + 1) - 2);
+    float4 best = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool found = false;
+    unsigned nodeIdx = 1u << height;
+    while (nodeIdx != 0u) {
+        const unsigned depth = 31u - (unsigned)__clz(nodeIdx);
+        const unsigned elevation = height - depth;
+        const gbo_csgnode* nd = node + nodeIdx - 1;
+        if (node_typecode(nd) >= GBO_CSG_LEAF) {
+            float4 is;
+            intersect_leaf(is, nd, plan, itra, t_min, ro, rd, polish);
+            if (fabsf(is.w) > t_min) {
+                if (!(is.x * rd.x + is.y * rd.y + is.z * rd.z < 0.f)) return -1;     // exits: full algorithm
+                if (!found || is.w < best.w) { best = is; found = true; }
+            }
+        }
+        nodeIdx = postorder_next(nodeIdx, elevation);
+    }
+    isect = best;
+    return found ? 1 : 0;
+}
+
 // csg_intersect_tree.h:683-719 (list nodes are not supported)
 GBO_DEV bool intersect_prim(float4& isect, const gbo_csgnode* node, const float4* plan, const gbo_qat4* itra,
                             float t_min, float3 o, float3 d, bool polish = false)

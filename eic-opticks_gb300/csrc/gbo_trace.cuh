@@ -118,10 +118,16 @@ GBO_DEV InstDev load_inst(const InstDev* p)
 
 // POLISH (precision mode): binary64 Newton polish of the quadric roots of sphere, zsphere and cylinder leaves
 template <bool TREE, bool POLISH>
-GBO_DEV bool prim_hit(float4& is, const Accel& a, int node_offset, float t_min, float3 o, float3 d)
+GBO_DEV bool prim_hit(float4& is, const Accel& a, int node_word, float t_min, float3 o, float3 d)
 {
-    const gbo_csgnode* root = a.node + node_offset;
-    if (TREE) return intersect_prim(is, root, a.plan, a.itra, t_min, o, d, POLISH);
+    const gbo_csgnode* root = a.node + (node_word & 0x3fffffff);
+    if (TREE) {
+        if (node_word & (1 << 30)) {                        // pure union tree: try the all-entering fast path
+            const int r = intersect_union_enter(is, root, a.plan, a.itra, t_min, o, d, POLISH);
+            if (r >= 0) return r == 1;
+        }
+        return intersect_prim(is, root, a.plan, a.itra, t_min, o, d, POLISH);
+    }
     if (node_typecode(root) >= GBO_CSG_LEAF) return intersect_leaf(is, root, a.plan, a.itra, t_min, o, d, POLISH);
     is = make_float4(0.f, 0.f, 0.f, 0.f);
     return false;
