@@ -38,9 +38,9 @@ def philox():
     save("philox.npz", cases=cases, uniforms=out)
 
 
-def csg():
-    rng = np.random.default_rng(7)
-    shapes = {
+def csg_shapes():
+    """The CSG shapes of csg.npz, each a prim to intersect in its own frame."""
+    return {
         "sphere": G.sphere(100), "zsphere": G.zsphere(100, -30, 60), "cylinder": G.cylinder(50, -80, 80),
         "cone": G.cone(80, -50, 20, 70), "box3": G.box3(50, 80, 120),
         "hyperboloid": G._node(L.CSG_HYPERBOLOID, (40, 60, -100, 100), bbox=(-100, -100, -100, 100, 100, 100)),
@@ -53,6 +53,11 @@ def csg():
                                                        G.with_transform(G.cylinder(127, -100, 100), G.translate(0, 0, -184))),
                               G.with_transform(G.cylinder(50, -30, 30), G.translate(0, 0, -313))),
     }
+
+
+def csg():
+    rng = np.random.default_rng(7)
+    shapes = csg_shapes()
     out = {}
     n = 2000
     for name, nd in shapes.items():
