@@ -7,7 +7,8 @@
 //
 //   k_merge_keys      key and input index per hit, OR of all keys (to skip radix passes over all-zero bytes)
 //   k_radix_hist      per-tile histogram of one key byte (256 bins in shared memory), digit-major layout
-//   k_scan_exclusive  one-block exclusive scan of the digit x tile counts (or of the run-head flags)
+//   k_scan_*          exclusive scan of the digit x tile counts (or of the run-head flags): tile sums, one-block
+//                     scan of the tile sums, per-tile scan
 //   k_radix_scatter   stable scatter: each warp owns a contiguous sub-tile, ranks equal digits with
 //                     __match_any_sync and a per-warp running offset, so input order survives every pass
 //   k_run_heads       1 where a key differs from its predecessor
@@ -67,13 +68,41 @@ __global__ void k_radix_hist(const uint64_t* keys, long long n, int shift, int n
     for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(size_t)d * ntiles + blockIdx.x] = h[d];
 }
 
-// exclusive scan of n uint32 in place by one block: each thread scans a contiguous chunk; total in *total
-__global__ void k_scan_exclusive(uint32_t* v, long long n, unsigned long long* total)
+// Exclusive scan of n uint32 in place, in three launches: k_scan_tiles sums each SCAN_TILE-word tile, k_scan_partials
+// scans the tile sums in one block (and writes the total), k_scan_down scans each tile from its tile's offset.  Each
+// warp owns SCAN_WARP_TILE consecutive words and reads them 32 at a time (coalesced), carrying its running sum.
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_WARP_TILE = 32 * SCAN_ITEMS;
+constexpr int SCAN_TILE = MB_WARPS * SCAN_WARP_TILE;
+
+__global__ void __launch_bounds__(MB_THREADS) k_scan_tiles(const uint32_t* v, long long n, uint32_t* partial)
+{
+    __shared__ uint32_t wsum[MB_WARPS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)warp * SCAN_WARP_TILE;
+    uint32_t s = 0u;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const long long i = base + k * 32 + lane;
+        s += i < n ? v[i] : 0u;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) wsum[warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0u;
+        for (int w = 0; w < MB_WARPS; w++) t += wsum[w];
+        partial[blockIdx.x] = t;
+    }
+}
+
+// one block: exclusive scan of the m tile sums in place, each thread over a contiguous chunk; total in *total
+__global__ void k_scan_partials(uint32_t* v, long long m, unsigned long long* total)
 {
     __shared__ unsigned long long part[SCAN_THREADS];
-    const long long per = (n + SCAN_THREADS - 1) / SCAN_THREADS;
+    const long long per = (m + SCAN_THREADS - 1) / SCAN_THREADS;
     const long long lo = (long long)threadIdx.x * per;
-    const long long hi = lo + per < n ? lo + per : n;
+    const long long hi = lo + per < m ? lo + per : m;
     unsigned long long s = 0ull;
     for (long long i = lo; i < hi; i++) s += v[i];
     part[threadIdx.x] = s;
@@ -91,6 +120,46 @@ __global__ void k_scan_exclusive(uint32_t* v, long long n, unsigned long long* t
         run += x;
     }
     if (threadIdx.x == SCAN_THREADS - 1 && total) *total = part[SCAN_THREADS - 1];
+}
+
+__global__ void __launch_bounds__(MB_THREADS) k_scan_down(uint32_t* v, long long n, const uint32_t* partial)
+{
+    __shared__ uint32_t wsum[MB_WARPS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)warp * SCAN_WARP_TILE;
+    uint32_t x[SCAN_ITEMS];
+    uint32_t s = 0u;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const long long i = base + k * 32 + lane;
+        x[k] = i < n ? v[i] : 0u;
+        s += x[k];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) wsum[warp] = s;
+    __syncthreads();
+    uint32_t run = partial[blockIdx.x];
+    for (int w = 0; w < warp; w++) run += wsum[w];
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        uint32_t inc = x[k];                                    // inclusive scan of this row of 32 words
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        const long long i = base + k * 32 + lane;
+        if (i < n) v[i] = run + inc - x[k];
+        run += __shfl_sync(0xffffffffu, inc, 31);
+    }
+}
+
+// exclusive scan of v[0..n) in place; scratch holds ceil(n / SCAN_TILE) words; the total (if wanted) lands in *total
+static void scan_exclusive(uint32_t* v, long long n, uint32_t* scratch, unsigned long long* total, cudaStream_t s)
+{
+    const long long tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    k_scan_tiles<<<(unsigned)tiles, MB_THREADS, 0, s>>>(v, n, scratch);
+    k_scan_partials<<<1, SCAN_THREADS, 0, s>>>(scratch, tiles, total);
+    k_scan_down<<<(unsigned)tiles, MB_THREADS, 0, s>>>(v, n, scratch);
 }
 
 __global__ void __launch_bounds__(MB_THREADS) k_radix_scatter(const uint64_t* keys, const uint32_t* idx, long long n,
@@ -160,15 +229,31 @@ __global__ void k_run_starts(const uint64_t* keys, long long n, const uint32_t* 
         if (i == 0 || keys[i] != keys[i - 1]) start[run_index[i]] = (uint32_t)i;
 }
 
+// one hit as four 16-byte loads when the array is 16-byte aligned (cudaMalloc'd hit buffers are)
+template <bool A16>
+__device__ __forceinline__ gbo_sphoton load_hit(const gbo_sphoton* p)
+{
+    if (A16) {
+        gbo_sphoton h;
+        const uint4* q = reinterpret_cast<const uint4*>(p);
+        uint4* o = reinterpret_cast<uint4*>(&h);
+#pragma unroll
+        for (int k = 0; k < 4; k++) o[k] = __ldg(q + k);
+        return h;
+    }
+    return *p;
+}
+
+template <bool A16>
 __global__ void k_run_reduce(const gbo_sphoton* in, const uint32_t* order, const uint32_t* start, long long runs,
                              long long n, gbo_sphoton* out)
 {
     for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < runs; r += (long long)gridDim.x * blockDim.x) {
         const long long b = start[r];
         const long long e = r + 1 < runs ? (long long)start[r + 1] : n;
-        gbo_sphoton acc = in[order[b]];
+        gbo_sphoton acc = load_hit<A16>(in + order[b]);
         for (long long j = b + 1; j < e; j++) {
-            const gbo_sphoton x = in[order[j]];
+            const gbo_sphoton x = load_hit<A16>(in + order[j]);
             const bool a_first = fminf(acc.time, x.time) == acc.time;
             const unsigned fm = acc.flagmask | x.flagmask;
             const unsigned hc = ((acc.hitcount_iindex >> 16) + (x.hitcount_iindex >> 16)) & 0xffffu;
@@ -176,7 +261,14 @@ __global__ void k_run_reduce(const gbo_sphoton* in, const uint32_t* order, const
             acc.flagmask = fm;
             acc.hitcount_iindex = (acc.hitcount_iindex & 0x0000ffffu) | (hc << 16);
         }
-        out[r] = acc;
+        if (A16) {
+            const uint4* q = reinterpret_cast<const uint4*>(&acc);
+            uint4* o = reinterpret_cast<uint4*>(out + r);
+#pragma unroll
+            for (int k = 0; k < 4; k++) o[k] = q[k];
+        } else {
+            out[r] = acc;
+        }
     }
 }
 
@@ -203,7 +295,7 @@ extern "C" int gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float t
     int rc = GBO_OK;
     const int ntiles = (int)((n + MB_TILE - 1) / MB_TILE);
     uint64_t *k0 = nullptr, *k1 = nullptr;
-    uint32_t *i0 = nullptr, *i1 = nullptr, *hist = nullptr;
+    uint32_t *i0 = nullptr, *i1 = nullptr, *hist = nullptr, *scan_tmp = nullptr;
     unsigned long long* scal = nullptr;                         // [0] key OR, [1] scan total
     unsigned long long h_scal[2] = {0ull, 0ull};
     const int grid = (int)((n + MB_THREADS - 1) / MB_THREADS < 4096 ? (n + MB_THREADS - 1) / MB_THREADS : 4096);
@@ -213,6 +305,7 @@ extern "C" int gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float t
     MCU(cudaMallocAsync((void**)&i1, (size_t)n * 4, s));
     MCU(cudaMallocAsync((void**)&hist, (size_t)256 * ntiles * 4 > (size_t)n * 4 ? (size_t)256 * ntiles * 4 : (size_t)n * 4, s));
     MCU(cudaMallocAsync((void**)&scal, 2 * sizeof(unsigned long long), s));
+    MCU(cudaMallocAsync((void**)&scan_tmp, (size_t)((n > 256ll * ntiles ? n : 256ll * ntiles) / SCAN_TILE + 1) * 4, s));
     MCU(cudaMemsetAsync(scal, 0, 2 * sizeof(unsigned long long), s));
     k_merge_keys<<<grid, MB_THREADS, 0, s>>>(d_in, n, time_window, k0, i0, scal);
     MCU(cudaGetLastError());
@@ -221,7 +314,7 @@ extern "C" int gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float t
     for (int byte = 0; byte < 8; byte++) {
         if (((h_scal[0] >> (8 * byte)) & 0xffull) == 0ull) continue;       // every key has a zero byte here
         k_radix_hist<<<ntiles, MB_THREADS, 0, s>>>(k0, n, 8 * byte, ntiles, hist);
-        k_scan_exclusive<<<1, SCAN_THREADS, 0, s>>>(hist, (long long)256 * ntiles, nullptr);
+        scan_exclusive(hist, (long long)256 * ntiles, scan_tmp, nullptr, s);
         k_radix_scatter<<<ntiles, MB_THREADS, 0, s>>>(k0, i0, n, 8 * byte, ntiles, hist, k1, i1);
         MCU(cudaGetLastError());
         uint64_t* tk = k0; k0 = k1; k1 = tk;
@@ -231,7 +324,7 @@ extern "C" int gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float t
         // runs of equal keys: heads -> exclusive scan (run index of each head) -> run starts -> fold
         uint32_t* head = hist;                                  // n words (hist was sized for max(n, 256 ntiles))
         k_run_heads<<<grid, MB_THREADS, 0, s>>>(k0, n, head);
-        k_scan_exclusive<<<1, SCAN_THREADS, 0, s>>>(head, n, scal + 1);
+        scan_exclusive(head, n, scan_tmp, scal + 1, s);
         MCU(cudaGetLastError());
         MCU(cudaMemcpyAsync(h_scal + 1, scal + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         MCU(cudaStreamSynchronize(s));
@@ -239,13 +332,16 @@ extern "C" int gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float t
         uint32_t* start = i1;                                   // free after the last pass
         k_run_starts<<<grid, MB_THREADS, 0, s>>>(k0, n, head, start);
         const int rgrid = (int)((runs + MB_THREADS - 1) / MB_THREADS < 4096 ? (runs + MB_THREADS - 1) / MB_THREADS : 4096);
-        k_run_reduce<<<rgrid > 0 ? rgrid : 1, MB_THREADS, 0, s>>>(d_in, i0, start, runs, n, d_out);
+        if ((((uintptr_t)d_in | (uintptr_t)d_out) & 15u) == 0u)
+            k_run_reduce<true><<<rgrid > 0 ? rgrid : 1, MB_THREADS, 0, s>>>(d_in, i0, start, runs, n, d_out);
+        else
+            k_run_reduce<false><<<rgrid > 0 ? rgrid : 1, MB_THREADS, 0, s>>>(d_in, i0, start, runs, n, d_out);
         MCU(cudaGetLastError());
         MCU(cudaStreamSynchronize(s));
         *num_out = runs;
     }
 done:
-    void* bufs[6] = {k0, k1, i0, i1, hist, scal};
+    void* bufs[7] = {k0, k1, i0, i1, hist, scal, scan_tmp};
     for (void* b : bufs)
         if (b) cudaFreeAsync(b, s);
     if (cudaStreamSynchronize(s) != cudaSuccess && rc == GBO_OK) rc = GBO_ERR_CUDA;

@@ -96,3 +96,23 @@ def test_device_merge_matches_oracle(E, oracle, n, num_ids, t_max):
     got = d_out.cpu().numpy()[: m.value * h.dtype.itemsize].view(h.dtype)
     want = oracle.merge_hits(h, 1.0)
     assert len(got) == len(want) and np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_device_merge_unaligned_buffers(E, oracle):
+    """Hit arrays that start 4 bytes past a 16-byte boundary take the 4-byte load path of the run fold."""
+    import ctypes as C
+    import torch
+    n = 50000
+    h = synthetic_hits(n, 900, 60.0, seed=5)
+    lib = E.load()
+    raw_in = torch.zeros(h.nbytes + 16, dtype=torch.uint8, device="cuda")
+    raw_in[4: 4 + h.nbytes] = torch.from_numpy(h.view(np.uint8).copy()).cuda()
+    raw_out = torch.zeros_like(raw_in)
+    m = C.c_int64()
+    rc = lib.gbo_merge_hits_device(C.c_void_p(raw_in.data_ptr() + 4), n, C.c_float(1.0),
+                                   C.c_void_p(raw_out.data_ptr() + 4), C.byref(m), None)
+    assert rc == 0
+    got = raw_out.cpu().numpy()[4: 4 + m.value * h.dtype.itemsize].view(h.dtype)
+    want = oracle.merge_hits(h, 1.0)
+    assert len(got) == len(want) and np.array_equal(got.view(np.uint32), want.view(np.uint32))
