@@ -39,8 +39,13 @@ L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) per photon of the simulate kernel from one ncu capture of a 998,319-photon crystal-array
 # event (200 gensteps), scaled to the benchmark event by its photon count: gensteps in, hits and hit bitmap out,
 # the only DRAM traffic, all grow with the photons
-TRAFFIC_B_PER_PHOTON = {"crystal_array": (443392.0 + 840192.0) / 998319}
-TRAFFIC_SOURCE = "profiles/k_simulate_crystal_array.md (ncu, 1M-photon event, scaled by photons)"
+# ncu DRAM bytes (read + write) per photon of the simulate kernels on the crystal event, scaled by photons:
+# one thread per photon (k_simulate, 1M-photon event), and the pregenerated pool (k_generate + k_simulate_pool,
+# 2.5M-photon event: 182.1 + 0.2 MB and 210.9 + 2.5 MB, larger than L2)
+TRAFFIC_B_PER_PHOTON = {("crystal_array", 1): (443392.0 + 840192.0) / 998319,
+                        ("crystal_array", 2): (182.1e6 + 0.2e6 + 210.9e6 + 2.5e6) / 2499792}
+TRAFFIC_SOURCE = {1: "profiles/k_simulate_crystal_array.md (ncu, 1M-photon event, scaled by photons)",
+                  2: "profiles/k_simulate_pool_pregen_crystal_array.md (ncu, 2.5M-photon event, scaled by photons)"}
 
 
 def peaks():
@@ -53,7 +58,7 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms during the timed region."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -69,7 +74,7 @@ class ClockSampler:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -106,6 +111,9 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
 
+
+KERNEL_MODES = {0: "photon pool", 1: "one thread per photon", 2: "photon pool over pregenerated photons"}
+KERNEL_NAMES = {0: "k_simulate_pool", 1: "k_simulate", 2: "k_generate + k_simulate_pool"}
 
 WORKLOADS = {
     "nested_boxes": "nested_boxes_torch_100k_input_photons",
@@ -258,7 +266,7 @@ def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
         sample = (GS.crystal_scint_gensteps(200, 5000, seed=99) if kind == "crystal" else
                   GS.water_cerenkov_gensteps(G.water_cube(), 2000, seed=99))
         r = eng.autotune(0, sample, trials=2)
-        tuned[kind] = {"mode": "photon pool" if r["kernel_mode"] == 0 else "one thread per photon",
+        tuned[kind] = {"mode": KERNEL_MODES[r["kernel_mode"]],
                        "refill_min": r["refill_min"], "refill_period": r["refill_period"]}
     photons = {id(ev[2]): int(ev[2].view(np.uint32)[:, 0, 3].astype(np.int64).sum()) for ev in events}
     total_photons = sum(photons.values())
@@ -425,7 +433,8 @@ def main():
                     help="gensteps per event (default: the workload's own, 2000 for the crystal array)")
     ap.add_argument("--workload", default="crystal_array", choices=sorted(WORKLOADS))
     ap.add_argument("--form", default=None,
-                    help="kernel form MODE,REFILL,PERIOD instead of the autotuner's choice (MODE 0: photon pool)")
+                    help="kernel form MODE,REFILL,PERIOD instead of the autotuner's choice (MODE 0: photon pool, "
+                         "1: one thread per photon, 2: photon pool over pregenerated photons)")
     ap.add_argument("--batch-events", type=int, default=None,
                     help="events of the workload for the same-configuration plain vs batched comparison")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
@@ -477,7 +486,7 @@ def main():
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ms, sim_ms, launches, hits = [], [], 0, 0
+    ms, sim_ms, gen_ms, launches, hits = [], [], [], 0, 0
     with ClockSampler(local) as clk:
         for k in range(args.steps):
             flush.zero_()
@@ -489,6 +498,7 @@ def main():
             ms.append(start.elapsed_time(end))
             st = eng.stats()
             sim_ms.append(st["ms_simulate"])
+            gen_ms.append(st["ms_generate"])
             launches += st["kernel_launches"]
     torch.cuda.synchronize()
     total_ms = sum(ms)
@@ -530,6 +540,7 @@ def main():
     f_hit = hits / n_photon
     b_alg = 96.0 / (n_photon / len(gs)) + 4 + 64 + 64 + 64 * f_hit + (64.0 if inp is not None else 0.0)
     sim_mean = float(np.mean(sim_ms))
+    traffic_key = (args.workload, tune["kernel_mode"])
     achieved = b_alg * n_photon / (sim_mean * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -541,19 +552,20 @@ def main():
                    "precision": "binary64 root polish + accumulators" if args.precision else "binary32",
                    "photons_per_step": n_photon, "gensteps_per_step": len(gs),
                    "hits_per_step": hits, "path": "plain: one event per launch", "l2": "flushed (256 MB write) between timed steps",
-                   "kernel": {"mode": "photon pool" if tune["kernel_mode"] == 0 else "one thread per photon",
+                   "kernel": {"mode": KERNEL_MODES[tune["kernel_mode"]],
                               "refill_min": tune["refill_min"], "refill_period": tune["refill_period"],
                               "chosen_by": "--form" if args.form else "autotuner on 10% sample"},
                    "max_bounce": 31, "parallelism": "replicas" if world > 1 else "1 GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": (TRAFFIC_B_PER_PHOTON[args.workload] * n_photon
-                                 if args.workload in TRAFFIC_B_PER_PHOTON and not args.precision else None),
-                     "traffic_source": TRAFFIC_SOURCE if args.workload in TRAFFIC_B_PER_PHOTON else None,
-                     "kernel": "k_simulate_pool" if tune["kernel_mode"] == 0 else "k_simulate",
+                     "traffic": (TRAFFIC_B_PER_PHOTON[traffic_key] * n_photon
+                                 if traffic_key in TRAFFIC_B_PER_PHOTON and not args.precision else None),
+                     "traffic_source": (TRAFFIC_SOURCE[tune["kernel_mode"]]
+                                        if traffic_key in TRAFFIC_B_PER_PHOTON and not args.precision else None),
+                     "kernel": KERNEL_NAMES[tune["kernel_mode"]],
                      "bytes_per_photon": b_alg,
-                     "kernel_ms": sim_mean, "peak_source": peak_kind},
+                     "kernel_ms": sim_mean, "generate_ms": float(np.mean(gen_ms)), "peak_source": peak_kind},
         "clocks": clk.summary(),
     }
     if not args.no_serving and world == 1:

@@ -230,11 +230,11 @@ GBO_DEV bool leaf_cylinder(float4& is, float4 q0, float2 q1, float t_min, float3
 }
 
 // csg_intersect_leaf_box3.h:63-155
-GBO_DEV bool leaf_box3(float4& is, float4 q0, float t_min, float3 ro, float3 rd)
+// idir = (1/rd.x, 1/rd.y, 1/rd.z), correctly rounded; the caller may pass the reciprocals it already holds
+GBO_DEV bool leaf_box3(float4& is, float4 q0, float t_min, float3 ro, float3 rd, float3 idir)
 {
     const float3 bmin = f3(-q0.x / 2.f, -q0.y / 2.f, -q0.z / 2.f);
     const float3 bmax = f3(q0.x / 2.f, q0.y / 2.f, q0.z / 2.f);
-    const float3 idir = f3(1.f / rd.x, 1.f / rd.y, 1.f / rd.z);
     const float3 t0 = (bmin - ro) * idir;
     const float3 t1 = (bmax - ro) * idir;
     const float3 nr = fminf3(t0, t1);
@@ -430,8 +430,9 @@ GBO_COLD bool leaf_phicut(float4& is, float4 q0, float t_min, float3 o, float3 d
 }
 
 // csg_intersect_leaf.h:174-325
+// rd_inv (optional): the correctly rounded reciprocals of rd's components, reused by an untransformed box3
 GBO_DEV bool intersect_leaf(float4& is, const gbo_csgnode* node, const float4* plan, const gbo_qat4* itra,
-                            float t_min, float3 ro, float3 rd, bool polish = false)
+                            float t_min, float3 ro, float3 rd, bool polish = false, const float3* rd_inv = nullptr)
 {
     is = make_float4(0.f, 0.f, 0.f, 0.f);
     const NodeView nd = load_node(node);
@@ -449,7 +450,11 @@ GBO_DEV bool intersect_leaf(float4& is, const gbo_csgnode* node, const float4* p
         case GBO_CSG_SPHERE:           valid = leaf_sphere(is, nd.q0, t_min, origin, direction, polish); break;
         case GBO_CSG_ZSPHERE:          valid = leaf_zsphere(is, nd.q0, nd.q1, t_min, origin, direction, polish); break;
         case GBO_CSG_CYLINDER:         valid = leaf_cylinder(is, nd.q0, nd.q1, t_min, origin, direction, polish); break;
-        case GBO_CSG_BOX3:             valid = leaf_box3(is, nd.q0, t_min, origin, direction); break;
+        case GBO_CSG_BOX3:
+            valid = leaf_box3(is, nd.q0, t_min, origin, direction,
+                              gt == 0 && rd_inv ? *rd_inv
+                                                : f3(1.f / direction.x, 1.f / direction.y, 1.f / direction.z));
+            break;
         case GBO_CSG_CONE:             valid = leaf_cone(is, nd.q0, t_min, origin, direction); break;
         case GBO_CSG_CONVEXPOLYHEDRON: valid = leaf_convexpolyhedron(is, nd.q0, plan, t_min, origin, direction); break;
         case GBO_CSG_HYPERBOLOID:      valid = leaf_hyperboloid(is, nd.q0, t_min, origin, direction); break;

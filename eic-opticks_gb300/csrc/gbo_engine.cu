@@ -83,9 +83,16 @@ struct Params {
     const unsigned long long* ev_photon_offset;     // event-local index of each entry's first photon (a piece of a
                                                     // sliced event starts past 0); nullptr: all 0
     unsigned long long* hit_gidx;           // launch index of each unordered hit (batched launches)
+    // pregenerated photons (kernel mode 2): k_generate writes each photon as generated and its random-stream
+    // place (draws consumed, subsequence); the pool kernel's refills read them instead of generating
+    gbo_sphoton* gen_photon;
+    ulonglong2* gen_rng;
+    int* gen_hint;
+    // start instance of each genstep's photons (k_genstep_hint), a traversal hint only; nullptr: none
+    const int* gs_hint;
 };
 
-GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng);
+GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng, int& hint);
 
 // Kernel forms: TREE when any prim is a CSG tree; PRECISE for the precision mode (binary64 root polish in the
 // quadric leaves, binary64 position / time accumulators).  The default form compiles none of the latter.
@@ -100,13 +107,13 @@ k_simulate(const __grid_constant__ Params P)
     if (active) {
         Rng rng;
         Acc64 acc;
-        generate(P, idx, p, rng);
+        int hint;
+        generate(P, idx, p, rng, hint);
         if (PRECISE) acc_init(acc, p);
 
         Seq seq;
         seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
         int bounce = 0;
-        int hint = -1;
         if (P.seq_out) seq_add(seq, 0u, flag_of(p), boundary_of(p));
         while (bounce < P.max_bounce && p.time < P.max_time) {
             const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
@@ -145,13 +152,15 @@ k_simulate(const __grid_constant__ Params P)
 
 // ---- persistent form: lanes refill from a photon pool so a warp never idles behind its longest photon --------
 
-GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng)
+// `hint` receives the start instance found for the photon's genstep (-1 when none was computed)
+GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng, int& hint)
 {
     int lo = 0, hi = P.num_gs - 1;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         if (__ldg(P.gs_end + mid) > (unsigned long long)idx) hi = mid; else lo = mid + 1;
     }
+    hint = P.gs_hint ? __ldg(P.gs_hint + lo) : -1;
     const float4* g = P.gs + 6 * (size_t)lo;
     float4 gq[6];
 #pragma unroll
@@ -185,6 +194,22 @@ GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng)
     set_index(p, photon_idx);
 }
 
+constexpr int POOL_CHUNK = 32;      // pregenerated photons a warp claims at once (kernel mode 2)
+
+// every photon of the launch generated up front, converged, so that the pool kernel's refills are plain loads
+__global__ void __launch_bounds__(SIM_BLOCK) k_generate(const __grid_constant__ Params P)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= P.num_photon) return;
+    Photon p;
+    Rng rng;
+    int hint;
+    generate(P, idx, p, rng, hint);
+    store_photon(P.gen_photon + idx, p);
+    P.gen_rng[idx] = make_ulonglong2(rng.pos, ((unsigned long long)rng.sub_hi << 32) | rng.sub_lo);
+    P.gen_hint[idx] = hint;
+}
+
 template <bool TREE, bool PRECISE>
 __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P,
                                                              unsigned long long* pool, int refill_min, int period)
@@ -201,11 +226,50 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
     Rng rng;
     Acc64 acc;
     Seq seq;
+    // mode 2 (warp-uniform): the warp's claimed chunk of pregenerated photons [cbase, cbase + cn), cused taken
+    long long cbase = 0;
+    int cn = 0, cused = 0;
     for (;; it++) {
-        // refill every `period` steps (or when the warp is empty): idle lanes take consecutive photon indices
-        // with one atomic per warp
+        // refill every `period` steps (or when the warp is empty): idle lanes take the next photon indices in lane
+        // order; mode 2 claims them POOL_CHUNK at a time (one atomic per chunk) and loads them as generated, the
+        // other pool mode claims exactly the idle lanes' count and generates them
         const unsigned idle = __ballot_sync(0xffffffffu, !live);
-        if (pool_open && (idle == 0xffffffffu || (it % period == 0 && __popc(idle) >= refill_min))) {
+        const bool refill = pool_open && (idle == 0xffffffffu || (it % period == 0 && __popc(idle) >= refill_min));
+        if (refill && P.gen_photon) {
+            const int n_idle = __popc(idle), rank = __popc(idle & lt), avail = cn - cused;
+            long long nb = 0;
+            int nn = 0;
+            if (avail < n_idle) {
+                unsigned long long b = 0;
+                if (lane == 0) b = atomicAdd(pool, (unsigned long long)POOL_CHUNK);
+                nb = (long long)__shfl_sync(0xffffffffu, b, 0);
+                const long long left = P.num_photon - nb;
+                nn = left <= 0 ? 0 : (left < POOL_CHUNK ? (int)left : POOL_CHUNK);
+            }
+            if (!live) {
+                const long long j = rank < avail ? cbase + cused + rank : (rank - avail < nn ? nb + (rank - avail) : -1);
+                if (j >= 0) {
+                    idx = j;
+                    load_photon(p, P.gen_photon + idx);
+                    const ulonglong2 r = P.gen_rng[idx];
+                    rng_init(rng, P.seed, r.y, r.x);
+                    hint = P.gen_hint[idx];
+                    if (PRECISE) acc_init(acc, p);
+                    bounce = 0;
+                    seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
+                    if (P.seq_out) seq_add(seq, 0u, flag_of(p), boundary_of(p));
+                    live = true;
+                }
+            }
+            if (avail < n_idle) {
+                cbase = nb;
+                cn = nn;
+                cused = n_idle - avail < nn ? n_idle - avail : nn;
+                if (nn == 0) pool_open = false;         // drained: every claimed photon has been handed out
+            } else {
+                cused += n_idle;
+            }
+        } else if (refill) {
             unsigned long long base = 0;
             const int leader = __ffs(idle) - 1;
             if ((int)lane == leader) base = atomicAdd(pool, (unsigned long long)__popc(idle));
@@ -215,10 +279,9 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
                 const unsigned long long mine = base + __popc(idle & lt);
                 if (mine < (unsigned long long)P.num_photon) {
                     idx = (long long)mine;
-                    generate(P, idx, p, rng);
+                    generate(P, idx, p, rng, hint);
                     if (PRECISE) acc_init(acc, p);
                     bounce = 0;
-                    hint = -1;
                     seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
                     if (P.seq_out) seq_add(seq, 0u, flag_of(p), boundary_of(p));
                     live = true;
@@ -274,6 +337,47 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
             }
         }
     }
+}
+
+// Start instance of each genstep's photons: of the instances whose padded world box holds the genstep position
+// (q1.xyz for every genstep type), the one with the smallest box, found by a point walk of the TLAS.  Only a
+// traversal hint: trace finds the same closest hit with any hint or none, faster when the hint is right (the
+// first step of a photon then skips the TLAS walk like every later step).
+__global__ void k_genstep_hint(Accel a, const float4* gs, int num_gs, int* hint)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= num_gs) return;
+    const float4 q1 = __ldg(gs + 6 * (size_t)g + 1);
+    const float x = q1.x, y = q1.y, z = q1.z;
+    int best = -1;
+    float best_vol = INFINITY;
+    int stack[TRAVERSAL_STACK];
+    int sp = 0;
+    int node = 0;
+    for (;;) {
+        const float4* nq = reinterpret_cast<const float4*>(a.tlas + node);
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            const float4 lo = __ldg(nq + 2 * c), hi = __ldg(nq + 2 * c + 1);
+            const int count = __float_as_int(hi.w);
+            if (count < 0 || !(x >= lo.x && x <= hi.x && y >= lo.y && y <= hi.y && z >= lo.z && z <= hi.z)) continue;
+            if (count == 0) {
+                if (sp < TRAVERSAL_STACK) stack[sp++] = __float_as_int(lo.w);
+                continue;
+            }
+            const int first = __float_as_int(lo.w);
+            for (int k = 0; k < count; k++) {
+                const int ii = __ldg(a.tlas_index + first + k);
+                const float4 blo = __ldg(a.inst_box + 2 * ii), bhi = __ldg(a.inst_box + 2 * ii + 1);
+                if (!(x >= blo.x && x <= bhi.x && y >= blo.y && y <= bhi.y && z >= blo.z && z <= bhi.z)) continue;
+                const float vol = (bhi.x - blo.x) * (bhi.y - blo.y) * (bhi.z - blo.z);
+                if (vol < best_vol || (vol == best_vol && ii < best)) { best_vol = vol; best = ii; }
+            }
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    hint[g] = best;
 }
 
 __global__ void k_genstep_prefix(const gbo_quad6* gs, int num_gs, unsigned long long* gs_end)
@@ -557,21 +661,31 @@ struct gbo_engine {
     DBuf<gbo_sphoton> hits_unordered;
     DBuf<gbo_sphoton> hits;
     DBuf<gbo_sphoton> merged;               // hits merged by (identity, time bucket), gbo_merge_hits
+    DBuf<gbo_sphoton> gen_photon;           // kernel mode 2: pregenerated photons, their random-stream places and
+    DBuf<ulonglong2> gen_rng;               // start instances
+    DBuf<int> gen_hint;
+    DBuf<int> gs_hint;                      // start instance per genstep
     long long num_merged = -1;
     DBuf<uint32_t> bitmap, word_prefix, block_sum;
     DBuf<unsigned long long> block_offset;
     DBuf<unsigned long long> counters;      // [0] unordered hit count, [1] total hits, [2] photons
     unsigned long long* host_counters = nullptr;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // upload, simulate, compact, end; [4]
+                                                                        // after the generation kernel (mode 2)
     long long num_photon = -1, num_hit = 0;
     int32_t event_id = -1;
     gbo_stats stats{};
 };
 
 template <bool TREE, bool PRECISE>
-static void launch_form(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s)
+static void launch_form(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s,
+                        cudaEvent_t after_gen)
 {
-    if (e->cfg.kernel_mode == 0) {
+    if (e->cfg.kernel_mode != 1) {
+        if (P.gen_photon && n > 0) {
+            k_generate<<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
+            if (after_gen) cudaEventRecord(after_gen, s);
+        }
         const int form = (TREE ? 1 : 0) | (PRECISE ? 2 : 0);
         const long long need = (n + SIM_BLOCK - 1) / SIM_BLOCK;
         const long long grid = need < e->pool_grid[form] ? need : e->pool_grid[form];
@@ -584,14 +698,19 @@ static void launch_form(const gbo_engine* e, const Params& P, long long n, unsig
 }
 
 // One launch of the simulation kernel over n photons in the engine's kernel form (pool or one thread per photon,
-// CSG trees or not, precision mode or not); `pool` is the photon-pool counter, zeroed by the caller.
-static void launch_simulate(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s)
+// CSG trees or not, precision mode or not); `pool` is the photon-pool counter, zeroed by the caller.  With
+// P.gen_photon set (kernel mode 2) the generation kernel runs first and the pool kernel reads its photons;
+// `after_gen` (optional) is recorded between the two.
+static void launch_simulate(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s,
+                            cudaEvent_t after_gen = nullptr)
 {
     const bool precise = e->cfg.precision != 0;
     if (e->has_tree) {
-        if (precise) launch_form<true, true>(e, P, n, pool, s); else launch_form<true, false>(e, P, n, pool, s);
+        if (precise) launch_form<true, true>(e, P, n, pool, s, after_gen);
+        else launch_form<true, false>(e, P, n, pool, s, after_gen);
     } else {
-        if (precise) launch_form<false, true>(e, P, n, pool, s); else launch_form<false, false>(e, P, n, pool, s);
+        if (precise) launch_form<false, true>(e, P, n, pool, s, after_gen);
+        else launch_form<false, false>(e, P, n, pool, s, after_gen);
     }
 }
 
@@ -617,8 +736,8 @@ int gbo_config_default(gbo_config* c)
     c->record_photon = 0;
     c->record_seq = 0;
     c->max_photon = 0;
-    c->kernel_mode = 0;
-    c->refill_min = 8;
+    c->kernel_mode = 2;
+    c->refill_min = 4;
     c->blocks_per_sm = 0;
     c->refill_period = 1;
     c->max_slot = 0;
@@ -673,7 +792,7 @@ void gbo_engine_destroy(gbo_engine* e)
     e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->inst_box.release(); e->overlap.release(); e->clear.release(); e->prim.release(); e->solid.release();
     e->node.release(); e->plan.release(); e->itra.release(); e->optical.release();
     e->gs.release(); e->gs_end.release(); e->input.release(); e->photon.release(); e->seq.release();
-    e->hits_unordered.release(); e->hits.release(); e->merged.release(); e->bitmap.release(); e->word_prefix.release();
+    e->hits_unordered.release(); e->hits.release(); e->merged.release(); e->gen_photon.release(); e->gen_rng.release(); e->gen_hint.release(); e->gs_hint.release(); e->bitmap.release(); e->word_prefix.release();
     e->block_sum.release(); e->block_offset.release(); e->counters.release();
     if (e->host_counters) cudaFreeHost(e->host_counters);
     for (auto& v : e->ev) if (v) cudaEventDestroy(v);
@@ -846,6 +965,12 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     if (keep_photon) { if (at.photon_base == 0 && (rc = e->photon.ensure(at.capacity))) return rc; }
     else { if ((rc = e->hits_unordered.ensure(num_photon))) return rc; }
     if (keep_seq && at.photon_base == 0) { if ((rc = e->seq.ensure(at.capacity))) return rc; }
+    if (e->cfg.kernel_mode == 2) {
+        if ((rc = e->gen_photon.ensure(num_photon))) return rc;
+        if ((rc = e->gen_rng.ensure(num_photon))) return rc;
+        if ((rc = e->gen_hint.ensure(num_photon))) return rc;
+    }
+    if (num_gs > 0 && (rc = e->gs_hint.ensure(num_gs))) return rc;
 
     Params P = make_params(e);
     const uint64_t skip = e->cfg.event_skipahead * (uint64_t)(event_id < 0 ? 0 : event_id);
@@ -864,11 +989,22 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
 
     CU(cudaMemsetAsync(e->counters.ptr, 0, 4 * sizeof(unsigned long long), s));
     int launches = prior_launches;
-    const bool pool = e->cfg.kernel_mode == 0;
+    const bool pool = e->cfg.kernel_mode != 1;
     if (pool && num_photon > 0) CU(cudaMemsetAsync(e->bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
+    if (e->cfg.kernel_mode == 2 && num_photon > 0) {
+        P.gen_photon = e->gen_photon.ptr;
+        P.gen_rng = e->gen_rng.ptr;
+        P.gen_hint = e->gen_hint.ptr;
+        launches++;
+    }
+    if (num_photon > 0) {
+        k_genstep_hint<<<(unsigned)((num_gs + 127) / 128), 128, 0, s>>>(P.acc, P.gs, (int)num_gs, e->gs_hint.ptr);
+        P.gs_hint = e->gs_hint.ptr;
+        launches++;
+    }
     CU(cudaEventRecord(e->ev[1], s));
     if (num_photon > 0) {
-        launch_simulate(e, P, num_photon, e->counters.ptr + 2, s);
+        launch_simulate(e, P, num_photon, e->counters.ptr + 2, s, P.gen_photon ? e->ev[4] : nullptr);
         CU(cudaGetLastError());
         launches++;
     }
@@ -905,6 +1041,8 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     cudaEventElapsedTime(&e->stats.ms_upload, e->ev[0], e->ev[1]);
     cudaEventElapsedTime(&e->stats.ms_simulate, e->ev[1], e->ev[2]);
     cudaEventElapsedTime(&e->stats.ms_compact, e->ev[2], e->ev[3]);
+    e->stats.ms_generate = 0.f;
+    if (P.gen_photon) cudaEventElapsedTime(&e->stats.ms_generate, e->ev[1], e->ev[4]);
     return GBO_OK;
 }
 
@@ -964,6 +1102,7 @@ int gbo_simulate(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         acc.ms_upload += e->stats.ms_upload;
         acc.ms_simulate += e->stats.ms_simulate;
         acc.ms_compact += e->stats.ms_compact;
+        acc.ms_generate += e->stats.ms_generate;
         acc.simulate_launches += e->stats.simulate_launches;
         acc.kernel_launches += e->stats.kernel_launches;
         at.photon_offset += n;
@@ -1124,6 +1263,7 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
     std::vector<Cand> cands = {{1, 32, 1}};
     for (int r : {1, 2, 4, 8, 16, 32})
         for (int p : {1, 4}) cands.push_back({0, r, p});
+    for (int r : {1, 2, 4, 8, 16}) cands.push_back({2, r, 1});
     const gbo_config saved = e->cfg;
     float best = 1e30f;
     Cand pick = cands[0];
@@ -1290,9 +1430,9 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_bounded(const __grid_con
     bool is_hit = false;
     if (idx < P.num_photon) {
         Rng rng;
-        generate(P, idx, p, rng);
+        int hint;
+        generate(P, idx, p, rng, hint);
         int bounce = 0;
-        int hint = -1;
         while (bounce < P.max_bounce && p.time < P.max_time) {
             const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
             Hit h;

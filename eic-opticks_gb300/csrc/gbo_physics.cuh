@@ -57,8 +57,10 @@ struct State {
 struct Hit {                 // per-ray intersect result, sysrap/squad.h:180-255 quad2 fields
     float3 normal;
     float t;
-    float lposcost;
-    float lposfphi;
+    // z of the intersect in the instance frame.  The reference carries lposcost = lpos.z / |lpos| and the photon
+    // path reads only its sign (qsim.h:2293, `lposcost < 0.f`), which is the sign of lpos.z; the cosine itself
+    // feeds the JUNO PMT surface models and the photonlite output, neither of which is on this path.
+    float lposz;
     unsigned iindex_identity;
     unsigned prim_boundary;
 };
@@ -502,7 +504,7 @@ GBO_DEV int propagate(const Tables& t, Photon& p, const Hit& h, Rng& rng, Acc64*
         const int ems = (int)s.optical.y;
         if (ems == GBO_EMS_NOSURFACE) command = propagate_at_boundary(t, p, s, h.normal, rng, flag);
         else if (ems == GBO_EMS_SURFACE) command = propagate_at_surface(t, p, s, h.normal, rng, flag);
-        else if (h.lposcost < 0.f) command = propagate_at_surface(t, p, s, h.normal, rng, flag);
+        else if (h.lposz < 0.f) command = propagate_at_surface(t, p, s, h.normal, rng, flag);
         else if (ems == GBO_EMS_ZPLUS_SENSOR_A) {
             skip(rng, 1);
             flag = GBO_SURFACE_DETECT;

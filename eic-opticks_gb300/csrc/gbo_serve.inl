@@ -87,6 +87,9 @@ struct Slot {
     DBuf<unsigned long long> gs_end, ev_photon_begin, ev_pos0, ev_photon_offset, block_offset, counters, hit_gidx, ev_hit;
     DBuf<int> ev_gs_begin;
     DBuf<gbo_sphoton> input, hits_unordered, hits;
+    DBuf<gbo_sphoton> gen_photon;       // kernel mode 2: the batch's pregenerated photons
+    DBuf<ulonglong2> gen_rng;
+    DBuf<int> gen_hint, gs_hint;        // start instance per pregenerated photon / per genstep
     DBuf<uint32_t> bitmap, word_prefix, block_sum;
     HBuf<gbo_quad6> h_gs;
     HBuf<unsigned long long> h_gs_end, h_ev_photon_begin, h_ev_pos0, h_ev_photon_offset, h_ev_hit, h_counters;
@@ -99,7 +102,8 @@ struct Slot {
     {
         gs.release(); gs_end.release(); ev_photon_begin.release(); ev_pos0.release(); ev_photon_offset.release();
         block_offset.release(); counters.release(); hit_gidx.release(); ev_hit.release(); ev_gs_begin.release();
-        input.release(); hits_unordered.release(); hits.release(); bitmap.release(); word_prefix.release();
+        input.release(); hits_unordered.release(); hits.release(); gen_photon.release(); gen_rng.release(); gen_hint.release(); gs_hint.release();
+        bitmap.release(); word_prefix.release();
         block_sum.release(); h_gs.release(); h_gs_end.release(); h_ev_photon_begin.release(); h_ev_pos0.release();
         h_ev_photon_offset.release(); h_ev_hit.release(); h_counters.release(); h_ev_gs_begin.release();
         staged.clear();
@@ -123,8 +127,10 @@ std::atomic<int>& big_counter(int device) { return g_big_in_flight[device >= 0 &
 // a batch's hits above this size go straight from the device into per-piece host buffers
 constexpr size_t SERVE_DIRECT_HIT_BYTES = 64ull << 20;
 
-// device bytes per photon slot of a batch: bitmap + prefix bits, unordered + ordered hit capacity, hit index
+// device bytes per photon slot of a batch: bitmap + prefix bits, unordered + ordered hit capacity, hit index;
+// kernel mode 2 adds the pregenerated photon and its random-stream place
 constexpr double SERVE_BYTES_PER_PHOTON = 0.25 + 64.0 + 64.0 + 8.0;
+constexpr double SERVE_BYTES_PER_PHOTON_GEN = 64.0 + 16.0 + 4.0;
 
 }  // namespace
 
@@ -179,8 +185,15 @@ int enqueue_batch(gbo_engine* e, Slot& sl, int n_ev, long long n_gs, bool has_in
     P.ev_pos0 = sl.ev_pos0.ptr;
     P.ev_photon_offset = sl.ev_photon_offset.ptr;
     P.hit_gidx = sl.hit_gidx.ptr;
+    if (e->cfg.kernel_mode == 2) {
+        P.gen_photon = sl.gen_photon.ptr;
+        P.gen_rng = sl.gen_rng.ptr;
+        P.gen_hint = sl.gen_hint.ptr;
+    }
     if (N > 0) {
-        if (e->cfg.kernel_mode == 0) CU(cudaMemsetAsync(sl.bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
+        if (e->cfg.kernel_mode != 1) CU(cudaMemsetAsync(sl.bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
+        k_genstep_hint<<<(unsigned)((n_gs + 127) / 128), 128, 0, s>>>(P.acc, P.gs, (int)n_gs, sl.gs_hint.ptr);
+        P.gs_hint = sl.gs_hint.ptr;
         launch_simulate(e, P, N, sl.counters.ptr + 2, s);
         CU(cudaGetLastError());
         k_word_prefix<<<(unsigned)nblk, SCAN_WORDS, 0, s>>>(sl.bitmap.ptr, words, sl.word_prefix.ptr, sl.block_sum.ptr);
@@ -241,7 +254,10 @@ int launch_batch(gbo_server* sv, Slot& sl)
         (rc = sl.ev_photon_offset.ensure(n_ev)) || (rc = sl.ev_hit.ensure(n_ev + 1)) ||
         (rc = sl.counters.ensure(4)) || (rc = sl.bitmap.ensure(words)) || (rc = sl.word_prefix.ensure(words)) ||
         (rc = sl.block_sum.ensure(nblk)) || (rc = sl.block_offset.ensure(nblk)) || (rc = sl.hits_unordered.ensure(N)) ||
-        (rc = sl.hit_gidx.ensure(N)) || (rc = sl.hits.ensure(N)) || (has_input && (rc = sl.input.ensure(N))))
+        (rc = sl.hit_gidx.ensure(N)) || (rc = sl.hits.ensure(N)) || (has_input && (rc = sl.input.ensure(N))) ||
+        (rc = sl.gs_hint.ensure(n_gs > 0 ? n_gs : 1)) ||
+        (e->cfg.kernel_mode == 2 &&
+         ((rc = sl.gen_photon.ensure(N)) || (rc = sl.gen_rng.ensure(N)) || (rc = sl.gen_hint.ensure(N)))))
         return rc;
     // input photons go up straight from each event's own copy, one copy per piece at the piece's launch position
     // (outside any graph: the source is pageable host memory)
@@ -500,7 +516,8 @@ int gbo_server_create(gbo_engine* e, const gbo_server_config* cfg, gbo_server** 
     auto* sv = new gbo_server();
     sv->e = e;
     sv->cfg = c;
-    const long long by_budget = (long long)((double)c.hbm_budget_bytes / (SERVE_BYTES_PER_PHOTON * c.slots));
+    const double per_photon = SERVE_BYTES_PER_PHOTON + (e->cfg.kernel_mode == 2 ? SERVE_BYTES_PER_PHOTON_GEN : 0.0);
+    const long long by_budget = (long long)((double)c.hbm_budget_bytes / (per_photon * c.slots));
     sv->max_batch_photon = c.max_batch_photon > 0 && c.max_batch_photon < by_budget ? c.max_batch_photon : by_budget;
     if (sv->max_batch_photon < 1) { delete sv; return fail(GBO_ERR_CAPACITY, "gbo_server_create: HBM budget below one photon per slot"); }
     sv->slots.resize((size_t)c.slots);

@@ -117,8 +117,10 @@ GBO_DEV InstDev load_inst(const InstDev* p)
 }
 
 // POLISH (precision mode): binary64 Newton polish of the quadric roots of sphere, zsphere and cylinder leaves
+// d_inv (optional): the correctly rounded reciprocals of d's components, for a single box3 leaf to reuse
 template <bool TREE, bool POLISH>
-GBO_DEV bool prim_hit(float4& is, const Accel& a, int node_word, float t_min, float3 o, float3 d)
+GBO_DEV bool prim_hit(float4& is, const Accel& a, int node_word, float t_min, float3 o, float3 d,
+                      const float3* d_inv = nullptr)
 {
     const gbo_csgnode* root = a.node + (node_word & 0x3fffffff);
     if (TREE) {
@@ -128,7 +130,7 @@ GBO_DEV bool prim_hit(float4& is, const Accel& a, int node_word, float t_min, fl
         }
         return intersect_prim(is, root, a.plan, a.itra, t_min, o, d, POLISH);
     }
-    if (node_typecode(root) >= GBO_CSG_LEAF) return intersect_leaf(is, root, a.plan, a.itra, t_min, o, d, POLISH);
+    if (node_typecode(root) >= GBO_CSG_LEAF) return intersect_leaf(is, root, a.plan, a.itra, t_min, o, d, POLISH, d_inv);
     is = make_float4(0.f, 0.f, 0.f, 0.f);
     return false;
 }
@@ -160,7 +162,8 @@ GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float
         if (!slab(pb0, pb1, oo, oinv, tmin, b.t, ptn)) continue;
         float4 is;
         if (!have64) { inst_ray64(a.inst64 + 12 * (size_t)ii, pos, dir, po, pd); have64 = true; }
-        if (!prim_hit<TREE, POLISH>(is, a, __float_as_int(pb0.w), tmin, po, pd)) continue;
+        // the prim-box reciprocals are those of the ray the leaf sees unless the precision mode re-transformed it
+        if (!prim_hit<TREE, POLISH>(is, a, __float_as_int(pb0.w), tmin, po, pd, POLISH ? nullptr : &oinv)) continue;
         const unsigned key = ((unsigned)ii << 16) | (unsigned)k2;
         if (is.w < b.t || (is.w == b.t && b.key != 0xffffffffu && key < b.key)) {
             b.t = is.w; b.key = key; b.is = is; b.inst = ii; b.pb = __float_as_uint(pb1.w);
@@ -173,21 +176,35 @@ constexpr int TRAVERSAL_STACK = 64;
 constexpr int HINT_FIRST = 0x7fffff;     // leaf item standing for the photon's previous instance
 constexpr int OVERLAP_FIRST = 0x7ffffe;  // leaf item standing for that instance's overlap list
 
-// work items: an inner node index (>= 0) or a leaf range encoded as -(1 + (first << 8 | count))
+// work items: an inner node index (>= 0), a leaf range encoded as -(1 + (first << 8 | count)), or ITEM_NONE
 GBO_DEV int leaf_item(int first, int count) { return -(1 + ((first << 8) | count)); }
+constexpr int ITEM_NONE = -0x7fffffff;
+
+// next work item: the top of the stack, else the TLAS root when it is still pending, else none
+GBO_DEV int pop_item(const int* stack, int& sp, bool& root_next)
+{
+    if (sp) return stack[--sp];
+    const int item = root_next ? 0 : ITEM_NONE;
+    root_next = false;
+    return item;
+}
 
 template <bool TREE, bool POLISH = false>
 GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tmax, int hint, Hit& h)
 {
     Best b;
     b.t = tmax; b.key = 0xffffffffu; b.is = make_float4(0.f, 0.f, 0.f, 0.f); b.inst = -1; b.pb = 0u;
-    const float3 inv = safe_inv(dir);
+    // the world-frame reciprocal direction serves the TLAS and list-neighbour box tests, which a step that stays
+    // inside its hint instance never reaches: computed on the way out of the hint item
+    float3 inv = f3(0.f, 0.f, 0.f);
     int stack[TRAVERSAL_STACK];
     int sp = 0;
-    constexpr int NONE = -0x7fffffff;
+    constexpr int NONE = ITEM_NONE;
     int item = 0;
     int ov_first = 0;
-    if (hint >= 0) { stack[sp++] = 0; item = leaf_item(HINT_FIRST, 1); }
+    bool root_next = false;         // the TLAS root waits under the hint item (kept out of the local-memory stack)
+    if (hint >= 0) { root_next = true; item = leaf_item(HINT_FIRST, 1); }
+    else inv = safe_inv(dir);
     // while-while traversal (Aila & Laine 2009): every lane first descends inner nodes until it holds a leaf, then
     // the lanes process their leaves together, so the expensive instance / CSG work runs with the warp converged;
     // each lane still visits its items in the same order as a one-item-per-iteration loop.  Leaf items are TLAS
@@ -212,7 +229,7 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
             } else if (v1) {
                 item = it1;
             } else {
-                item = sp ? stack[--sp] : NONE;
+                item = pop_item(stack, sp, root_next);
             }
         }
         while (item < 0 && item != NONE) {
@@ -222,7 +239,15 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
             for (int k = 0; k < count; k++) {
                 const int ii = first == HINT_FIRST ? hint
                              : first == OVERLAP_FIRST ? __ldg(a.overlap + ov_first + k) : __ldg(a.tlas_index + first + k);
-                if (first >= OVERLAP_FIRST || ii != hint) test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b);
+                if (first < OVERLAP_FIRST && ii == hint) continue;
+                if (first == OVERLAP_FIRST || count > 1) {
+                    // the instance's padded world box first: a list neighbour or a leaf sibling whose box the
+                    // segment (tmin, best] misses holds no closer hit, and skips the transform and prim tests
+                    const float4 wlo = __ldg(a.inst_box + 2 * ii), whi = __ldg(a.inst_box + 2 * ii + 1);
+                    float tn;
+                    if (!slab(wlo, whi, pos, inv, tmin, b.t, tn)) continue;
+                }
+                test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b);
             }
             if (first == HINT_FIRST) {
                 // when the previous instance's closest hit keeps the whole segment inside its box, only the instances
@@ -233,7 +258,9 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
                 if (ocount >= 0 && inside_box(blo, bhi, pos) && inside_box(blo, bhi, e)) {
                     ov_first = __float_as_int(blo.w);
                     sp = 0;
-                    item = ocount > 0 ? leaf_item(OVERLAP_FIRST, ocount) : NONE;
+                    root_next = false;
+                    item = NONE;
+                    if (ocount > 0) { item = leaf_item(OVERLAP_FIRST, ocount); inv = safe_inv(dir); }
                     continue;
                 }
                 // a container (long overlap list): a segment inside its clear ball meets no other instance
@@ -241,37 +268,38 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
                     const float4 cb = __ldg(a.clear + hint);
                     if (cb.w > 0.f && inside_ball(cb, pos) && inside_ball(cb, e)) {
                         sp = 0;
+                        root_next = false;
                         item = NONE;
                         continue;
                     }
                 }
+                inv = safe_inv(dir);                // the TLAS walk follows
             }
-            item = sp ? stack[--sp] : NONE;
+            item = pop_item(stack, sp, root_next);
         }
     }
 
     if (b.inst < 0) {
         h.normal = f3(0.f, 0.f, 0.f);
         h.t = 1.f;
-        h.lposcost = 0.f;
-        h.lposfphi = 0.f;
+        h.lposz = 0.f;
         h.iindex_identity = 0xffffffffu;
         h.prim_boundary = 0xffffffffu;
         return;
     }
     const InstDev d = load_inst(a.inst + b.inst);
     float3 n = f3(b.is.x, b.is.y, b.is.z);
-    float3 lpos;
+    float lz;
     if (d.is_identity) {
-        lpos = pos + b.is.w * dir;
+        lz = pos.z + b.is.w * dir.z;
     } else {
         n = inst_normal(d, n);
-        lpos = inst_point(d, pos) + b.is.w * inst_vector(d, dir);
+        lz = (d.c2[0] * pos.x + d.c2[1] * pos.y + d.c2[2] * pos.z + d.c2[3]) +
+             b.is.w * (d.c2[0] * dir.x + d.c2[1] * dir.y + d.c2[2] * dir.z);
     }
     h.normal = n;
     h.t = b.is.w;
-    h.lposcost = lpos.z / sqrtf(dot(lpos, lpos));
-    h.lposfphi = 0.f;
+    h.lposz = lz;
     h.iindex_identity = ((d.iindex & 0xffffu) << 16) | (d.identity & 0xffffu);
     h.prim_boundary = b.pb;
 }

@@ -55,7 +55,7 @@ class TuneResult(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("num_photon", C.c_int64), ("num_hit", C.c_int64), ("ms_upload", C.c_float),
                 ("ms_simulate", C.c_float), ("ms_compact", C.c_float), ("simulate_launches", C.c_int32),
-                ("kernel_launches", C.c_int32)]
+                ("kernel_launches", C.c_int32), ("ms_generate", C.c_float), ("reserved", C.c_int32)]
 
 
 EXPORTS = ["gbo_config_default", "gbo_engine_create", "gbo_engine_destroy", "gbo_simulate", "gbo_simulate_device",

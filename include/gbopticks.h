@@ -76,13 +76,17 @@ typedef struct gbo_config {
     int32_t  record_photon;         /* keep the full photon array of each event */
     int32_t  record_seq;            /* keep seqhis/seqbnd of each event */
     int64_t  max_photon;            /* capacity limit per event (0: no limit beyond device memory) */
-    int32_t  kernel_mode;           /* 0: persistent photon-pool kernel (default), 1: one thread per photon */
-    int32_t  refill_min;            /* pool kernel: idle lanes a warp waits for before refilling (1..32, 8) */
+    int32_t  kernel_mode;           /* 0: persistent photon-pool kernel generating its photons, 1: one thread per
+                                       photon, 2 (default): photon pool over photons generated up front by a
+                                       separate kernel (84 more device bytes per photon; gbo_simulate_noalloc runs
+                                       its own one-thread kernel) */
+    int32_t  refill_min;            /* pool kernel: idle lanes a warp waits for before refilling (1..32, 4) */
     int32_t  blocks_per_sm;         /* pool kernel: resident blocks per SM (0: occupancy maximum) */
     int32_t  refill_period;         /* pool kernel: steps between refill checks (compaction period, >= 1) */
     int64_t  max_slot;              /* OPTICKS_MAX_SLOT: photons per launch, larger events are sliced (0: no slicing) */
-    int32_t  precision;             /* 0: binary32 as the reference (default); 1: binary64 Newton polish of quadric
-                                       roots when |t| 2^-24 > 1e-4 mm and binary64 position/time accumulators */
+    int32_t  precision;             /* 0: binary32 as the reference (default); 1: binary64 Newton polish of every
+                                       accepted sphere / zsphere / cylinder root and binary64 position/time
+                                       accumulators */
     int32_t  reserved;
 } gbo_config;
 
@@ -101,6 +105,8 @@ typedef struct gbo_stats {
     float   ms_compact;             /* hit scan + gather */
     int32_t simulate_launches;
     int32_t kernel_launches;        /* all engine kernels of the last event */
+    float   ms_generate;            /* kernel mode 2: the generation kernel (part of ms_simulate) */
+    int32_t reserved;
 } gbo_stats;
 
 int         gbo_config_default(gbo_config* cfg);

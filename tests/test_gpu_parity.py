@@ -185,7 +185,8 @@ def test_kernel_forms_agree(E):
     z = load_golden("sim_crystal_array.npz")
     arrays = golden_arrays(z)
     outs = []
-    for mode, refill in ((1, 1), (0, 1), (0, 8), (0, 32)):
+    forms = ((1, 1), (0, 1), (0, 8), (0, 32), (2, 1), (2, 8))
+    for mode, refill in forms:
         eng = E.Engine(arrays, record_photon=1, record_seq=1, kernel_mode=mode, refill_min=refill)
         n = eng.simulate(int(z["event_index"]), z["gs"])
         outs.append((eng.photons(), eng.seq(), eng.hits(), n))
@@ -195,6 +196,11 @@ def test_kernel_forms_agree(E):
         assert np.array_equal(s.view(np.uint64), s0.view(np.uint64))
         print("kernel forms: max |dpos| %.3g mm, |dt| %.3g ns, |dvec| %.3g, |dwl| %.3g" % assert_photons_agree(p, p0))
         assert n == n0 and np.array_equal(h["index"], h0["index"])
+    # pregenerated photons (mode 2) run the same pool kernel: the same bytes as generating in the kernel
+    pool = outs[forms.index((0, 1))]
+    for k in (forms.index((2, 1)), forms.index((2, 8))):
+        assert np.array_equal(outs[k][0].view(np.uint32), pool[0].view(np.uint32))
+        assert np.array_equal(outs[k][2].view(np.uint32), pool[2].view(np.uint32))
 
 
 @pytest.mark.parametrize("max_slot", [500, 1000, 1234])

@@ -30,8 +30,8 @@ def make_events(rng, n, geom_kind, wc=None):
     return events
 
 
-@pytest.mark.parametrize("kind,use_graph", [("crystal", 1), ("water", 1), ("crystal", 0)])
-def test_served_events_equal_alone(E, kind, use_graph):
+@pytest.mark.parametrize("kind,use_graph,mode", [("crystal", 1, 0), ("water", 1, 0), ("crystal", 0, 0), ("crystal", 1, 2)])
+def test_served_events_equal_alone(E, kind, use_graph, mode):
     from eic_opticks_gb300 import geometry as G
     geom = G.crystal_array() if kind == "crystal" else G.water_cube()
     arrays = geom.arrays()
@@ -43,7 +43,7 @@ def test_served_events_equal_alone(E, kind, use_graph):
         alone[eid] = eng_alone.hits()
     eng_alone.close()
 
-    eng = E.Engine(arrays)
+    eng = E.Engine(arrays, kernel_mode=mode)
     srv = E.Server(eng, slots=3, max_batch_events=16, use_graph=use_graph)
     tickets = {}
     lock = threading.Lock()
