@@ -455,11 +455,13 @@ GBO_DEV bool intersect_leaf(float4& is, const gbo_csgnode* node, const float4* p
                               gt == 0 && rd_inv ? *rd_inv
                                                 : f3(1.f / direction.x, 1.f / direction.y, 1.f / direction.z));
             break;
-        case GBO_CSG_CONE:             valid = leaf_cone(is, nd.q0, t_min, origin, direction); break;
-        case GBO_CSG_CONVEXPOLYHEDRON: valid = leaf_convexpolyhedron(is, nd.q0, plan, t_min, origin, direction); break;
-        case GBO_CSG_HYPERBOLOID:      valid = leaf_hyperboloid(is, nd.q0, t_min, origin, direction); break;
-        case GBO_CSG_PHICUT:           valid = leaf_phicut(is, nd.q0, t_min, origin, direction); break;
-        case GBO_CSG_HALFSPACE:        valid = leaf_halfspace(is, nd.q0, t_min, origin, direction); break;
+        // the out-of-line leaves write a copy: `is` itself never has its address taken, so it stays in registers
+        // on the other paths
+        case GBO_CSG_CONE:             { float4 c = is; valid = leaf_cone(c, nd.q0, t_min, origin, direction); is = c; } break;
+        case GBO_CSG_CONVEXPOLYHEDRON: { float4 c = is; valid = leaf_convexpolyhedron(c, nd.q0, plan, t_min, origin, direction); is = c; } break;
+        case GBO_CSG_HYPERBOLOID:      { float4 c = is; valid = leaf_hyperboloid(c, nd.q0, t_min, origin, direction); is = c; } break;
+        case GBO_CSG_PHICUT:           { float4 c = is; valid = leaf_phicut(c, nd.q0, t_min, origin, direction); is = c; } break;
+        case GBO_CSG_HALFSPACE:        { float4 c = is; valid = leaf_halfspace(c, nd.q0, t_min, origin, direction); is = c; } break;
         default: break;
     }
     if (valid && gt > 0) {

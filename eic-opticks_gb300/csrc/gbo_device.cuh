@@ -147,17 +147,21 @@ GBO_DEV void store_photon(gbo_sphoton* s, const Photon& p)
                        __uint_as_float(p.index), __uint_as_float(p.flagmask));
 }
 
-// photon history nibbles : sysrap/sseq.h:174-184
-struct Seq { unsigned long long his[2], bnd[2]; };
-GBO_DEV void seq_add(Seq& q, unsigned slot, unsigned flag, unsigned boundary)
+// photon history nibbles : sysrap/sseq.h:174-184.  The record is kept in its output slot in device memory (a
+// debug output): the simulation loop then holds no registers for it when recording is off.
+GBO_DEV void seq_add(gbo_seq* q, unsigned slot, unsigned flag, unsigned boundary)
 {
     const unsigned iseq = slot / 16u;
     const unsigned shift = 4u * (slot - iseq * 16u);
     if (iseq < 2u) {
-        const unsigned long long h = ((unsigned long long)(__ffs((int)flag) & 0xf)) << shift;
-        const unsigned long long b = ((unsigned long long)(boundary & 0xfu)) << shift;
-        if (iseq == 0) { q.his[0] |= h; q.bnd[0] |= b; } else { q.his[1] |= h; q.bnd[1] |= b; }
+        q->seqhis[iseq] |= ((unsigned long long)(__ffs((int)flag) & 0xf)) << shift;
+        q->seqbnd[iseq] |= ((unsigned long long)(boundary & 0xfu)) << shift;
     }
+}
+GBO_DEV void seq_start(gbo_seq* q, unsigned flag, unsigned boundary)
+{
+    q->seqhis[0] = q->seqhis[1] = q->seqbnd[0] = q->seqbnd[1] = 0ull;
+    seq_add(q, 0u, flag, boundary);
 }
 
 }  // namespace gbo

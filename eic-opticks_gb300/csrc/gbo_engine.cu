@@ -111,10 +111,8 @@ k_simulate(const __grid_constant__ Params P)
         generate(P, idx, p, rng, hint);
         if (PRECISE) acc_init(acc, p);
 
-        Seq seq;
-        seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
         int bounce = 0;
-        if (P.seq_out) seq_add(seq, 0u, flag_of(p), boundary_of(p));
+        if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
         while (bounce < P.max_bounce && p.time < P.max_time) {
             const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
             Hit h;
@@ -124,16 +122,11 @@ k_simulate(const __grid_constant__ Params P)
             h.normal = normalize(h.normal);
             const int command = propagate(P.tab, p, h, rng, PRECISE ? &acc : nullptr);
             bounce++;
-            if (P.seq_out) seq_add(seq, (unsigned)bounce, flag_of(p), boundary_of(p));
+            if (P.seq_out) seq_add(P.seq_out + idx, (unsigned)bounce, flag_of(p), boundary_of(p));
             if (command == CMD_BREAK) break;
         }
         is_hit = (p.flagmask & P.hitmask) == P.hitmask;
         if (P.photon_out) store_photon(P.photon_out + idx, p);
-        if (P.seq_out) {
-            ulonglong2* s = reinterpret_cast<ulonglong2*>(P.seq_out + idx);
-            s[0] = make_ulonglong2(seq.his[0], seq.his[1]);
-            s[1] = make_ulonglong2(seq.bnd[0], seq.bnd[1]);
-        }
     }
     const unsigned lane = threadIdx.x & 31u;
     const unsigned mask = __ballot_sync(0xffffffffu, is_hit);
@@ -225,7 +218,6 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
     Photon p;
     Rng rng;
     Acc64 acc;
-    Seq seq;
     // mode 2 (warp-uniform): the warp's claimed chunk of pregenerated photons [cbase, cbase + cn), cused taken
     long long cbase = 0;
     int cn = 0, cused = 0;
@@ -256,8 +248,7 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
                     hint = P.gen_hint[idx];
                     if (PRECISE) acc_init(acc, p);
                     bounce = 0;
-                    seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
-                    if (P.seq_out) seq_add(seq, 0u, flag_of(p), boundary_of(p));
+                    if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
                     live = true;
                 }
             }
@@ -282,8 +273,7 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
                     generate(P, idx, p, rng, hint);
                     if (PRECISE) acc_init(acc, p);
                     bounce = 0;
-                    seq.his[0] = seq.his[1] = seq.bnd[0] = seq.bnd[1] = 0ull;
-                    if (P.seq_out) seq_add(seq, 0u, flag_of(p), boundary_of(p));
+                    if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
                     live = true;
                 }
             }
@@ -305,7 +295,7 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
                     h.normal = normalize(h.normal);
                     const int command = propagate(P.tab, p, h, rng, PRECISE ? &acc : nullptr);
                     bounce++;
-                    if (P.seq_out) seq_add(seq, (unsigned)bounce, flag_of(p), boundary_of(p));
+                    if (P.seq_out) seq_add(P.seq_out + idx, (unsigned)bounce, flag_of(p), boundary_of(p));
                     done = command == CMD_BREAK;
                 }
             } else {
@@ -316,11 +306,6 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
         if (done) {
             if (is_hit) atomicOr(P.bitmap + (idx >> 5), 1u << (idx & 31));
             if (P.photon_out) store_photon(P.photon_out + idx, p);
-            if (P.seq_out) {
-                ulonglong2* s = reinterpret_cast<ulonglong2*>(P.seq_out + idx);
-                s[0] = make_ulonglong2(seq.his[0], seq.his[1]);
-                s[1] = make_ulonglong2(seq.bnd[0], seq.bnd[1]);
-            }
             live = false;
         }
         if (P.hit_unordered) {
