@@ -41,9 +41,9 @@ L2_FLUSH_BYTES = 256 << 20
 # the only DRAM traffic, all grow with the photons
 # ncu DRAM bytes (read + write) per photon of the simulate kernels on the crystal event, scaled by photons:
 # one thread per photon (k_simulate, 1M-photon event), and the pregenerated pool (k_generate + k_simulate_pool,
-# 2.5M-photon event: 182.1 + 0.2 MB and 210.9 + 2.5 MB, larger than L2)
+# 2.5M-photon event: 0.22 + 182.10 MB and 210.98 + 2.46 MB, larger than L2)
 TRAFFIC_B_PER_PHOTON = {("crystal_array", 1): (443392.0 + 840192.0) / 998319,
-                        ("crystal_array", 2): (182.1e6 + 0.2e6 + 210.9e6 + 2.5e6) / 2499792}
+                        ("crystal_array", 2): (0.22e6 + 182.10e6 + 210.98e6 + 2.46e6) / 2499792}
 TRAFFIC_SOURCE = {1: "profiles/k_simulate_crystal_array.md (ncu, 1M-photon event, scaled by photons)",
                   2: "profiles/k_simulate_pool_pregen_crystal_array.md (ncu, 2.5M-photon event, scaled by photons)"}
 

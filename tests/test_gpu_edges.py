@@ -85,3 +85,39 @@ def test_event_above_photon_limit_is_refused(E):
         eng.simulate(0, GS.crystal_scint_gensteps(4, 500, seed=1, poisson=False))
     assert eng.simulate(0, GS.crystal_scint_gensteps(1, 500, seed=1, poisson=False)) >= 0    # still usable
     eng.close()
+
+
+@pytest.mark.parametrize("n_photon", [1, 31, 33, 1000, 4097])
+def test_pregenerated_pool_small_events_equal_one_thread(E, n_photon):
+    """The pregenerated photon pool hands photons out in warp chunks of 32: events smaller than one chunk, than the
+    grid, and with ragged last chunks give the same photons and hits as the one-thread-per-photon kernel."""
+    from eic_opticks_gb300 import geometry as G, gensteps as GS
+    arrays = G.crystal_array().arrays()
+    gs = GS.crystal_scint_gensteps(1, n_photon, seed=n_photon, poisson=False)
+    out = []
+    for mode in (1, 2):
+        eng = E.Engine(arrays, record_photon=1, record_seq=1, kernel_mode=mode, refill_min=1)
+        eng.simulate(5, gs)
+        out.append((eng.photons(), eng.seq(), eng.hits()))
+        eng.close()
+    (p1, s1, h1), (p2, s2, h2) = out
+    assert len(p1) == len(p2) == n_photon
+    assert np.array_equal(s1.view(np.uint64), s2.view(np.uint64))
+    assert np.array_equal(p1["index"], p2["index"]) and np.array_equal(h1["index"], h2["index"])
+
+
+def test_genstep_hint_outside_every_instance(E):
+    """A genstep whose position lies outside every instance box gets no start hint; its photons still trace from
+    the TLAS root and match the one-thread kernel."""
+    from eic_opticks_gb300 import geometry as G, gensteps as GS
+    arrays = G.nested_boxes(sensor=True).arrays()
+    gs = GS.input_photon_genstep(2000)
+    gs.view(np.float32)[0, 1, :3] = 1e7          # q1.xyz: far outside the world box
+    inp = GS.isotropic_photons(2000, seed=4)
+    out = []
+    for mode in (1, 2):
+        eng = E.Engine(arrays, kernel_mode=mode)
+        eng.simulate(0, gs, inp)
+        out.append(eng.hits())
+        eng.close()
+    assert len(out[0]) > 0 and np.array_equal(out[0]["index"], out[1]["index"])
