@@ -58,7 +58,8 @@ struct Builder {
 
     Builder(std::vector<int32_t>& idx, std::vector<BvhNode>& n) : index(idx), nodes(n) {}
 
-    int build(int begin, int end, int depth)
+    // forced_mid (begin < forced_mid < end): split there instead of by SAH
+    int build(int begin, int end, int depth, int forced_mid = -1)
     {
         max_depth = std::max(max_depth, depth);
         Box bb, cb;
@@ -76,43 +77,60 @@ struct Builder {
             nodes[self].count = n;
             return self;
         }
-        // binned SAH over the widest centroid axis, 16 bins
+        // binned SAH, 32 bins on each axis with a centroid spread; the cheapest split over the three axes
+        int mid = begin + n / 2;
         int axis = 0;
         for (int k = 1; k < 3; k++) if (cb.hi[k] - cb.lo[k] > cb.hi[axis] - cb.lo[axis]) axis = k;
-        int mid = begin + n / 2;
-        const double span = cb.hi[axis] - cb.lo[axis];
-        if (span > 0.0) {
-            const int NB = 16;
-            Box bin[NB];
-            int cnt[NB] = {0};
-            for (int i = begin; i < end; i++) {
-                int b = (int)((boxes[index[i]].centroid(axis) - cb.lo[axis]) / span * NB);
-                b = std::min(NB - 1, std::max(0, b));
-                cnt[b]++;
-                bin[b].grow(boxes[index[i]]);
-            }
+        if (forced_mid > begin && forced_mid < end) {
+            mid = forced_mid;
+        } else if (cb.hi[axis] - cb.lo[axis] > 0.0) {
+            constexpr int NB = 32;
             double best = 1e300;
-            int best_split = -1;
-            for (int s = 1; s < NB; s++) {
-                Box l, r;
-                int nl = 0, nr = 0;
-                for (int b = 0; b < s; b++) { if (cnt[b]) { l.grow(bin[b]); nl += cnt[b]; } }
-                for (int b = s; b < NB; b++) { if (cnt[b]) { r.grow(bin[b]); nr += cnt[b]; } }
-                if (nl == 0 || nr == 0) continue;
-                double cost = l.area() * nl + r.area() * nr;
-                if (cost < best) { best = cost; best_split = s; }
+            int best_axis = -1, best_split = -1;
+            for (int ax = 0; ax < 3; ax++) {
+                const double span = cb.hi[ax] - cb.lo[ax];
+                if (!(span > 0.0)) continue;
+                Box bin[NB];
+                int cnt[NB] = {0};
+                for (int i = begin; i < end; i++) {
+                    int bi = (int)((boxes[index[i]].centroid(ax) - cb.lo[ax]) / span * NB);
+                    bi = std::min(NB - 1, std::max(0, bi));
+                    cnt[bi]++;
+                    bin[bi].grow(boxes[index[i]]);
+                }
+                // right-to-left sweep of the suffix areas, then left-to-right over the split planes
+                double right_area[NB];
+                int right_cnt[NB];
+                Box acc;
+                int nacc = 0;
+                for (int bi = NB - 1; bi >= 1; bi--) {
+                    if (cnt[bi]) { acc.grow(bin[bi]); nacc += cnt[bi]; }
+                    right_area[bi] = acc.area();
+                    right_cnt[bi] = nacc;
+                }
+                Box left;
+                int nl = 0;
+                for (int sp = 1; sp < NB; sp++) {
+                    if (cnt[sp - 1]) { left.grow(bin[sp - 1]); nl += cnt[sp - 1]; }
+                    if (nl == 0 || right_cnt[sp] == 0) continue;
+                    const double cost = left.area() * nl + right_area[sp] * right_cnt[sp];
+                    if (cost < best) { best = cost; best_axis = ax; best_split = sp; }
+                }
             }
-            if (best_split > 0) {
+            if (best_axis >= 0) {
+                const int ax = best_axis;
+                const double span = cb.hi[ax] - cb.lo[ax];
                 auto it = std::partition(index.begin() + begin, index.begin() + end, [&](int32_t id) {
-                    int b = (int)((boxes[id].centroid(axis) - cb.lo[axis]) / span * NB);
-                    b = std::min(NB - 1, std::max(0, b));
-                    return b < best_split;
+                    int bi = (int)((boxes[id].centroid(ax) - cb.lo[ax]) / span * NB);
+                    bi = std::min(NB - 1, std::max(0, bi));
+                    return bi < best_split;
                 });
                 mid = (int)(it - index.begin());
+                axis = ax;
             }
             if (mid == begin || mid == end) {
                 std::nth_element(index.begin() + begin, index.begin() + begin + n / 2, index.begin() + end,
-                                 [&](int32_t a, int32_t b) { return boxes[a].centroid(axis) < boxes[b].centroid(axis); });
+                                 [&](int32_t a, int32_t c) { return boxes[a].centroid(axis) < boxes[c].centroid(axis); });
                 mid = begin + n / 2;
             }
         }
@@ -353,12 +371,25 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
             out.clear[4 * (size_t)i + 3] = (float)(r * r);
         }
     }
+    // Containers (instances whose box has at least a quarter of the area of the box of everything, e.g. a world
+    // volume) hang off the root in their own subtree: inside the SAH split they would stretch every node on the
+    // way down to their leaf to their own size, and a TLAS walk would descend that whole chain for any ray.
     out.tlas_index.resize(num_inst);
-    for (int i = 0; i < num_inst; i++) out.tlas_index[i] = i;
+    int num_big = 0;
+    {
+        Box all;
+        for (int i = 0; i < num_inst; i++) all.grow(inst_box[i]);
+        const double big_area = 0.25 * all.area();
+        for (int i = 0; i < num_inst; i++)
+            if (inst_box[i].area() >= big_area) out.tlas_index[num_big++] = i;
+        int k = num_big;
+        for (int i = 0; i < num_inst; i++)
+            if (inst_box[i].area() < big_area) out.tlas_index[k++] = i;
+    }
     Builder b(out.tlas_index, out.tlas);
     b.boxes = inst_box;
     out.tlas.reserve(2 * num_inst);
-    b.build(0, num_inst, 0);
+    b.build(0, num_inst, 0, num_big > 0 && num_big < num_inst ? num_big : -1);
     out.max_depth = b.max_depth;
 
     // two-child-box form: node k of tlas2 corresponds to inner node map[k] of tlas
