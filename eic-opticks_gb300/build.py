@@ -17,7 +17,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["gbo_engine.cu", "gbo_merge.cu"]
 CPP_SOURCES = ["gbo_accel.cpp"]
-HEADERS = ["gbo_device.cuh", "gbo_csg.cuh", "gbo_physics.cuh", "gbo_trace.cuh", "gbo_accel.h", "gbo_serve.inl"]
+HEADERS = ["gbo_device.cuh", "gbo_csg.cuh", "gbo_physics.cuh", "gbo_trace.cuh", "gbo_accel.h", "gbo_serve.inl",
+           "gbo_merge.h"]
 
 
 def _newer(target, deps):

@@ -26,6 +26,7 @@
 #include "../../include/gbopticks.h"
 #include "gbo_accel.h"
 #include "gbo_trace.cuh"
+#include "gbo_merge.h"
 
 namespace gbo {
 
@@ -646,6 +647,7 @@ struct gbo_engine {
     DBuf<gbo_sphoton> hits_unordered;
     DBuf<gbo_sphoton> hits;
     DBuf<gbo_sphoton> merged;               // hits merged by (identity, time bucket), gbo_merge_hits
+    gbo::MergeScratch* merge_scratch = nullptr;     // the merge's work buffers, kept between events
     DBuf<gbo_sphoton> gen_photon;           // kernel mode 2: pregenerated photons, their random-stream places and
     DBuf<ulonglong2> gen_rng;               // start instances
     DBuf<int> gen_hint;
@@ -777,7 +779,7 @@ void gbo_engine_destroy(gbo_engine* e)
     e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->inst_box.release(); e->overlap.release(); e->clear.release(); e->prim.release(); e->solid.release();
     e->node.release(); e->plan.release(); e->itra.release(); e->optical.release();
     e->gs.release(); e->gs_end.release(); e->input.release(); e->photon.release(); e->seq.release();
-    e->hits_unordered.release(); e->hits.release(); e->merged.release(); e->gen_photon.release(); e->gen_rng.release(); e->gen_hint.release(); e->gs_hint.release(); e->bitmap.release(); e->word_prefix.release();
+    e->hits_unordered.release(); e->hits.release(); e->merged.release(); gbo::merge_scratch_free(e->merge_scratch); e->merge_scratch = nullptr; e->gen_photon.release(); e->gen_rng.release(); e->gen_hint.release(); e->gs_hint.release(); e->bitmap.release(); e->word_prefix.release();
     e->block_sum.release(); e->block_offset.release(); e->counters.release();
     if (e->host_counters) cudaFreeHost(e->host_counters);
     for (auto& v : e->ev) if (v) cudaEventDestroy(v);
@@ -1174,7 +1176,8 @@ int gbo_merge_hits(gbo_engine* e, float time_window, int64_t* num_merged)
     int rc;
     if ((rc = e->merged.ensure(e->num_hit > 0 ? e->num_hit : 1))) return rc;
     int64_t n = 0;
-    rc = gbo_merge_hits_device(e->hits.ptr, e->num_hit, time_window, e->merged.ptr, &n, e->stream);
+    if (!e->merge_scratch) e->merge_scratch = gbo::merge_scratch_new();
+    rc = gbo::merge_hits(e->hits.ptr, e->num_hit, time_window, e->merged.ptr, &n, e->stream, e->merge_scratch);
     if (rc) return fail(rc, "gbo_merge_hits: merge of %lld hits failed", e->num_hit);
     e->num_merged = n;
     *num_merged = n;

@@ -18,7 +18,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "gbopticks.h"
+#include "gbo_merge.h"
 
 namespace {
 
@@ -276,13 +276,31 @@ __global__ void k_run_reduce(const gbo_sphoton* in, const uint32_t* order, const
 
 }  // namespace
 
-// Merge n device hits into d_out (room for n); *num_out receives the merged count.  Synchronous on `stream`.
-extern "C" int gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float time_window, gbo_sphoton* d_out,
-                                     int64_t* num_out, void* stream_)
+namespace gbo {
+
+// Grow-only device buffers of the hit merge, kept by an engine between events
+struct MergeScratch {
+    void* buf[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    size_t cap[7] = {0, 0, 0, 0, 0, 0, 0};
+};
+
+MergeScratch* merge_scratch_new() { return new MergeScratch(); }
+
+void merge_scratch_free(MergeScratch* m)
+{
+    if (!m) return;
+    for (void* b : m->buf)
+        if (b) cudaFree(b);
+    delete m;
+}
+
+// Merge n device hits into d_out (room for n); *num_out receives the merged count.  Synchronous on `stream`.  With
+// `scratch` the work buffers come from (and grow) it; without, they are allocated and freed stream-ordered.
+int merge_hits(const gbo_sphoton* d_in, int64_t n, float time_window, gbo_sphoton* d_out, int64_t* num_out,
+               cudaStream_t s, MergeScratch* scratch)
 {
     if (!num_out || n < 0 || (n > 0 && (!d_in || !d_out))) return GBO_ERR_ARG;
     if (n > 0xffffffffll) return GBO_ERR_CAPACITY;
-    cudaStream_t s = (cudaStream_t)stream_;
     *num_out = 0;
     if (n == 0) return GBO_OK;
     if (time_window == 0.f) {                                   // NOMERGE_TIME_WINDOW: the hits as they are
@@ -294,18 +312,32 @@ extern "C" int gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float t
     }
     int rc = GBO_OK;
     const int ntiles = (int)((n + MB_TILE - 1) / MB_TILE);
-    uint64_t *k0 = nullptr, *k1 = nullptr;
-    uint32_t *i0 = nullptr, *i1 = nullptr, *hist = nullptr, *scan_tmp = nullptr;
-    unsigned long long* scal = nullptr;                         // [0] key OR, [1] scan total
+    const long long scan_n = n > 256ll * ntiles ? n : 256ll * ntiles;
+    // k0, k1 (keys), i0, i1 (input indices), hist (digit x tile counts, later the run heads), scal ([0] key OR,
+    // [1] run count), scan_tmp (tile sums of the scans)
+    const size_t need[7] = {(size_t)n * 8, (size_t)n * 8, (size_t)n * 4, (size_t)n * 4, (size_t)scan_n * 4,
+                            2 * sizeof(unsigned long long), (size_t)(scan_n / SCAN_TILE + 1) * 4};
+    void* b[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    for (int k = 0; k < 7; k++) {
+        if (scratch) {
+            if (scratch->cap[k] < need[k]) {
+                if (scratch->buf[k]) cudaFree(scratch->buf[k]);
+                scratch->buf[k] = nullptr;
+                scratch->cap[k] = 0;
+                MCU(cudaMalloc(&scratch->buf[k], need[k]));
+                scratch->cap[k] = need[k];
+            }
+            b[k] = scratch->buf[k];
+        } else {
+            MCU(cudaMallocAsync(&b[k], need[k], s));
+        }
+    }
+    {
+    uint64_t *k0 = (uint64_t*)b[0], *k1 = (uint64_t*)b[1];
+    uint32_t *i0 = (uint32_t*)b[2], *i1 = (uint32_t*)b[3], *hist = (uint32_t*)b[4], *scan_tmp = (uint32_t*)b[6];
+    unsigned long long* scal = (unsigned long long*)b[5];
     unsigned long long h_scal[2] = {0ull, 0ull};
     const int grid = (int)((n + MB_THREADS - 1) / MB_THREADS < 4096 ? (n + MB_THREADS - 1) / MB_THREADS : 4096);
-    MCU(cudaMallocAsync((void**)&k0, (size_t)n * 8, s));
-    MCU(cudaMallocAsync((void**)&k1, (size_t)n * 8, s));
-    MCU(cudaMallocAsync((void**)&i0, (size_t)n * 4, s));
-    MCU(cudaMallocAsync((void**)&i1, (size_t)n * 4, s));
-    MCU(cudaMallocAsync((void**)&hist, (size_t)256 * ntiles * 4 > (size_t)n * 4 ? (size_t)256 * ntiles * 4 : (size_t)n * 4, s));
-    MCU(cudaMallocAsync((void**)&scal, 2 * sizeof(unsigned long long), s));
-    MCU(cudaMallocAsync((void**)&scan_tmp, (size_t)((n > 256ll * ntiles ? n : 256ll * ntiles) / SCAN_TILE + 1) * 4, s));
     MCU(cudaMemsetAsync(scal, 0, 2 * sizeof(unsigned long long), s));
     k_merge_keys<<<grid, MB_THREADS, 0, s>>>(d_in, n, time_window, k0, i0, scal);
     MCU(cudaGetLastError());
@@ -320,30 +352,38 @@ extern "C" int gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float t
         uint64_t* tk = k0; k0 = k1; k1 = tk;
         uint32_t* ti = i0; i0 = i1; i1 = ti;
     }
-    {
-        // runs of equal keys: heads -> exclusive scan (run index of each head) -> run starts -> fold
-        uint32_t* head = hist;                                  // n words (hist was sized for max(n, 256 ntiles))
-        k_run_heads<<<grid, MB_THREADS, 0, s>>>(k0, n, head);
-        scan_exclusive(head, n, scan_tmp, scal + 1, s);
-        MCU(cudaGetLastError());
-        MCU(cudaMemcpyAsync(h_scal + 1, scal + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-        MCU(cudaStreamSynchronize(s));
-        const long long runs = (long long)h_scal[1];
-        uint32_t* start = i1;                                   // free after the last pass
-        k_run_starts<<<grid, MB_THREADS, 0, s>>>(k0, n, head, start);
-        const int rgrid = (int)((runs + MB_THREADS - 1) / MB_THREADS < 4096 ? (runs + MB_THREADS - 1) / MB_THREADS : 4096);
-        if ((((uintptr_t)d_in | (uintptr_t)d_out) & 15u) == 0u)
-            k_run_reduce<true><<<rgrid > 0 ? rgrid : 1, MB_THREADS, 0, s>>>(d_in, i0, start, runs, n, d_out);
-        else
-            k_run_reduce<false><<<rgrid > 0 ? rgrid : 1, MB_THREADS, 0, s>>>(d_in, i0, start, runs, n, d_out);
-        MCU(cudaGetLastError());
-        MCU(cudaStreamSynchronize(s));
-        *num_out = runs;
+    // runs of equal keys: heads -> exclusive scan (run index of each head) -> run starts -> fold
+    uint32_t* head = hist;                                      // n words (hist was sized for max(n, 256 ntiles))
+    k_run_heads<<<grid, MB_THREADS, 0, s>>>(k0, n, head);
+    scan_exclusive(head, n, scan_tmp, scal + 1, s);
+    MCU(cudaGetLastError());
+    MCU(cudaMemcpyAsync(h_scal + 1, scal + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    MCU(cudaStreamSynchronize(s));
+    const long long runs = (long long)h_scal[1];
+    uint32_t* start = i1;                                       // free after the last pass
+    k_run_starts<<<grid, MB_THREADS, 0, s>>>(k0, n, head, start);
+    const int rgrid = (int)((runs + MB_THREADS - 1) / MB_THREADS < 4096 ? (runs + MB_THREADS - 1) / MB_THREADS : 4096);
+    if ((((uintptr_t)d_in | (uintptr_t)d_out) & 15u) == 0u)
+        k_run_reduce<true><<<rgrid > 0 ? rgrid : 1, MB_THREADS, 0, s>>>(d_in, i0, start, runs, n, d_out);
+    else
+        k_run_reduce<false><<<rgrid > 0 ? rgrid : 1, MB_THREADS, 0, s>>>(d_in, i0, start, runs, n, d_out);
+    MCU(cudaGetLastError());
+    MCU(cudaStreamSynchronize(s));
+    *num_out = runs;
     }
 done:
-    void* bufs[7] = {k0, k1, i0, i1, hist, scal, scan_tmp};
-    for (void* b : bufs)
-        if (b) cudaFreeAsync(b, s);
+    if (!scratch)
+        for (void* x : b)
+            if (x) cudaFreeAsync(x, s);
     if (cudaStreamSynchronize(s) != cudaSuccess && rc == GBO_OK) rc = GBO_ERR_CUDA;
     return rc;
+}
+
+}  // namespace gbo
+
+// Merge n device hits into d_out (room for n) with stream-ordered temporary buffers.
+extern "C" int gbo_merge_hits_device(const gbo_sphoton* d_in, int64_t n, float time_window, gbo_sphoton* d_out,
+                                     int64_t* num_out, void* stream)
+{
+    return gbo::merge_hits(d_in, n, time_window, d_out, num_out, (cudaStream_t)stream, nullptr);
 }
