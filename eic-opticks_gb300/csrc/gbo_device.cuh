@@ -137,6 +137,19 @@ GBO_DEV void load_photon(Photon& p, const gbo_sphoton* s)
     p.index = __float_as_uint(d.z); p.flagmask = __float_as_uint(d.w);
 }
 
+// the same through L2 only (ld.global.cg): streamed photons read once do not displace the L1-resident geometry and
+// boundary texture lines
+GBO_DEV void load_photon_streamed(Photon& p, const gbo_sphoton* s)
+{
+    const float4* q = reinterpret_cast<const float4*>(s);
+    const float4 a = __ldcg(q), b = __ldcg(q + 1), c = __ldcg(q + 2), d = __ldcg(q + 3);
+    p.pos = f3(a.x, a.y, a.z); p.time = a.w;
+    p.mom = f3(b.x, b.y, b.z); p.hitcount_iindex = __float_as_uint(b.w);
+    p.pol = f3(c.x, c.y, c.z); p.wavelength = c.w;
+    p.orient_boundary_flag = __float_as_uint(d.x); p.identity = __float_as_uint(d.y);
+    p.index = __float_as_uint(d.z); p.flagmask = __float_as_uint(d.w);
+}
+
 GBO_DEV void store_photon(gbo_sphoton* s, const Photon& p)
 {
     float4* q = reinterpret_cast<float4*>(s);

@@ -243,10 +243,10 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
                 const long long j = rank < avail ? cbase + cused + rank : (rank - avail < nn ? nb + (rank - avail) : -1);
                 if (j >= 0) {
                     idx = j;
-                    load_photon(p, P.gen_photon + idx);
-                    const ulonglong2 r = P.gen_rng[idx];
+                    load_photon_streamed(p, P.gen_photon + idx);
+                    const ulonglong2 r = __ldcg(P.gen_rng + idx);
                     rng_init(rng, P.seed, r.y, r.x);
-                    hint = P.gen_hint[idx];
+                    hint = __ldcg(P.gen_hint + idx);
                     if (PRECISE) acc_init(acc, p);
                     bounce = 0;
                     if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
