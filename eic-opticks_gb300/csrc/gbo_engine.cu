@@ -204,7 +204,52 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_generate(const __grid_constant__ 
     P.gen_hint[idx] = hint;
 }
 
-template <bool TREE, bool PRECISE>
+// Kernel-mode-2 refill (warp-uniform chunk state cbase, cn, cused): idle lanes take the next pregenerated photons in
+// lane order, the warp claiming POOL_CHUNK more with one atomic when its chunk runs short.
+template <bool PRECISE>
+GBO_DEV void refill_pregenerated(const Params& P, unsigned long long* pool, unsigned idle, unsigned lane, unsigned lt,
+                                 bool& live, long long& idx, Photon& p, Rng& rng, int& hint, Acc64& acc, int& bounce,
+                                 long long& cbase, int& cn, int& cused, bool& pool_open)
+{
+    const int n_idle = __popc(idle), rank = __popc(idle & lt), avail = cn - cused;
+    long long nb = 0;
+    int nn = 0;
+    if (avail < n_idle) {
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(pool, (unsigned long long)POOL_CHUNK);
+        nb = (long long)__shfl_sync(0xffffffffu, b, 0);
+        const long long left = P.num_photon - nb;
+        nn = left <= 0 ? 0 : (left < POOL_CHUNK ? (int)left : POOL_CHUNK);
+    }
+    if (!live) {
+        const long long j = rank < avail ? cbase + cused + rank : (rank - avail < nn ? nb + (rank - avail) : -1);
+        if (j >= 0) {
+            idx = j;
+            load_photon_streamed(p, P.gen_photon + idx);
+            const ulonglong2 r = __ldcg(P.gen_rng + idx);
+            rng_init(rng, P.seed, r.y, r.x);
+            hint = __ldcg(P.gen_hint + idx);
+            if (PRECISE) acc_init(acc, p);
+            bounce = 0;
+            if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
+            live = true;
+        }
+    }
+    if (avail < n_idle) {
+        cbase = nb;
+        cn = nn;
+        cused = n_idle - avail < nn ? n_idle - avail : nn;
+        if (nn == 0) pool_open = false;         // drained: every claimed photon has been handed out
+    } else {
+        cused += n_idle;
+    }
+}
+
+// PREGEN: the kernel-mode-2 form without the generator.  Without a call to the out-of-line generator, its
+// by-reference arguments no longer force the photon state through local memory (5 % faster on the crystal event).
+// The CSG-tree forms keep one kernel for both pool modes (a runtime choice): without the call boundary their
+// register pressure grows into heavy spills.
+template <bool TREE, bool PRECISE, bool PREGEN>
 __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P,
                                                              unsigned long long* pool, int refill_min, int period)
 {
@@ -228,54 +273,27 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
         // other pool mode claims exactly the idle lanes' count and generates them
         const unsigned idle = __ballot_sync(0xffffffffu, !live);
         const bool refill = pool_open && (idle == 0xffffffffu || (it % period == 0 && __popc(idle) >= refill_min));
-        if (refill && P.gen_photon) {
-            const int n_idle = __popc(idle), rank = __popc(idle & lt), avail = cn - cused;
-            long long nb = 0;
-            int nn = 0;
-            if (avail < n_idle) {
-                unsigned long long b = 0;
-                if (lane == 0) b = atomicAdd(pool, (unsigned long long)POOL_CHUNK);
-                nb = (long long)__shfl_sync(0xffffffffu, b, 0);
-                const long long left = P.num_photon - nb;
-                nn = left <= 0 ? 0 : (left < POOL_CHUNK ? (int)left : POOL_CHUNK);
-            }
-            if (!live) {
-                const long long j = rank < avail ? cbase + cused + rank : (rank - avail < nn ? nb + (rank - avail) : -1);
-                if (j >= 0) {
-                    idx = j;
-                    load_photon_streamed(p, P.gen_photon + idx);
-                    const ulonglong2 r = __ldcg(P.gen_rng + idx);
-                    rng_init(rng, P.seed, r.y, r.x);
-                    hint = __ldcg(P.gen_hint + idx);
-                    if (PRECISE) acc_init(acc, p);
-                    bounce = 0;
-                    if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
-                    live = true;
-                }
-            }
-            if (avail < n_idle) {
-                cbase = nb;
-                cn = nn;
-                cused = n_idle - avail < nn ? n_idle - avail : nn;
-                if (nn == 0) pool_open = false;         // drained: every claimed photon has been handed out
-            } else {
-                cused += n_idle;
-            }
-        } else if (refill) {
-            unsigned long long base = 0;
-            const int leader = __ffs(idle) - 1;
-            if ((int)lane == leader) base = atomicAdd(pool, (unsigned long long)__popc(idle));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (base + __popc(idle) >= (unsigned long long)P.num_photon) pool_open = false;
-            if (!live) {
-                const unsigned long long mine = base + __popc(idle & lt);
-                if (mine < (unsigned long long)P.num_photon) {
-                    idx = (long long)mine;
-                    generate(P, idx, p, rng, hint);
-                    if (PRECISE) acc_init(acc, p);
-                    bounce = 0;
-                    if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
-                    live = true;
+        if (PREGEN || P.gen_photon) {
+            if (refill)
+                refill_pregenerated<PRECISE>(P, pool, idle, lane, lt, live, idx, p, rng, hint, acc, bounce, cbase, cn,
+                                             cused, pool_open);
+        } else if constexpr (!PREGEN) {
+            if (refill) {
+                unsigned long long base = 0;
+                const int leader = __ffs(idle) - 1;
+                if ((int)lane == leader) base = atomicAdd(pool, (unsigned long long)__popc(idle));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (base + __popc(idle) >= (unsigned long long)P.num_photon) pool_open = false;
+                if (!live) {
+                    const unsigned long long mine = base + __popc(idle & lt);
+                    if (mine < (unsigned long long)P.num_photon) {
+                        idx = (long long)mine;
+                        generate(P, idx, p, rng, hint);
+                        if (PRECISE) acc_init(acc, p);
+                        bounce = 0;
+                        if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
+                        live = true;
+                    }
                 }
             }
         }
@@ -678,7 +696,12 @@ static void launch_form(const gbo_engine* e, const Params& P, long long n, unsig
         const long long grid = need < e->pool_grid[form] ? need : e->pool_grid[form];
         const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
         const int period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
-        k_simulate_pool<TREE, PRECISE><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
+        bool pregen_form = false;
+        if constexpr (!TREE) pregen_form = P.gen_photon != nullptr;
+        if constexpr (!TREE) {
+            if (pregen_form) k_simulate_pool<TREE, PRECISE, true><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
+        }
+        if (!pregen_form) k_simulate_pool<TREE, PRECISE, false><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
     } else {
         k_simulate<TREE, PRECISE><<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
     }
@@ -864,10 +887,10 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     {
         int sms = 0, b[4] = {0, 0, 0, 0};
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_simulate_pool<false, false>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_simulate_pool<true, false>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_simulate_pool<false, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_simulate_pool<true, true>, SIM_BLOCK, 0) != cudaSuccess) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_simulate_pool<false, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_simulate_pool<true, false, false>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_simulate_pool<false, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_simulate_pool<true, true, false>, SIM_BLOCK, 0) != cudaSuccess) {
             gbo_engine_destroy(e);
             return fail(GBO_ERR_CUDA, "occupancy query failed");
         }

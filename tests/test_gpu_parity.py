@@ -196,11 +196,12 @@ def test_kernel_forms_agree(E):
         assert np.array_equal(s.view(np.uint64), s0.view(np.uint64))
         print("kernel forms: max |dpos| %.3g mm, |dt| %.3g ns, |dvec| %.3g, |dwl| %.3g" % assert_photons_agree(p, p0))
         assert n == n0 and np.array_equal(h["index"], h0["index"])
-    # pregenerated photons (mode 2) run the same pool kernel: the same bytes as generating in the kernel
-    pool = outs[forms.index((0, 1))]
-    for k in (forms.index((2, 1)), forms.index((2, 8))):
-        assert np.array_equal(outs[k][0].view(np.uint32), pool[0].view(np.uint32))
-        assert np.array_equal(outs[k][2].view(np.uint32), pool[2].view(np.uint32))
+    # one compiled kernel gives the same bytes whatever its refill setting (which lane runs a photon, and when,
+    # does not change the photon)
+    for a, b in (((0, 1), (0, 32)), ((2, 1), (2, 8))):
+        pa, pb = outs[forms.index(a)], outs[forms.index(b)]
+        assert np.array_equal(pa[0].view(np.uint32), pb[0].view(np.uint32))
+        assert np.array_equal(pa[2].view(np.uint32), pb[2].view(np.uint32))
 
 
 @pytest.mark.parametrize("max_slot", [500, 1000, 1234])

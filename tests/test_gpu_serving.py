@@ -36,7 +36,7 @@ def test_served_events_equal_alone(E, kind, use_graph, mode):
     geom = G.crystal_array() if kind == "crystal" else G.water_cube()
     arrays = geom.arrays()
     events = make_events(np.random.default_rng(7), 40, kind, wc=geom if kind == "water" else None)
-    eng_alone = E.Engine(arrays)
+    eng_alone = E.Engine(arrays, kernel_mode=mode)       # the same compiled kernel form as the server's
     alone = {}
     for eid, gs in events:
         eng_alone.simulate(eid, gs)
