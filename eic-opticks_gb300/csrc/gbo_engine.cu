@@ -42,7 +42,9 @@ namespace gbo {
                                     // registers) measured 12 % faster than ptxas' unbounded choice on the crystal event
 #endif
 #ifndef GBO_POOL_MINB_TREE
-#define GBO_POOL_MINB_TREE GBO_POOL_MINB   // the pool kernel's form for geometries with CSG trees
+#define GBO_POOL_MINB_TREE 3        // the pool kernel's form for geometries with CSG trees: 3 x 128 threads per SM
+                                    // (168 registers, no spills) measured 3 % faster than 4 (128 registers, 860 B of
+                                    // spills) on the 20,000-sensor event
 #endif
 #ifdef GBO_POOL_MAXNREG                // register budget of the pool kernel instead of its launch bounds
 #define GBO_POOL_BOUNDS __maxnreg__(GBO_POOL_MAXNREG)
@@ -246,9 +248,8 @@ GBO_DEV void refill_pregenerated(const Params& P, unsigned long long* pool, unsi
 }
 
 // PREGEN: the kernel-mode-2 form without the generator.  Without a call to the out-of-line generator, its
-// by-reference arguments no longer force the photon state through local memory (5 % faster on the crystal event).
-// The CSG-tree forms keep one kernel for both pool modes (a runtime choice): without the call boundary their
-// register pressure grows into heavy spills.
+// by-reference arguments no longer force the photon state through local memory (crystal event 751M -> 864M
+// photons/s).
 template <bool TREE, bool PRECISE, bool PREGEN>
 __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P,
                                                              unsigned long long* pool, int refill_min, int period)
@@ -696,12 +697,10 @@ static void launch_form(const gbo_engine* e, const Params& P, long long n, unsig
         const long long grid = need < e->pool_grid[form] ? need : e->pool_grid[form];
         const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
         const int period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
-        bool pregen_form = false;
-        if constexpr (!TREE) pregen_form = P.gen_photon != nullptr;
-        if constexpr (!TREE) {
-            if (pregen_form) k_simulate_pool<TREE, PRECISE, true><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
-        }
-        if (!pregen_form) k_simulate_pool<TREE, PRECISE, false><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
+        if (P.gen_photon)
+            k_simulate_pool<TREE, PRECISE, true><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
+        else
+            k_simulate_pool<TREE, PRECISE, false><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
     } else {
         k_simulate<TREE, PRECISE><<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
     }
@@ -888,9 +887,9 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
         int sms = 0, b[4] = {0, 0, 0, 0};
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_simulate_pool<false, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_simulate_pool<true, false, false>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_simulate_pool<true, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_simulate_pool<false, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_simulate_pool<true, true, false>, SIM_BLOCK, 0) != cudaSuccess) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_simulate_pool<true, true, true>, SIM_BLOCK, 0) != cudaSuccess) {
             gbo_engine_destroy(e);
             return fail(GBO_ERR_CUDA, "occupancy query failed");
         }
