@@ -23,6 +23,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -67,7 +68,7 @@ class ClockSampler:
     def __init__(self, device=0):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks_%d.csv" % os.getpid())
+        self.path = os.path.join(tempfile.gettempdir(), "bench_clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
         try:
