@@ -667,6 +667,8 @@ struct gbo_engine {
     DBuf<gbo_sphoton> hits;
     DBuf<gbo_sphoton> merged;               // hits merged by (identity, time bucket), gbo_merge_hits
     gbo::MergeScratch* merge_scratch = nullptr;     // the merge's work buffers, kept between events
+    gbo_server* event_server = nullptr;             // started by the first gbo_event_submit
+    std::mutex event_server_mu;
     DBuf<gbo_sphoton> gen_photon;           // kernel mode 2: pregenerated photons, their random-stream places and
     DBuf<ulonglong2> gen_rng;               // start instances
     DBuf<int> gen_hint;
@@ -792,6 +794,8 @@ static int make_texture(cudaArray_t* arr, cudaTextureObject_t* tex, const void* 
 void gbo_engine_destroy(gbo_engine* e)
 {
     if (!e) return;
+    if (e->event_server) gbo_server_destroy(e->event_server);
+    e->event_server = nullptr;
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     if (e->bnd_tex) cudaDestroyTextureObject(e->bnd_tex);

@@ -650,4 +650,81 @@ void gbo_server_destroy(gbo_server* sv)
     delete sv;
 }
 
+// ---- event API on the engine handle ----------------------------------------------------------------------------
+
+static gbo_server* engine_event_server(gbo_engine* e)
+{
+    std::lock_guard<std::mutex> lock(e->event_server_mu);
+    if (!e->event_server) {
+        gbo_server_config c;
+        gbo_server_config_default(&c);
+        if (gbo_server_create(e, &c, &e->event_server) != GBO_OK) e->event_server = nullptr;
+    }
+    return e->event_server;
+}
+
+int gbo_event_submit_photons(gbo_engine* e, const gbo_quad6* gs, size_t num_gs, const gbo_sphoton* input_photon,
+                             size_t num_input_photon, uint32_t event_id, gbo_ticket* ticket)
+{
+    if (!e || !ticket) return fail(GBO_ERR_ARG, "gbo_event_submit: null argument");
+    if (event_id > 0x7fffffffu) return fail(GBO_ERR_ARG, "gbo_event_submit: event id %u above 2^31-1", event_id);
+    gbo_server* sv = engine_event_server(e);
+    if (!sv) return GBO_ERR_CUDA;                       // gbo_server_create recorded the reason
+    return gbo_server_submit(sv, (int32_t)event_id, gs, (int64_t)num_gs, input_photon, (int64_t)num_input_photon,
+                             ticket);
+}
+
+int gbo_event_submit(gbo_engine* e, const gbo_quad6* gs, size_t num_gs, uint32_t event_id, gbo_ticket* ticket)
+{
+    return gbo_event_submit_photons(e, gs, num_gs, nullptr, 0, event_id, ticket);
+}
+
+static gbo_server* engine_server_of(gbo_engine* e, const char* what)
+{
+    if (!e) { fail(GBO_ERR_ARG, "%s: null engine", what); return nullptr; }
+    std::lock_guard<std::mutex> lock(e->event_server_mu);
+    if (!e->event_server) fail(GBO_ERR_STATE, "%s: no event submitted", what);
+    return e->event_server;
+}
+
+int gbo_event_wait(gbo_engine* e, gbo_ticket ticket, int64_t timeout_ns)
+{
+    gbo_server* sv = engine_server_of(e, "gbo_event_wait");
+    if (!sv) return e ? GBO_ERR_STATE : GBO_ERR_ARG;
+    // round up so that a positive timeout never becomes a zero one
+    return gbo_server_wait(sv, ticket, timeout_ns < 0 ? -1 : (timeout_ns + 999) / 1000);
+}
+
+int64_t gbo_event_num_hits(gbo_engine* e, gbo_ticket ticket)
+{
+    gbo_server* sv = engine_server_of(e, "gbo_event_num_hits");
+    if (!sv) return -(int64_t)(e ? GBO_ERR_STATE : GBO_ERR_ARG);
+    int64_t n = 0;
+    const int rc = gbo_server_event_info(sv, ticket, nullptr, &n, nullptr);
+    return rc == GBO_OK ? n : -(int64_t)rc;
+}
+
+int gbo_event_copy_hits(gbo_engine* e, gbo_ticket ticket, gbo_sphoton* dst, size_t n)
+{
+    gbo_server* sv = engine_server_of(e, "gbo_event_copy_hits");
+    if (!sv) return e ? GBO_ERR_STATE : GBO_ERR_ARG;
+    return gbo_server_copy_hits(sv, ticket, dst, 0, (int64_t)n);
+}
+
+int gbo_event_release(gbo_engine* e, gbo_ticket ticket)
+{
+    gbo_server* sv = engine_server_of(e, "gbo_event_release");
+    if (!sv) return e ? GBO_ERR_STATE : GBO_ERR_ARG;
+    return gbo_server_release(sv, ticket);
+}
+
+int gbo_geometry_create(const gbo_geometry_desc* g, gbo_geometry** out)
+{
+    gbo_config c;
+    gbo_config_default(&c);
+    return gbo_engine_create(g, &c, 0, out);
+}
+
+void gbo_geometry_destroy(gbo_geometry* g) { gbo_engine_destroy(g); }
+
 }  // extern "C"

@@ -203,6 +203,27 @@ int  gbo_server_release(gbo_server* s, uint64_t ticket);
 int  gbo_server_get_stats(gbo_server* s, gbo_server_stats* out);
 void gbo_server_destroy(gbo_server* s);
 
+/* ---- event API on the engine handle --------------------------------------------------------------------------
+ * The event server through the engine: the first submission starts a server with gbo_server_config_default that
+ * the engine owns (gbo_engine_destroy stops it).  These are the submission / wait / hit-download / release calls a
+ * threaded caller binds in place of SEvt::AddGenstep + G4CXOpticks::simulate + SEvt::GetNumHit / getHit +
+ * G4CXOpticks::reset (sysrap/SEvt.hh:487, g4cx/G4CXOpticks.hh:95-96, sysrap/SEvt.cc:2050, :4991).  Submission is
+ * thread-safe, copies its input and returns at once; timeouts are in nanoseconds (< 0: no limit). */
+typedef uint64_t gbo_ticket;
+int     gbo_event_submit(gbo_engine* e, const gbo_quad6* gs, size_t num_gs, uint32_t event_id, gbo_ticket* ticket);
+int     gbo_event_submit_photons(gbo_engine* e, const gbo_quad6* gs, size_t num_gs, const gbo_sphoton* input_photon,
+                                 size_t num_input_photon, uint32_t event_id, gbo_ticket* ticket);
+int     gbo_event_wait(gbo_engine* e, gbo_ticket ticket, int64_t timeout_ns);       /* GBO_ERR_TIMEOUT: in flight */
+int64_t gbo_event_num_hits(gbo_engine* e, gbo_ticket ticket);                       /* < 0: error (not done, unknown) */
+int     gbo_event_copy_hits(gbo_engine* e, gbo_ticket ticket, gbo_sphoton* dst, size_t n);   /* the first n hits */
+int     gbo_event_release(gbo_engine* e, gbo_ticket ticket);
+
+/* The geometry handle of the drop-in contract is the engine (geometry uploaded to one GPU with its tables):
+ * gbo_geometry_create = gbo_engine_create with gbo_config_default (the OPTICKS_* environment applied) on device 0. */
+typedef struct gbo_engine gbo_geometry;
+int  gbo_geometry_create(const gbo_geometry_desc* g, gbo_geometry** out);
+void gbo_geometry_destroy(gbo_geometry* g);
+
 /* gbo_simulate_noalloc : has no counterpart in the reference.  One event like gbo_simulate_device, for callers
  * that may not allocate device memory while events run (memory reserved up front by another runtime, or event
  * threads on which cudaMalloc/cudaFree must not be called because they synchronise the device).  Gensteps

@@ -58,3 +58,14 @@ def test_engine_create_rejects_bad_geometry(lib):
     lib.gbo_last_error.restype = ctypes.c_char_p
     rc = lib.gbo_engine_create(ctypes.byref(d), None, 0, ctypes.byref(h))
     assert rc == 1 and b"missing" in lib.gbo_last_error()
+
+
+def test_event_api_argument_errors_without_gpu(lib):
+    """The engine-handle event API refuses a null engine before touching the GPU."""
+    lib.gbo_event_num_hits.restype = ctypes.c_int64
+    t = ctypes.c_uint64()
+    assert lib.gbo_event_submit(None, None, ctypes.c_size_t(0), ctypes.c_uint32(1), ctypes.byref(t)) == 1
+    assert lib.gbo_event_wait(None, ctypes.c_uint64(1), ctypes.c_int64(0)) == 1
+    assert lib.gbo_event_num_hits(None, ctypes.c_uint64(1)) < 0
+    assert lib.gbo_event_copy_hits(None, ctypes.c_uint64(1), None, ctypes.c_size_t(0)) == 1
+    assert lib.gbo_event_release(None, ctypes.c_uint64(1)) == 1

@@ -131,3 +131,47 @@ def test_server_input_photons(E, max_batch_photon):
         srv.release(t)
     srv.close()
     eng.close()
+
+
+def test_event_api_on_engine_handle(E):
+    """gbo_event_submit / wait / num_hits / copy_hits / release on the engine handle, from three producer threads:
+    each event's hits equal those of gbo_simulate with the same event id."""
+    import ctypes as C
+    from eic_opticks_gb300 import geometry as G, gensteps as GS
+    arrays = G.crystal_array().arrays()
+    events = [(500 + k, GS.crystal_scint_gensteps(4 + k, 700, seed=90 + k)) for k in range(9)]
+    alone_eng = E.Engine(arrays)
+    alone = {}
+    for eid, gs in events:
+        alone_eng.simulate(eid, gs)
+        alone[eid] = alone_eng.hits()
+    alone_eng.close()
+    eng = E.Engine(arrays)
+    lib = eng.lib
+    lib.gbo_event_num_hits.restype = C.c_int64
+    tickets, lock = {}, threading.Lock()
+
+    def producer(chunk):
+        for eid, gs in chunk:
+            t = C.c_uint64()
+            g = np.ascontiguousarray(gs)
+            rc = lib.gbo_event_submit(eng.handle, g.ctypes.data_as(C.c_void_p), C.c_size_t(len(g)), C.c_uint32(eid),
+                                      C.byref(t))
+            assert rc == 0
+            with lock:
+                tickets[eid] = t.value
+
+    threads = [threading.Thread(target=producer, args=(events[i::3],)) for i in range(3)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    for eid, t in tickets.items():
+        assert lib.gbo_event_wait(eng.handle, C.c_uint64(t), C.c_int64(60_000_000_000)) == 0
+        n = lib.gbo_event_num_hits(eng.handle, C.c_uint64(t))
+        assert n == len(alone[eid])
+        got = np.zeros(n, dtype=alone[eid].dtype)
+        assert lib.gbo_event_copy_hits(eng.handle, C.c_uint64(t), got.ctypes.data_as(C.c_void_p), C.c_size_t(n)) == 0
+        assert np.array_equal(got.view(np.uint32), alone[eid].view(np.uint32)), eid
+        assert lib.gbo_event_release(eng.handle, C.c_uint64(t)) == 0
+    eng.close()
