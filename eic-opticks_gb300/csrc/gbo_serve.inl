@@ -573,7 +573,7 @@ int gbo_server_wait(gbo_server* sv, uint64_t ticket, int64_t timeout_us)
     if (it == sv->events.end()) return fail(GBO_ERR_ARG, "gbo_server_wait: unknown ticket %llu", (unsigned long long)ticket);
     std::shared_ptr<ServerEvent> ev = it->second;
     auto done = [&] { return ev->status >= 2; };
-    if (timeout_us < 0) sv->cv_done.wait(lock, done);
+    if (timeout_us < 0 || timeout_us > (1ll << 40)) sv->cv_done.wait(lock, done);      // beyond ~12 days: no limit
     else if (!sv->cv_done.wait_for(lock, std::chrono::microseconds(timeout_us), done))
         return fail(GBO_ERR_TIMEOUT, "gbo_server_wait: event %llu not done", (unsigned long long)ticket);
     if (ev->status == 3) return fail(GBO_ERR_DEVICE, "event %llu failed: %s", (unsigned long long)ticket, ev->error.c_str());
@@ -692,7 +692,8 @@ int gbo_event_wait(gbo_engine* e, gbo_ticket ticket, int64_t timeout_ns)
     gbo_server* sv = engine_server_of(e, "gbo_event_wait");
     if (!sv) return e ? GBO_ERR_STATE : GBO_ERR_ARG;
     // round up so that a positive timeout never becomes a zero one
-    return gbo_server_wait(sv, ticket, timeout_ns < 0 ? -1 : (timeout_ns + 999) / 1000);
+    const int64_t us = timeout_ns < 0 ? -1 : timeout_ns / 1000 + (timeout_ns % 1000 != 0 ? 1 : 0);
+    return gbo_server_wait(sv, ticket, us);
 }
 
 int64_t gbo_event_num_hits(gbo_engine* e, gbo_ticket ticket)
