@@ -10,19 +10,26 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "g4cx_example.cc")
 
 
-def compile_example(out_dir):
+def compile_example(out_dir, src=SRC, name="g4cx_example", extra=()):
     import __graft_entry__ as ge
     ge.load_package()
     from eic_opticks_gb300 import build
     lib = build.build()
-    exe = os.path.join(out_dir, "g4cx_example")
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), SRC, "-o", exe,
-                           lib, "-Wl,-rpath," + os.path.dirname(lib)])
+    exe = os.path.join(out_dir, name)
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), src, "-o", exe,
+                           lib, "-Wl,-rpath," + os.path.dirname(lib), *extra])
     return exe
 
 
 def test_cpp_interface_compiles(tmp_path):
     exe = compile_example(str(tmp_path))
+    assert os.path.exists(exe)
+
+
+def test_event_api_example_compiles(tmp_path):
+    """The engine-handle event API as a C caller binds it (tests/cpp/event_api_example.cc) compiles and links."""
+    exe = compile_example(str(tmp_path), os.path.join(ROOT, "tests", "cpp", "event_api_example.cc"),
+                          "event_api_example", ["-pthread"])
     assert os.path.exists(exe)
 
 
