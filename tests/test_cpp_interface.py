@@ -56,3 +56,24 @@ def test_cpp_interface_matches_python_binding(tmp_path):
     eng.close()
     assert int(out[1]) == n > 0
     assert int(out[3]) == hits["index"][0] and int(out[5]) == hits["index"][-1]
+
+
+@pytest.mark.gpu
+def test_event_api_example_matches_python_binding(tmp_path):
+    """The C event-API example (four events from two threads) gives each event the hit count and first hit of
+    gbo_simulate with the same event id."""
+    from eic_opticks_gb300 import engine as E, geometry as G, gensteps as GS
+    arrays = G.crystal_array().arrays()
+    gs = GS.crystal_scint_gensteps(12, 600, seed=6)
+    exe = compile_example(str(tmp_path), os.path.join(ROOT, "tests", "cpp", "event_api_example.cc"),
+                          "event_api_example", ["-pthread"])
+    write_inputs(str(tmp_path), arrays, gs, 20)
+    lines = subprocess.check_output([exe, str(tmp_path)]).decode().strip().splitlines()
+    assert len(lines) == 4
+    eng = E.Engine(arrays)
+    for line in lines:
+        w = line.split()
+        eid, n, first = int(w[1]), int(w[3]), int(w[6])
+        assert eng.simulate(eid, gs) == n > 0
+        assert eng.hits()["index"][0] == first
+    eng.close()
