@@ -37,16 +37,30 @@ METRIC = "propagated photons/s, batched vs plain per-event launch on 1 GB300; p9
 UNIT = "photons/s"
 WORKLOAD = "crystal_array_8x8_CsI_scint_2000gs_poisson5000"
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) per photon of the simulate kernel from one ncu capture of a 998,319-photon crystal-array
-# event (200 gensteps), scaled to the benchmark event by its photon count: gensteps in, hits and hit bitmap out,
-# the only DRAM traffic, all grow with the photons
-# ncu DRAM bytes (read + write) per photon of the simulate kernels on the crystal event, scaled by photons:
-# one thread per photon (k_simulate, 1M-photon event), and the pregenerated pool (k_generate + k_simulate_pool,
-# 2.5M-photon event: 0.22 + 182.10 MB and 210.98 + 2.46 MB, larger than L2)
+# ncu DRAM bytes (read + write) per photon of the simulate kernels on the crystal event, scaled to the benchmark
+# event by its photon count (all of it grows with the photons): one thread per photon (k_simulate, 1M-photon event:
+# gensteps in, hits and hit bitmap out), and the pregenerated pool (k_generate + k_simulate_pool, 2.5M-photon event:
+# 0.22 + 182.10 MB and 210.98 + 2.46 MB, larger than L2)
 TRAFFIC_B_PER_PHOTON = {("crystal_array", 1): (443392.0 + 840192.0) / 998319,
                         ("crystal_array", 2): (0.22e6 + 182.10e6 + 210.98e6 + 2.46e6) / 2499792}
 TRAFFIC_SOURCE = {1: "profiles/k_simulate_crystal_array.md (ncu, 1M-photon event, scaled by photons)",
                   2: "profiles/k_simulate_pool_pregen_crystal_array.md (ncu, 2.5M-photon event, scaled by photons)"}
+
+
+def pinned_photons(n):
+    """A host array of n photon records in page-locked memory (the destination of the end-to-end hit download);
+    pageable memory if the allocator cannot pin it."""
+    import torch
+    from eic_opticks_gb300 import engine as E
+    try:
+        buf = torch.empty(n * E.L.PHOTON.itemsize, dtype=torch.uint8, pin_memory=True)
+    except RuntimeError:
+        return np.zeros(n, dtype=E.L.PHOTON)
+    pinned_photons.keep.append(buf)             # the tensor owns the memory: keep it alive with the array
+    return buf.numpy().view(E.L.PHOTON)
+
+
+pinned_photons.keep = []
 
 
 def peaks():
@@ -519,7 +533,7 @@ def main():
         t0 = time.perf_counter()
         nh = eng.simulate(2000 + k, gs, inp)
         if hits_host is None or len(hits_host) < nh:
-            hits_host = np.zeros(max(nh, 1) * 2, dtype=E.L.PHOTON)
+            hits_host = pinned_photons(max(nh, 1) * 2)
         eng.hits(out=hits_host[:nh])
         dt = time.perf_counter() - t0
         if k >= args.warmup:
