@@ -65,17 +65,18 @@ def torch_gensteps(num_gs, photons_per_gs, torch_type=L.T_DISC, pos=(0.0, 0.0, -
     gu[:, 0, 0] = L.GS_TORCH
     gu[:, 0, 3] = photons_per_gs
     m = np.asarray(mom, dtype=np.float32)
-    m = m / np.float32(np.sqrt(np.float32(m @ m)))
+    dot = np.float32(m[0] * m[0]) + np.float32(m[1] * m[1]) + np.float32(m[2] * m[2])
+    m = m * (np.float32(1.0) / np.sqrt(np.float32(dot)))       # normalize(float3), sysrap/scuda.h:606-610
     g[:, 1, 0:3] = pos
     g[:, 1, 3] = time
     g[:, 2, 0:3] = m
-    g[:, 2, 3] = 1.0
+    g[:, 2, 3] = 0.0                    # weight (FillGenstep default "0")
     g[:, 3, 3] = wavelength
     g[:, 4, 0:2] = zenith
     g[:, 4, 2:4] = azimuth
     g[:, 5, 0] = radius
     g[:, 5, 1] = distance
-    gu[:, 5, 2] = 0
+    gu[:, 5, 2] = 255                   # mode (FillGenstep sets 255)
     gu[:, 5, 3] = torch_type
     return g
 

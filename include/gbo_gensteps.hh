@@ -20,6 +20,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -158,6 +159,92 @@ inline gbo_quad6 MakeGenstep_Cerenkov_FromTable(const TrackInfo& t, const StepPo
     const double m2 = CerenkovMeanPhotonsPerMM(t.charge, beta_post, energy_eV, rindex, n) * step;
     return MakeGenstep_G4Cerenkov_modified(t, s, matline, numPhotons, bi, energy_eV[0], energy_eV[n - 1], maxCos,
                                            (1.0 - maxCos) * (1.0 + maxCos), m1, m2);
+}
+
+// ---- torch gensteps : storch::FillGenstep (sysrap/storch.h:104-146) ----------------------------------------------
+// The reference's test and demo gensteps: every field from an environment key with the same default
+// (storch_FillGenstep_pos "0,0,-90", _time "0.0", _mom "0,0,1" then normalized in binary32, _wavelength "420",
+// _distance "0", _weight "0", _zenith "0,1", _azimuth "0,1", _radius "50", _type "disc"; mode 255).  Type names
+// as sysrap/storchtype.h: undef disc line point circle rectangle sphere_marsaglia sphere.
+
+struct TorchParams {
+    float pos[3] = {0.f, 0.f, -90.f};
+    float time = 0.f;
+    float mom[3] = {0.f, 0.f, 1.f};
+    float weight = 0.f;
+    float wavelength = 420.f;
+    float zenith[2] = {0.f, 1.f};
+    float azimuth[2] = {0.f, 1.f};
+    float radius = 50.f;
+    float distance = 0.f;
+    uint32_t type = GBO_T_DISC;
+};
+
+inline uint32_t TorchType(const char* name)
+{
+    static const char* names[] = {"undef", "disc", "line", "point", "circle", "rectangle", "sphere_marsaglia", "sphere"};
+    for (uint32_t k = 0; k < 8; k++)
+        if (std::strcmp(name, names[k]) == 0) return k;
+    return 0;
+}
+
+namespace detail {
+// comma-separated values of an environment key into v[0..n) (missing values keep their defaults)
+inline void env_floats(const char* key, float* v, int n)
+{
+    const char* s = std::getenv(key);
+    if (!s) return;
+    for (int k = 0; k < n && *s; k++) {
+        char* end = nullptr;
+        const float x = std::strtof(s, &end);
+        if (end == s) break;
+        v[k] = x;
+        s = *end == ',' ? end + 1 : end;
+    }
+}
+}  // namespace detail
+
+// the parameters with the reference's storch_FillGenstep_* environment overrides applied; type 0 (undef) when
+// storch_FillGenstep_type names no torch type (the reference asserts)
+inline TorchParams TorchParamsFromEnv()
+{
+    TorchParams p;
+    detail::env_floats("storch_FillGenstep_pos", p.pos, 3);
+    detail::env_floats("storch_FillGenstep_time", &p.time, 1);
+    detail::env_floats("storch_FillGenstep_mom", p.mom, 3);
+    detail::env_floats("storch_FillGenstep_wavelength", &p.wavelength, 1);
+    detail::env_floats("storch_FillGenstep_distance", &p.distance, 1);
+    detail::env_floats("storch_FillGenstep_weight", &p.weight, 1);
+    detail::env_floats("storch_FillGenstep_zenith", p.zenith, 2);
+    detail::env_floats("storch_FillGenstep_azimuth", p.azimuth, 2);
+    detail::env_floats("storch_FillGenstep_radius", &p.radius, 1);
+    if (const char* t = std::getenv("storch_FillGenstep_type")) p.type = TorchType(t);
+    return p;
+}
+
+inline gbo_quad6 MakeGenstep_Torch(const TorchParams& p, int32_t numphoton)
+{
+    gbo_quad6 g;
+    std::memset(&g, 0, sizeof(g));
+    detail::put_u(g, 0, 0, GBO_GS_TORCH);
+    detail::put_i(g, 0, 3, numphoton);
+    for (int k = 0; k < 3; k++) g.q[1].f[k] = p.pos[k];
+    g.q[1].f[3] = p.time;
+    // normalize(float3) of the reference's smath: binary32 components over the binary32 length
+    const float len = std::sqrt(p.mom[0] * p.mom[0] + p.mom[1] * p.mom[1] + p.mom[2] * p.mom[2]);
+    const float inv = 1.f / len;
+    for (int k = 0; k < 3; k++) g.q[2].f[k] = p.mom[k] * inv;
+    g.q[2].f[3] = p.weight;
+    g.q[3].f[3] = p.wavelength;
+    g.q[4].f[0] = p.zenith[0];
+    g.q[4].f[1] = p.zenith[1];
+    g.q[4].f[2] = p.azimuth[0];
+    g.q[4].f[3] = p.azimuth[1];
+    g.q[5].f[0] = p.radius;
+    g.q[5].f[1] = p.distance;
+    detail::put_u(g, 5, 2, 255u);
+    detail::put_u(g, 5, 3, p.type);
+    return g;
 }
 
 }  // namespace gbo

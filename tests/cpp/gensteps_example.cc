@@ -1,5 +1,6 @@
-// Writes gensteps made by include/gbo_gensteps.hh for fixed step values, and the Cerenkov yield on a table, to
-// the directory given as argv[1] (gs.bin: quad6 records; yield.txt: photons per mm at several betas).
+// Writes gensteps made by include/gbo_gensteps.hh for fixed step values (scintillation, Cerenkov, and a torch
+// genstep from the storch_FillGenstep_* environment), and the Cerenkov yield on a table, to the directory given as
+// argv[1] (gs.bin: quad6 records; yield.txt: photons per mm at several betas).
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -25,6 +26,7 @@ int main(int argc, char** argv)
     std::vector<gbo_quad6> gs;
     gs.push_back(gbo::MakeGenstep_DsG4Scintillation_r4695(t, s, 11, 4321, 1, 12.5));
     gs.push_back(gbo::MakeGenstep_Cerenkov_FromTable(t, s, 7, 55, e.data(), n.data(), (int)n.size()));
+    gs.push_back(gbo::MakeGenstep_Torch(gbo::TorchParamsFromEnv(), 1000));      // storch_FillGenstep_* from the env
     FILE* f = std::fopen((dir + "/gs.bin").c_str(), "wb");
     std::fwrite(gs.data(), sizeof(gbo_quad6), gs.size(), f);
     std::fclose(f);

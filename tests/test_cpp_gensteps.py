@@ -8,11 +8,13 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def run_example(tmp):
+def run_example(tmp, env=None):
     exe = os.path.join(tmp, "gensteps_example")
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
                            os.path.join(ROOT, "tests", "cpp", "gensteps_example.cc"), "-o", exe])
-    subprocess.check_call([exe, tmp])
+    e = {k: v for k, v in os.environ.items() if not k.startswith("storch_FillGenstep_")}
+    e.update(env or {})
+    subprocess.check_call([exe, tmp], env=e)
     gs = np.fromfile(os.path.join(tmp, "gs.bin"), dtype=np.float32).reshape(-1, 6, 4)
     y = np.loadtxt(os.path.join(tmp, "yield.txt"))
     return gs, y
@@ -62,3 +64,21 @@ def test_cerenkov_yield_against_fine_integration(tmp_path):
         want = fine_yield(beta, e, n)
         assert abs(got - want) <= 1e-4 * max(want, 1e-3) + 1e-6, (beta, got, want)
     assert y[0, 1] == 0.0                                   # below threshold (beta n < 1 everywhere)
+
+
+def test_torch_genstep_defaults_and_environment(tmp_path):
+    """MakeGenstep_Torch(TorchParamsFromEnv()) : storch::FillGenstep's fields, defaults and environment keys
+    (sysrap/storch.h:104-146), the same record as the Python torch_gensteps with those parameters."""
+    from eic_opticks_gb300 import gensteps as GS, layout as L
+    gs, _ = run_example(str(tmp_path))
+    want = GS.torch_gensteps(1, 1000)
+    assert np.array_equal(gs[2].view(np.uint32), want[0].view(np.uint32))
+    env = {"storch_FillGenstep_pos": "1,2,3", "storch_FillGenstep_mom": "0,3,4", "storch_FillGenstep_type": "sphere",
+           "storch_FillGenstep_radius": "7.5", "storch_FillGenstep_wavelength": "500", "storch_FillGenstep_zenith": "0.1,0.2",
+           "storch_FillGenstep_time": "2.5"}
+    gs, _ = run_example(str(tmp_path), env)
+    want = GS.torch_gensteps(1, 1000, torch_type=L.T_SPHERE, pos=(1, 2, 3), mom=(0, 3, 4), wavelength=500.0,
+                             radius=7.5, zenith=(0.1, 0.2), time=2.5)
+    assert np.array_equal(gs[2].view(np.uint32), want[0].view(np.uint32))
+    gs, _ = run_example(str(tmp_path), {"storch_FillGenstep_type": "nonsense"})
+    assert gs[2].view(np.uint32)[5, 3] == 0                        # undef: the reference asserts on it
