@@ -56,6 +56,51 @@ def isotropic_photons(n, wavelength=420.0, seed=42, origin=(0.0, 0.0, 0.0)):
     return p
 
 
+def load_photons_txt(path):
+    """Input photons from a text file as the reference's photon-file source reads them (src/GPUPhotonFileSource.h
+    load_photons_txt): one photon per line, 11 values ``pos_x pos_y pos_z time mom_x mom_y mom_z pol_x pol_y pol_z
+    wavelength``; blank lines and lines starting with '#' skipped, lines that do not start with 11 numbers skipped
+    (extra tokens after them are ignored, as the stream extraction ignores them).  Other fields are zero."""
+    rows = []
+    with open(path) as f:
+        for line in f:
+            line = line.rstrip("\n")
+            if not line or line[0] == "#":
+                continue
+            tok = line.split()
+            try:
+                v = [float(t) for t in tok[:11]]
+            except ValueError:
+                continue
+            if len(v) == 11:
+                rows.append(v)
+    p = np.zeros(len(rows), dtype=L.PHOTON)
+    if rows:
+        a = np.asarray(rows, dtype=np.float32)
+        p["pos"] = a[:, 0:3]
+        p["time"] = a[:, 3]
+        p["mom"] = a[:, 4:7]
+        p["pol"] = a[:, 7:10]
+        p["wavelength"] = a[:, 10]
+    return p
+
+
+def _g(x):
+    """A number as C++ iostream writes a double by default (6 significant digits, %g)."""
+    return "%g" % float(x)
+
+
+def write_hits_txt(hits, path):
+    """Hits in the text format of the reference's photon-file application (src/GPUPhotonFileSource.h
+    EndOfEventAction): ``time wavelength  (x, y, z)  (mx, my, mz)  (px, py, pz)`` per line."""
+    with open(path, "w") as f:
+        for h in hits:
+            pos, mom, pol = h["pos"], h["mom"], h["pol"]
+            f.write("%s %s  (%s, %s, %s)  (%s, %s, %s)  (%s, %s, %s)\n" % (
+                _g(h["time"]), _g(h["wavelength"]), _g(pos[0]), _g(pos[1]), _g(pos[2]),
+                _g(mom[0]), _g(mom[1]), _g(mom[2]), _g(pol[0]), _g(pol[1]), _g(pol[2])))
+
+
 def torch_gensteps(num_gs, photons_per_gs, torch_type=L.T_DISC, pos=(0.0, 0.0, -90.0), mom=(0.0, 0.0, 1.0),
                    wavelength=420.0, radius=50.0, zenith=(0.0, 1.0), azimuth=(0.0, 1.0), distance=0.0, time=0.0):
     """Torch gensteps with storch.h fields: pos/time, mom/weight, pol/wavelength, zenith, azimuth,

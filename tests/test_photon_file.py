@@ -1,0 +1,37 @@
+"""Input-photon text files and the hit text format of the reference's photon-file application
+(src/GPUPhotonFileSource.h): the C++ header (include/gbo_photon_file.hh) and the Python helpers
+(eic_opticks_gb300.gensteps) read and write the same records."""
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+SAMPLE = """# x y z t mx my mz px py pz wl
+-10 -30 -90 0 0 0.287348 0.957826 1 0 0 420
+
+-10 -30 -90 0.5 0 0.287348 0.957826 1 0 0 450 trailing
+not a photon line
+1e-3 2.5 -3.25 1.25e2 0.6 0.8 0 0 0 1 399.5
+1 2 3
+"""
+
+
+def test_photon_file_roundtrip(tmp_path):
+    from eic_opticks_gb300 import gensteps as GS, layout as L
+    src = tmp_path / "photons.txt"
+    src.write_text(SAMPLE)
+    exe = str(tmp_path / "photon_file_example")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", "cpp", "photon_file_example.cc"), "-o", exe])
+    subprocess.check_call([exe, str(src), str(tmp_path / "p.bin"), str(tmp_path / "hits_cpp.txt")])
+    cpp = np.fromfile(str(tmp_path / "p.bin"), dtype=L.PHOTON)
+    py = GS.load_photons_txt(str(src))
+    assert len(py) == len(cpp) == 3
+    assert np.array_equal(py.view(np.uint32), cpp.view(np.uint32))
+    assert py["wavelength"][1] == np.float32(450) and py["time"][2] == np.float32(125.0)
+    GS.write_hits_txt(py, str(tmp_path / "hits_py.txt"))
+    assert (tmp_path / "hits_py.txt").read_text() == (tmp_path / "hits_cpp.txt").read_text()
+    assert (tmp_path / "hits_py.txt").read_text().splitlines()[0] == \
+        "0 420  (-10, -30, -90)  (0, 0.287348, 0.957826)  (1, 0, 0)"
