@@ -101,6 +101,37 @@ def write_hits_txt(hits, path):
                 _g(mom[0]), _g(mom[1]), _g(mom[2]), _g(pol[0]), _g(pol[1]), _g(pol[2])))
 
 
+TORCH_TYPES = {"disc": L.T_DISC, "line": L.T_LINE, "point": L.T_POINT, "circle": L.T_CIRCLE,
+               "rectangle": L.T_RECTANGLE, "sphere_marsaglia": L.T_SPHERE_MARSAGLIA, "sphere": L.T_SPHERE}
+
+
+def torch_genstep_from_config(path):
+    """The torch genstep and event settings of a reference application config file (config/*.json, read by
+    gphox::Config::ReadConfig, src/config.cpp): ``torch`` gives every storch field (gentype, trackid, matline,
+    numphoton, pos, time, mom (normalized in binary32), weight, pol, wavelength, zenith, azimuth, radius, distance,
+    mode, type by name), ``event`` the event mode and maxslot.  Returns (gensteps (1,6,4) float32, event dict)."""
+    import json
+    with open(path) as f:
+        cfg = json.load(f)
+    t = cfg["torch"]
+    if t.get("gentype", "TORCH") != "TORCH":
+        raise ValueError("torch.gentype %r is not TORCH" % t.get("gentype"))
+    if t["type"] not in TORCH_TYPES:
+        raise ValueError("torch.type %r is not a torch type" % t["type"])
+    g = torch_gensteps(1, int(t["numphoton"]), torch_type=TORCH_TYPES[t["type"]], pos=tuple(t["pos"]),
+                       mom=tuple(t["mom"]), wavelength=float(t["wavelength"]), radius=float(t["radius"]),
+                       zenith=tuple(t["zenith"]), azimuth=tuple(t["azimuth"]), distance=float(t["distance"]),
+                       time=float(t["time"]))
+    gu = g.view(np.uint32)
+    gu[0, 0, 1] = int(t.get("trackid", 0))
+    gu[0, 0, 2] = int(t.get("matline", 0))
+    g[0, 2, 3] = float(t.get("weight", 0.0))
+    g[0, 3, 0:3] = t.get("pol", (0.0, 0.0, 0.0))
+    gu[0, 5, 2] = int(t.get("mode", 255))
+    ev = cfg.get("event", {})
+    return g, {"mode": ev.get("mode"), "maxslot": ev.get("maxslot")}
+
+
 def torch_gensteps(num_gs, photons_per_gs, torch_type=L.T_DISC, pos=(0.0, 0.0, -90.0), mom=(0.0, 0.0, 1.0),
                    wavelength=420.0, radius=50.0, zenith=(0.0, 1.0), azimuth=(0.0, 1.0), distance=0.0, time=0.0):
     """Torch gensteps with storch.h fields: pos/time, mom/weight, pol/wavelength, zenith, azimuth,

@@ -35,3 +35,28 @@ def test_photon_file_roundtrip(tmp_path):
     assert (tmp_path / "hits_py.txt").read_text() == (tmp_path / "hits_cpp.txt").read_text()
     assert (tmp_path / "hits_py.txt").read_text().splitlines()[0] == \
         "0 420  (-10, -30, -90)  (0, 0.287348, 0.957826)  (1, 0, 0)"
+
+
+CONFIG = """{
+  "torch": {"gentype": "TORCH", "trackid": 3, "matline": 5, "numphoton": 250,
+            "pos": [1.0, -2.0, 4.5], "time": 0.25, "mom": [0.0, 3.0, 4.0], "weight": 0.0,
+            "pol": [1.0, 0.0, 0.0], "wavelength": 440.0, "zenith": [0.0, 1.0], "azimuth": [0.0, 1.0],
+            "radius": 2.5, "distance": 0.0, "mode": 255, "type": "circle"},
+  "event": {"mode": "Minimal", "maxslot": 12345}
+}"""
+
+
+def test_torch_genstep_from_config(tmp_path):
+    """A reference application config (gphox::Config::ReadConfig layout) gives the storch genstep field by field."""
+    from eic_opticks_gb300 import gensteps as GS, layout as L
+    p = tmp_path / "cfg.json"
+    p.write_text(CONFIG)
+    g, ev = GS.torch_genstep_from_config(str(p))
+    u = g.view(np.uint32)
+    assert g.shape == (1, 6, 4) and ev == {"mode": "Minimal", "maxslot": 12345}
+    assert list(u[0, 0]) == [L.GS_TORCH, 3, 5, 250]
+    assert list(g[0, 1]) == [1.0, -2.0, 4.5, 0.25]
+    assert np.array_equal(g[0, 2, :3], np.array([0.0, 0.6, 0.8], dtype=np.float32)) and g[0, 2, 3] == 0.0
+    assert list(g[0, 3]) == [1.0, 0.0, 0.0, 440.0]
+    assert list(g[0, 4]) == [0.0, 1.0, 0.0, 1.0]
+    assert g[0, 5, 0] == 2.5 and g[0, 5, 1] == 0.0 and u[0, 5, 2] == 255 and u[0, 5, 3] == L.T_CIRCLE
