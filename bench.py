@@ -43,8 +43,8 @@ L2_FLUSH_BYTES = 256 << 20
 # 0.22 + 182.10 MB and 210.98 + 2.46 MB, larger than L2)
 TRAFFIC_B_PER_PHOTON = {("crystal_array", 1): (443392.0 + 840192.0) / 998319,
                         ("crystal_array", 2): (0.22e6 + 182.10e6 + 210.98e6 + 2.46e6) / 2499792}
-TRAFFIC_SOURCE = {1: "profiles/k_simulate_crystal_array.md (ncu, 1M-photon event, scaled by photons)",
-                  2: "profiles/k_simulate_pool_pregen_crystal_array.md (ncu, 2.5M-photon event, scaled by photons)"}
+TRAFFIC_SOURCE = {1: "ncu DRAM bytes of k_simulate on a 1M-photon crystal event, scaled by photons",
+                  2: "ncu DRAM bytes of k_generate + k_simulate_pool on a 2.5M-photon crystal event, scaled by photons"}
 
 
 def pinned_photons(n):

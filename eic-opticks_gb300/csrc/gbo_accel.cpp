@@ -77,12 +77,16 @@ struct Builder {
             nodes[self].count = n;
             return self;
         }
-        // binned SAH, 32 bins on each axis with a centroid spread; the cheapest split over the three axes
+        // binned SAH, 32 bins on each axis with a centroid spread; the cheapest split over the three axes; deep in
+        // the tree a median split on the widest centroid axis, which bounds the remaining depth by log2(n)
         int mid = begin + n / 2;
         int axis = 0;
         for (int k = 1; k < 3; k++) if (cb.hi[k] - cb.lo[k] > cb.hi[axis] - cb.lo[axis]) axis = k;
         if (forced_mid > begin && forced_mid < end) {
             mid = forced_mid;
+        } else if (depth >= TLAS_MEDIAN_DEPTH) {
+            std::nth_element(index.begin() + begin, index.begin() + mid, index.begin() + end,
+                             [&](int32_t a, int32_t c) { return boxes[a].centroid(axis) < boxes[c].centroid(axis); });
         } else if (cb.hi[axis] - cb.lo[axis] > 0.0) {
             constexpr int NB = 32;
             double best = 1e300;
@@ -391,6 +395,11 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
     out.tlas.reserve(2 * num_inst);
     b.build(0, num_inst, 0, num_big > 0 && num_big < num_inst ? num_big : -1);
     out.max_depth = b.max_depth;
+    if (out.max_depth > TLAS_STACK_DEPTH) {
+        std::snprintf(err, errlen, "instance tree depth %d exceeds the %d-entry traversal stack", out.max_depth,
+                      TLAS_STACK_DEPTH);
+        return 1;
+    }
 
     // two-child-box form: node k of tlas2 corresponds to inner node map[k] of tlas
     const std::vector<BvhNode>& t = out.tlas;

@@ -23,6 +23,13 @@
 
 namespace gbo {
 
+// Entries of the per-ray traversal stack.  A walk pushes at most one entry per inner node on its path, so a TLAS
+// whose deepest leaf sits at depth <= TLAS_STACK_DEPTH never overflows it; the builder switches to median splits
+// below TLAS_MEDIAN_DEPTH (at most 16 further levels for the 65,536-instance limit) and refuses any tree deeper
+// than the stack, so no subtree is ever dropped.
+constexpr int TLAS_STACK_DEPTH = 64;
+constexpr int TLAS_MEDIAN_DEPTH = 40;
+
 struct BvhNode {
     float bmin[3];
     int32_t left_first;

@@ -184,7 +184,10 @@ GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng, int& 
         case GBO_GS_G4Cerenkov_modified: gen_cerenkov(P.tab, p, rng, gq); break;
         case GBO_GS_SCINTILLATION:
         case GBO_GS_DsG4Scintillation_r4695: gen_scint(P.tab, p, rng, gq); break;
-        case GBO_GS_INPUT_PHOTON: load_photon(p, P.input_photon + idx); set_flag(p, GBO_TORCH); break;
+        case GBO_GS_INPUT_PHOTON:
+            if (P.input_photon) { load_photon(p, P.input_photon + idx); set_flag(p, GBO_TORCH); }
+            else { set_flag(p, GBO_NAN_ABORT); p.time = __int_as_float(0x7f800000); }   // hosts refuse this case
+            break;
         default: break;
     }
     set_index(p, photon_idx);
@@ -385,16 +388,21 @@ __global__ void k_genstep_hint(Accel a, const float4* gs, int num_gs, int* hint)
     hint[g] = best;
 }
 
-__global__ void k_genstep_prefix(const gbo_quad6* gs, int num_gs, unsigned long long* gs_end)
+// input_gs (may be null) receives 1 when any genstep is an INPUT_PHOTON genstep, else 0: the host then checks that
+// input photons were given for every photon slot before any photon is generated
+__global__ void k_genstep_prefix(const gbo_quad6* gs, int num_gs, unsigned long long* gs_end,
+                                 unsigned long long* input_gs)
 {
     // single block: chunked inclusive scan of numphoton
     __shared__ unsigned long long buf[1024];
     __shared__ unsigned long long carry;
-    if (threadIdx.x == 0) carry = 0ull;
+    __shared__ int any_input;
+    if (threadIdx.x == 0) { carry = 0ull; any_input = 0; }
     __syncthreads();
     for (int base = 0; base < num_gs; base += blockDim.x) {
         const int i = base + threadIdx.x;
         unsigned long long v = i < num_gs ? (unsigned long long)gs[i].q[0].u[3] : 0ull;
+        if (i < num_gs && gs[i].q[0].i[0] == GBO_GS_INPUT_PHOTON) any_input = 1;
         buf[threadIdx.x] = v;
         __syncthreads();
         for (int off = 1; off < (int)blockDim.x; off <<= 1) {
@@ -408,6 +416,7 @@ __global__ void k_genstep_prefix(const gbo_quad6* gs, int num_gs, unsigned long 
         if (threadIdx.x == blockDim.x - 1) carry += buf[threadIdx.x];
         __syncthreads();
     }
+    if (input_gs && threadIdx.x == 0) *input_gs = any_input ? 1ull : 0ull;
 }
 
 __global__ void k_word_prefix(const uint32_t* bitmap, long long words, uint32_t* word_prefix, uint32_t* block_sum)
@@ -1139,7 +1148,15 @@ int gbo_simulate_slice(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int
     CU(cudaSetDevice(e->device));
     std::vector<unsigned long long> end((size_t)num_gs);
     unsigned long long total = 0;
-    for (int64_t i = 0; i < num_gs; i++) { total += gs[i].q[0].u[3]; end[(size_t)i] = total; }
+    bool has_input_gs = false;
+    for (int64_t i = 0; i < num_gs; i++) {
+        total += gs[i].q[0].u[3];
+        end[(size_t)i] = total;
+        if (gs[i].q[0].i[0] == GBO_GS_INPUT_PHOTON) has_input_gs = true;
+    }
+    if (has_input_gs && (long long)num_input_photon < (long long)total)
+        return fail(GBO_ERR_ARG, "gbo_simulate_slice: INPUT_PHOTON gensteps need %llu photons, %lld given", total,
+                    (long long)num_input_photon);
     cudaStream_t s = e->stream;
     CU(cudaEventRecord(e->ev[0], s));
     int rc;
@@ -1158,19 +1175,24 @@ int gbo_simulate_device(gbo_engine* e, int32_t event_id, const void* d_gs, int64
     if (!e) return fail(GBO_ERR_ARG, "gbo_simulate_device: null engine");
     if (num_gs < 0 || (num_gs > 0 && !d_gs)) return fail(GBO_ERR_ARG, "gbo_simulate_device: bad gensteps");
     if (num_gs > 0x7fffffff) return fail(GBO_ERR_CAPACITY, "gbo_simulate_device: %lld gensteps", (long long)num_gs);
+    if (num_input < 0 || (num_input > 0 && !d_input)) return fail(GBO_ERR_ARG, "gbo_simulate_device: bad input photons");
     CU(cudaSetDevice(e->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
     int rc;
-    if ((rc = e->gs_end.ensure((size_t)(num_gs > 0 ? num_gs : 1)))) return rc;
+    // one slot past the prefix receives the INPUT_PHOTON flag
+    if ((rc = e->gs_end.ensure((size_t)num_gs + 1))) return rc;
     CU(cudaEventRecord(e->ev[0], s));
     unsigned long long total = 0;
     if (num_gs > 0) {
-        k_genstep_prefix<<<1, 1024, 0, s>>>((const gbo_quad6*)d_gs, (int)num_gs, e->gs_end.ptr);
+        k_genstep_prefix<<<1, 1024, 0, s>>>((const gbo_quad6*)d_gs, (int)num_gs, e->gs_end.ptr, e->gs_end.ptr + num_gs);
         CU(cudaGetLastError());
-        CU(cudaMemcpyAsync(e->host_counters + 3, e->gs_end.ptr + (num_gs - 1), sizeof(unsigned long long),
+        CU(cudaMemcpyAsync(e->host_counters + 2, e->gs_end.ptr + (num_gs - 1), 2 * sizeof(unsigned long long),
                            cudaMemcpyDeviceToHost, s));
         CU(cudaStreamSynchronize(s));
-        total = e->host_counters[3];
+        total = e->host_counters[2];
+        if (e->host_counters[3] && (long long)num_input < (long long)total)
+            return fail(GBO_ERR_ARG, "gbo_simulate_device: INPUT_PHOTON gensteps need %llu photons, %lld given", total,
+                        (long long)num_input);
     }
     return run_event(e, event_id, (const gbo_quad6*)d_gs, num_gs, (const gbo_sphoton*)d_input, num_input,
                      (long long)total, s, num_gs > 0 ? 1 : 0);
@@ -1477,6 +1499,15 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_bounded(const __grid_con
 
 namespace {
 constexpr int NA_MAX_DEVICES = 64;
+
+// Restores the calling thread's current device when it goes out of scope.
+struct DeviceGuard {
+    int dev = -1;
+    bool ok = false;
+    DeviceGuard() { ok = cudaGetDevice(&dev) == cudaSuccess; }
+    ~DeviceGuard() { if (ok) cudaSetDevice(dev); }
+};
+
 std::mutex g_noalloc_mutex;
 void* g_noalloc_ptr[NA_MAX_DEVICES] = {nullptr};
 
@@ -1513,6 +1544,10 @@ int gbo_simulate_noalloc(gbo_engine* e, int32_t event_id, const void* d_gs, int6
         return fail(GBO_ERR_CAPACITY, "gbo_simulate_noalloc: %lld gensteps above the limit of %lld", (long long)num_gs,
                     NA_MAX_GENSTEP);
     if (hit_capacity < 0 || (hit_capacity > 0 && !d_hits)) return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: bad hit buffer");
+    if (num_input_photon < 0 || (num_input_photon > 0 && !d_input_photon))
+        return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: bad input photons");
+    DeviceGuard keep_device;            // the caller's current device is restored on every return
+    if (!keep_device.ok) return fail(GBO_ERR_CUDA, "gbo_simulate_noalloc: cudaGetDevice failed");
     CU(cudaSetDevice(e->device));
     unsigned char* s_base = nullptr;
     int rc = noalloc_scratch(e->device, &s_base);
@@ -1529,14 +1564,15 @@ int gbo_simulate_noalloc(gbo_engine* e, int32_t event_id, const void* d_gs, int6
 
     // counters left over from the previous call must start at zero
     CU(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
-    k_genstep_prefix<<<1, 1024, 0, s>>>((const gbo_quad6*)d_gs, (int)num_gs, gs_end);
+    k_genstep_prefix<<<1, 1024, 0, s>>>((const gbo_quad6*)d_gs, (int)num_gs, gs_end, counters + 3);
     CU(cudaGetLastError());
-    unsigned long long total = 0;
+    unsigned long long total = 0, input_gs = 0;
     CU(cudaMemcpyAsync(&total, gs_end + (num_gs - 1), sizeof(total), cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(&input_gs, counters + 3, sizeof(input_gs), cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
     if ((long long)total > NA_MAX_PHOTON)
         return fail(GBO_ERR_CAPACITY, "gbo_simulate_noalloc: %llu photons above the limit of %lld", total, NA_MAX_PHOTON);
-    if (num_input_photon > 0 && (long long)num_input_photon < (long long)total)
+    if ((input_gs || num_input_photon > 0) && (long long)num_input_photon < (long long)total)
         return fail(GBO_ERR_ARG, "gbo_simulate_noalloc: %lld input photons for %llu photon slots", (long long)num_input_photon, total);
 
     Params P = make_params(e);

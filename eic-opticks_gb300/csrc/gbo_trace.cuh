@@ -171,7 +171,7 @@ GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float
     }
 }
 
-constexpr int TRAVERSAL_STACK = 64;
+constexpr int TRAVERSAL_STACK = TLAS_STACK_DEPTH;
 
 constexpr int HINT_FIRST = 0x7fffff;     // leaf item standing for the photon's previous instance
 constexpr int OVERLAP_FIRST = 0x7ffffe;  // leaf item standing for that instance's overlap list

@@ -56,24 +56,90 @@ def isotropic_photons(n, wavelength=420.0, seed=42, origin=(0.0, 0.0, 0.0)):
     return p
 
 
+_FLT_MAX = np.finfo(np.float32).max
+
+
+def _round_to_float32(frac):
+    """The binary32 value nearest to an exact rational, ties to even (one rounding, as strtof does; a conversion
+    through a Python float would round twice).  None when the value rounds beyond the binary32 range."""
+    from fractions import Fraction
+    lim = Fraction(int(_FLT_MAX)) + Fraction(2) ** 103          # half an ulp above the largest finite binary32
+    if abs(frac) >= lim:
+        return None
+    c = np.float32(float(frac))
+    best = None
+    for cand in (np.nextafter(c, np.float32(-np.inf)), c, np.nextafter(c, np.float32(np.inf))):
+        if not np.isfinite(cand):
+            continue
+        err = abs(Fraction(float(cand)) - frac)
+        even = (int(np.array(cand, dtype=np.float32).view(np.uint32)) & 1) == 0
+        if best is None or err < best[0] or (err == best[0] and even):
+            best = (err, cand)
+    return best[1]
+
+
+def _cxx_extract_floats(line, count):
+    """Reads `count` floats from a line the way ``std::istringstream >> float`` does in libstdc++'s "C" locale
+    (num_get::_M_extract_float then strtof): skip white space, accumulate an optional sign, digits with at most one
+    decimal point, and an exponent marker (only after a mantissa digit) with an optional sign and digits; the whole
+    accumulation must convert, and a value beyond the binary32 range fails.  A failed extraction ends the line
+    (returns None); what follows the last value is ignored.  So "nan", "inf", "1_0" (as a non-final value) and "1e"
+    fail, "1_0" as the final value reads 1, and "1.5.5" reads 1.5 then .5."""
+    from fractions import Fraction
+    vals, i, n = [], 0, len(line)
+    for _ in range(count):
+        while i < n and line[i] in " \t\n\v\f\r":
+            i += 1
+        acc = ""
+        if i < n and line[i] in "+-":
+            acc += line[i]
+            i += 1
+        found_mant = found_dec = found_sci = False
+        while i < n:
+            c = line[i]
+            if c.isdigit() and c in "0123456789":
+                acc += c
+                found_mant = True
+            elif c == "." and not found_dec and not found_sci:
+                acc += c
+                found_dec = True
+            elif c in "eE" and not found_sci and found_mant:
+                acc += "e"
+                found_sci = True
+                i += 1
+                if i < n and line[i] in "+-":
+                    acc += line[i]
+                else:
+                    continue
+            else:
+                break
+            i += 1
+        mant = acc.split("e")[0].lstrip("+-")
+        expo = acc.split("e")[1] if "e" in acc else None
+        if not any(ch.isdigit() for ch in mant) or (expo is not None and not expo.lstrip("+-")):
+            return None
+        v = _round_to_float32(Fraction(acc))
+        if v is None:
+            return None
+        vals.append(v)
+    return vals
+
+
 def load_photons_txt(path):
     """Input photons from a text file as the reference's photon-file source reads them (src/GPUPhotonFileSource.h
     load_photons_txt): one photon per line, 11 values ``pos_x pos_y pos_z time mom_x mom_y mom_z pol_x pol_y pol_z
-    wavelength``; blank lines and lines starting with '#' skipped, lines that do not start with 11 numbers skipped
-    (extra tokens after them are ignored, as the stream extraction ignores them).  Other fields are zero."""
+    wavelength`` read by C++ stream extraction (see _cxx_extract_floats); blank lines and lines starting with '#'
+    skipped, lines whose 11 extractions do not all succeed skipped, anything after the 11th value ignored.  Other
+    fields are zero."""
     rows = []
-    with open(path) as f:
-        for line in f:
-            line = line.rstrip("\n")
-            if not line or line[0] == "#":
-                continue
-            tok = line.split()
-            try:
-                v = [float(t) for t in tok[:11]]
-            except ValueError:
-                continue
-            if len(v) == 11:
-                rows.append(v)
+    with open(path, "rb") as f:
+        text = f.read().decode("latin-1")        # bytes as std::getline sees them; lines end at '\n' only
+    for line in text.split("\n"):
+        if not line or line[0] == "#":
+            continue
+        v = _cxx_extract_floats(line, 11)
+        if v is not None:
+            rows.append(v)
     p = np.zeros(len(rows), dtype=L.PHOTON)
     if rows:
         a = np.asarray(rows, dtype=np.float32)

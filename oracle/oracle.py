@@ -11,6 +11,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REFLIB = os.path.join(HERE, "_ref", "libref.so")
+REFDEV_CUBIN = os.path.join(HERE, "_ref", "ref_device.cubin")
+REFDEV_RUN = os.path.join(HERE, "_ref", "libref_device_run.so")
 
 
 class Tex(C.Structure):
@@ -152,6 +154,55 @@ def simulate(cfg, gs, input_photon=None, event_index=0, photon_offset=0, nthread
                            C.c_uint32(event_index), C.c_int64(n), _ptr(out),
                            _ptr(sq) if sq is not None else None, C.c_int(nthreads))
     return out, sq
+
+
+_refdev = None
+
+
+def ref_device_available():
+    """True when the reference-header device build (ref_device.cubin) is present."""
+    return os.path.exists(REFDEV_CUBIN)
+
+
+def ref_device_lib():
+    global _refdev
+    if _refdev is None:
+        if not os.path.exists(REFDEV_RUN):
+            subprocess.check_call(["make", "-s", "-C", HERE, "ref-device-run"])
+        _refdev = C.CDLL(REFDEV_RUN)
+        _refdev.ref_device_simulate.restype = C.c_int
+        _refdev.ref_device_last_error.restype = C.c_char_p
+    return _refdev
+
+
+def ref_device_simulate(cfg, gs, input_photon=None, event_index=0):
+    """Run the reference's own headers, compiled by nvcc for the GPU (ref_device.cu), over every photon of ``gs``
+    on the current GPU, one thread per photon.  Returns (photons, seq, kernel_ms)."""
+    from importlib import import_module
+    L = import_module("eic_opticks_gb300.layout")
+    if not ref_device_available():
+        raise RuntimeError("reference device build oracle/_ref/ref_device.cubin not present")
+    gs = np.ascontiguousarray(gs, dtype=np.float32)
+    counts = gs.view(np.uint32)[:, 0, 3].astype(np.int64)
+    seed = np.ascontiguousarray(np.repeat(np.arange(len(gs), dtype=np.int32), counts))
+    n = len(seed)
+    if input_photon is not None:
+        input_photon = np.ascontiguousarray(input_photon)
+        if len(input_photon) < n:
+            raise ValueError("%d input photons for %d photons" % (len(input_photon), n))
+    out = np.zeros(n, dtype=L.PHOTON)
+    sq = np.zeros(n, dtype=L.SEQ)
+    sizes = np.array([len(cfg.node), len(cfg.prim), len(cfg.solid), len(cfg.itra), len(cfg.plan), len(cfg.optical)],
+                     dtype=np.int32)
+    ms = C.c_float(0.0)
+    lib_ = ref_device_lib()
+    rc = lib_.ref_device_simulate(REFDEV_CUBIN.encode(), C.byref(cfg.sim), _ptr(sizes), _ptr(gs), C.c_int64(len(gs)),
+                                  _ptr(seed), _ptr(input_photon) if input_photon is not None else None,
+                                  C.c_uint64(0), C.c_int32(event_index), C.c_int64(n), _ptr(out), _ptr(sq),
+                                  C.byref(ms))
+    if rc != 0:
+        raise RuntimeError("reference device build: " + lib_.ref_device_last_error().decode())
+    return out, sq, ms.value
 
 
 def trace(cfg, pos, dirs, tmin=0.05, tmax=1e9):

@@ -6,7 +6,8 @@
 //   * instances whose box has at least a quarter of the scene's box area are exactly those under the root's first
 //     child (when other instances exist);
 //   * every overlap-list entry is another instance whose world box meets the listing instance's box;
-//   * no other instance's world box enters a clear ball.
+//   * no other instance's world box enters a clear ball;
+//   * the deepest leaf fits the traversal stack (one entry per inner node on a path).
 // Prints one summary line; exits non-zero on the first violation.
 #include <cmath>
 #include <cstdio>
@@ -68,6 +69,7 @@ int main(int argc, char** argv)
                       inst.data(), (int)inst.size(), A, err, sizeof(err)) == 0, "build_accel: %s", err);
     const int n = (int)inst.size();
     CHECK((int)A.tlas_index.size() == n && (int)A.inst_box.size() == n, "sizes");
+    CHECK(A.max_depth <= TLAS_STACK_DEPTH, "depth %d above the traversal stack", A.max_depth);
 
     // walk the two-child-box nodes: containment and instance coverage
     std::vector<int> seen(n, 0);

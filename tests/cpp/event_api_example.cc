@@ -1,4 +1,5 @@
-// event_api_example.cc : the engine-handle event API as a C caller binds it (the calls shown in INTEGRATION.md).
+// event_api_example.cc : the engine-handle event API as a C caller binds it (gbo_event_submit / _wait /
+// _num_hits / _copy_hits / _release from two producer threads).
 // Usage: event_api_example <folder with node.bin ... gs.bin, meta.txt as g4cx_example reads> ; prints the hit count
 // of each of four events submitted from two threads.
 #include <cstdio>

@@ -62,4 +62,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GBO_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_gdml_golden.py <reference checkout>  (or set GBO_REFERENCE_DIR)")
+    main(ref)

@@ -39,6 +39,38 @@ def test_accel_invariants(checker, tmp_path, name):
     assert out.returncode == 0, out.stdout + out.stderr
 
 
+def degenerate(kind):
+    """Instance sets that defeat a surface-area split: thousands of coincident boxes, and a chain of box clusters at
+    geometrically growing distances (each cluster 150 coincident boxes)."""
+    from eic_opticks_gb300 import geometry as G
+    g = G.Geometry("degenerate")
+    m = G.Material("m")
+    s = g.add_solid("b", [(G.box3(10, 10, 10), g.boundary(m, None, None, m))])
+    if kind == "coincident":
+        for _ in range(8000):
+            g.add_instance(s, G.translate(1.0, 2.0, 3.0))
+    else:
+        for k in range(60):
+            for _ in range(150):
+                g.add_instance(s, G.translate(3.0 ** (k * 0.7), 0.0, 0.0))
+    g.icdf = G.default_icdf()
+    return g.arrays()
+
+
+@pytest.mark.parametrize("kind", ["coincident", "chain"])
+def test_accel_depth_bounded_on_degenerate_instances(checker, tmp_path, kind):
+    """Degenerate instance sets either build within the traversal stack (the checker asserts the depth bound and
+    every invariant above) or are refused with a message; a walk never drops a subtree."""
+    arrays = degenerate(kind)
+    for k in ("node", "prim", "solid", "inst"):
+        np.ascontiguousarray(arrays[k]).tofile(str(tmp_path / ("%s.bin" % k)))
+    out = subprocess.run([checker, str(tmp_path)], capture_output=True, text=True)
+    print(kind, out.stdout.strip())
+    assert out.returncode == 0 or "traversal stack" in out.stdout, out.stdout + out.stderr
+    depth = int(out.stdout.split(" depth ")[1].split()[0])
+    assert depth <= 64
+
+
 @pytest.mark.parametrize("fixture", ["sim_gdml_sipm8x8.npz", "sim_gdml_basic_detector.npz", "sim_gdml_raindrop.npz"])
 def test_accel_invariants_gdml(checker, tmp_path, fixture):
     """Geometries translated from the reference's GDML files (the arrays stored with their golden fixtures)."""

@@ -8,7 +8,7 @@ import pytest
 
 from conftest import golden_arrays, load_golden
 
-REF_GEOM = os.path.join(os.sep, "root", "reference", "tests", "geom")
+REF_GEOM = os.path.join(os.environ.get("GBO_REFERENCE_DIR") or os.devnull, "tests", "geom")
 
 
 def test_raindrop_file_photons_all_hit(oracle):

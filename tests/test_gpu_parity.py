@@ -133,6 +133,70 @@ def test_simulate_matches_reference_golden(E, name):
     eng.close()
 
 
+def strict_compare(eng_p, eng_seqhis, ref_p, ref_seqhis):
+    """The parity bars against the reference's own device arithmetic: flag history (seqhis) identical; for those
+    photons, positions within 1e-3 mm and times within 1e-3 ns, or one ulp of the value where that is larger;
+    integer words (flags, boundary, identity, index, instance) identical."""
+    same = np.all(eng_seqhis == ref_seqhis, axis=1)
+    a, b = eng_p[same], ref_p[same]
+    pos_ok = np.all(np.abs(a["pos"] - b["pos"]) <= np.maximum(POS_TOL_MM, np.spacing(np.abs(b["pos"]))), axis=1)
+    t_ok = np.abs(a["time"] - b["time"]) <= np.maximum(TIME_TOL_NS, np.spacing(np.abs(b["time"])))
+    wa, wb = a.view(np.uint32).reshape(-1, 16), b.view(np.uint32).reshape(-1, 16)
+    int_ok = np.all(wa[:, [7, 12, 13, 14, 15]] == wb[:, [7, 12, 13, 14, 15]], axis=1)
+    exact = np.all(wa == wb, axis=1)
+    n = max(1, len(same))
+    m = max(1, int(same.sum()))
+    return {"photons": len(same), "history": same.sum() / n, "pos": pos_ok.sum() / m, "time": t_ok.sum() / m,
+            "ints": int_ok.sum() / m, "bit_exact": exact.sum() / n}
+
+
+def _device_golden(name):
+    import os
+    from conftest import GOLDEN
+    path = os.path.join(GOLDEN, "dev_%s.npz" % name)
+    if not os.path.exists(path):
+        pytest.fail("reference-device fixture %s missing" % path)
+    return np.load(path, allow_pickle=False)
+
+
+@pytest.mark.parametrize("name", SIM_FIXTURES)
+def test_simulate_matches_reference_device(E, name):
+    """Every host fixture's inputs against the reference's headers compiled by nvcc and run on the GPU."""
+    z = load_golden("sim_%s.npz" % name)
+    d = _device_golden(name)
+    eng = E.Engine(golden_arrays(z), record_photon=1, record_seq=1)
+    inp = z["input_photon"] if len(z["input_photon"]) else None
+    eng.simulate(int(z["event_index"]), z["gs"], inp)
+    r = strict_compare(eng.photons(), eng.seq()["seqhis"], d["photon"], d["seq"]["seqhis"])
+    eng.close()
+    print("%s vs reference device build: %s" % (name, " ".join("%s %.6g" % kv for kv in r.items())))
+    assert r["history"] >= 0.999 and r["pos"] >= 0.999 and r["time"] >= 0.999 and r["ints"] >= 0.999
+
+
+@pytest.mark.parametrize("name", ["cfg1_nested_boxes", "cfg2_crystal_array", "cfg3_water_cube", "cfg5_large_sphere"])
+def test_benchmark_configs_match_reference_device(E, name):
+    """100k-photon samples of the benchmark configurations (the full 20,000-sensor geometry for the large sphere)
+    against the reference's headers compiled by nvcc and run on the GPU."""
+    import importlib.util
+    import os
+    from conftest import GOLDEN
+    spec = importlib.util.spec_from_file_location("make_device_golden", os.path.join(GOLDEN, "make_device_golden.py"))
+    mdg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mdg)
+    d = _device_golden(name)
+    arrays, gs, inp, ev = mdg.config_inputs(name)
+    assert mdg.geometry_digest(arrays) == str(d["geometry_sha256"]), "geometry generator changed since the fixture"
+    assert (mdg.digest(inp) if inp is not None else "") == str(d["input_photon_sha256"])
+    assert np.array_equal(gs.view(np.uint32), d["gs"].view(np.uint32))
+    eng = E.Engine(arrays, record_photon=1, record_seq=1)
+    eng.simulate(int(d["event_index"]), gs, inp)
+    r = strict_compare(eng.photons(), eng.seq()["seqhis"], d["photon"], d["seqhis"])
+    eng.close()
+    print("%s vs reference device build: %s" % (name, " ".join("%s %.6g" % kv for kv in r.items())))
+    assert r["photons"] >= 100_000
+    assert r["history"] >= 0.999 and r["pos"] >= 0.999 and r["time"] >= 0.999 and r["ints"] >= 0.999
+
+
 @pytest.mark.parametrize("keep_photon", [1, 0])
 def test_hits_in_photon_order(E, keep_photon):
     z = load_golden("sim_crystal_array.npz")

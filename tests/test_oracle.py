@@ -76,8 +76,9 @@ def test_hit_selection_order(oracle):
 @pytest.fixture(scope="module")
 def ref(oracle):
     import os
-    if not os.path.isdir("/root/reference/qudarap"):
-        pytest.skip("reference tree not available")
+    ref = os.environ.get("GBO_REFERENCE_DIR")
+    if not ref or not os.path.isdir(os.path.join(ref, "qudarap")):
+        pytest.skip("reference tree not available (GBO_REFERENCE_DIR)")
     oracle.build(ref=True)
     if oracle.reflib() is None:
         pytest.skip("reference build not available")

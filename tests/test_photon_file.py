@@ -15,6 +15,18 @@ SAMPLE = """# x y z t mx my mz px py pz wl
 not a photon line
 1e-3 2.5 -3.25 1.25e2 0.6 0.8 0 0 0 1 399.5
 1 2 3
+1 2 3 4 0 0 1 1 0 0 1_0
+1 2 3 4 0 0 1 1 0 0 nan
+inf 2 3 4 0 0 1 1 0 0 400
+1.5.5 3 4 0 0 1 1 0 0 400
+0x1p3 2 3 4 0 0 1 1 0 0 400
+1e 2 3 4 0 0 1 1 0 0 400
+1 2 3 4 0 0 1 1 0 0 1e40
+1 2 3 4 0 0 1 1 0 0 1e-45
+1.000000059604644776257986737988403547205962240695953369140625 0 0 0 0 0 1 1 0 0 420
++5 -6 .5 5. 1E2 1e+2 0 1 0 0 420
+--5 2 3 4 0 0 1 1 0 0 400
+1 2 3 4 0 0 1 1 0 0 1_0 1 2 3
 """
 
 
@@ -28,9 +40,15 @@ def test_photon_file_roundtrip(tmp_path):
     subprocess.check_call([exe, str(src), str(tmp_path / "p.bin"), str(tmp_path / "hits_cpp.txt")])
     cpp = np.fromfile(str(tmp_path / "p.bin"), dtype=L.PHOTON)
     py = GS.load_photons_txt(str(src))
-    assert len(py) == len(cpp) == 3
+    # accepted: the three plain photons, "1_0" as the last value (reads 1), "1.5.5" (reads 1.5 then .5), the
+    # underflowing 1e-45, the value that one rounding takes above 1.0, signs and exponent forms, the trailing tokens
+    assert len(py) == len(cpp) == 9
     assert np.array_equal(py.view(np.uint32), cpp.view(np.uint32))
     assert py["wavelength"][1] == np.float32(450) and py["time"][2] == np.float32(125.0)
+    assert py["wavelength"][3] == np.float32(1.0) and list(py["pos"][4]) == [1.5, 0.5, 3.0]
+    assert py["wavelength"][5] == np.float32(1e-45) and py["wavelength"][5] > 0
+    assert py["pos"][6].view(np.uint32)[0] == 0x3F800001           # 1 + 2^-23, not 1.0 (rounded once)
+    assert list(py["pos"][7]) == [5.0, -6.0, 0.5] and py["time"][7] == 5.0
     GS.write_hits_txt(py, str(tmp_path / "hits_py.txt"))
     assert (tmp_path / "hits_py.txt").read_text() == (tmp_path / "hits_cpp.txt").read_text()
     assert (tmp_path / "hits_py.txt").read_text().splitlines()[0] == \
