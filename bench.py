@@ -43,8 +43,9 @@ L2_FLUSH_BYTES = 256 << 20
 # 0.22 + 182.10 MB and 210.98 + 2.46 MB, larger than L2)
 TRAFFIC_B_PER_PHOTON = {("crystal_array", 1): (443392.0 + 840192.0) / 998319,
                         ("crystal_array", 2): (0.22e6 + 182.10e6 + 210.98e6 + 2.46e6) / 2499792}
-TRAFFIC_SOURCE = {1: "ncu DRAM bytes of k_simulate on a 1M-photon crystal event, scaled by photons",
-                  2: "ncu DRAM bytes of k_generate + k_simulate_pool on a 2.5M-photon crystal event, scaled by photons"}
+TRAFFIC_SOURCE = {("crystal_array", 1): "ncu DRAM bytes of k_simulate on a 1M-photon crystal event, scaled by photons",
+                  ("crystal_array", 2): "ncu DRAM bytes of k_generate + k_simulate_pool on a 2.5M-photon crystal "
+                                        "event, scaled by photons"}
 
 
 def pinned_photons(n):
@@ -85,6 +86,8 @@ class ClockSampler:
         self.path = os.path.join(tempfile.gettempdir(), "bench_clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
+        if self.device < 0:          # no sampling asked
+            return self
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
@@ -281,8 +284,8 @@ def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
         sample = (GS.crystal_scint_gensteps(200, 5000, seed=99) if kind == "crystal" else
                   GS.water_cerenkov_gensteps(G.water_cube(), 2000, seed=99))
         r = eng.autotune(0, sample, trials=2)
-        tuned[kind] = {"mode": KERNEL_MODES[r["kernel_mode"]],
-                       "refill_min": r["refill_min"], "refill_period": r["refill_period"]}
+        tuned[kind] = {"mode": KERNEL_MODES[r["kernel_mode"]], "refill_min": r["refill_min"],
+                       "refill_period": r["refill_period"], "blocks_per_sm": r["blocks_per_sm"]}
     photons = {id(ev[2]): int(ev[2].view(np.uint32)[:, 0, 3].astype(np.int64).sum()) for ev in events}
     total_photons = sum(photons.values())
     for kind, eid, gs in events[:4]:                          # warm-up
@@ -386,7 +389,7 @@ def same_config_batching(geom, kind, n_events, tune, submitters=16):
     events = [workload(seed=100 + k, kind=kind)[1:] for k in range(n_events)]
     photons = sum(int(g.view(np.uint32)[:, 0, 3].astype(np.int64).sum()) for g, _ in events)
     eng = E.Engine(geom, kernel_mode=tune["kernel_mode"], refill_min=tune["refill_min"],
-                   refill_period=tune["refill_period"])
+                   refill_period=tune["refill_period"], blocks_per_sm=tune.get("blocks_per_sm", 0))
     eng.simulate(0, *events[0])
     t0 = time.perf_counter()
     for k, (g, inp) in enumerate(events):
@@ -426,6 +429,178 @@ def same_config_batching(geom, kind, n_events, tune, submitters=16):
             "batched_photons_per_s": photons / batched_s, "batched_over_plain": plain_s / batched_s,
             "batches": st["batches"], "drain_latency_ms": {"p50": 1e3 * pct(lat, 50), "p99": 1e3 * pct(lat, 99)}}
 
+def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=None, num_gs=None, precision=0,
+                     clocks=False):
+    """One configuration on this rank's GPU: device-resident photons/s (value) and photons/s through the C ABI
+    with host buffers (e2e), the simulate kernels' algorithmic HBM bytes against the measured copy bandwidth, the
+    kernel form the autotuner picked on a 10 % sample.  Returns a dict; the engine and inputs ride along under
+    keys starting with '_' for the caller."""
+    import torch
+    from eic_opticks_gb300 import engine as E
+    geom, gs, inp = workload(seed=1 + rank, num_gs=num_gs, kind=kind)
+    n_photon = int(gs.view(np.uint32)[:, 0, 3].astype(np.int64).sum())
+    n_inp = 0 if inp is None else len(inp)
+    if form:
+        mode, refill, period = form
+        eng = E.Engine(geom, device=local, precision=precision, kernel_mode=mode, refill_min=refill,
+                       refill_period=period)
+        tune = {"kernel_mode": mode, "refill_min": refill, "refill_period": period, "blocks_per_sm": 0}
+    else:
+        # kernel form picked by the autotuner on a 10% sample of the workload (setup, outside the timed region)
+        eng = E.Engine(geom, device=local, precision=precision)
+        if inp is None:
+            tune = eng.autotune(0, gs[: max(1, len(gs) // 10)], trials=2)
+        else:
+            tune = eng.autotune(0, gs, inp, trials=2)
+
+    d_gs = torch.from_numpy(gs.copy()).to(f"cuda:{local}")
+    d_inp = torch.from_numpy(inp.view(np.uint8).copy()).to(f"cuda:{local}") if inp is not None else None
+    inp_ptr = d_inp.data_ptr() if d_inp is not None else 0
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    # ---- device-resident throughput (value) ----
+    for w in range(warmup):
+        eng.simulate_device(w, d_gs.data_ptr(), len(gs), inp_ptr, n_inp)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms, sim_ms, gen_ms, launches, hits = [], [], [], 0, 0
+    with ClockSampler(local if clocks else -1) as clk:
+        for k in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            start.record()
+            hits = eng.simulate_device(1000 + k, d_gs.data_ptr(), len(gs), inp_ptr, n_inp)
+            end.record()
+            end.synchronize()
+            ms.append(start.elapsed_time(end))
+            st = eng.stats()
+            sim_ms.append(st["ms_simulate"])
+            gen_ms.append(st["ms_generate"])
+            launches += st["kernel_launches"]
+    torch.cuda.synchronize()
+    total_ms = sum(ms)
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t[0])
+    value = world * n_photon * steps / (total_ms * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers (e2e) ----
+    hits_host = None
+    e2e_ms = []
+    h2d = gs.nbytes + (inp.nbytes if inp is not None else 0)
+    nh = 0
+    for k in range(warmup + steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nh = eng.simulate(2000 + k, gs, inp)
+        if hits_host is None or len(hits_host) < nh:
+            hits_host = pinned_photons(max(nh, 1) * 2)
+        eng.hits(out=hits_host[:nh])
+        dt = time.perf_counter() - t0
+        if k >= warmup:
+            e2e_ms.append(dt * 1e3)
+    d2h = nh * 64 + 32      # ordered hits + the counters read that sizes them
+    e2e_total = sum(e2e_ms)
+    if dist:
+        t = torch.tensor([e2e_total], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t[0])
+    e2e_value = world * n_photon * steps / (e2e_total * 1e-3)
+
+    hbm, peak_kind = peaks()
+    f_hit = hits / n_photon
+    b_alg = 96.0 / (n_photon / len(gs)) + 4 + 64 + 64 + 64 * f_hit + (64.0 if inp is not None else 0.0)
+    sim_mean = float(np.mean(sim_ms))
+    traffic_key = (kind, tune["kernel_mode"])
+    achieved = b_alg * n_photon / (sim_mean * 1e-3) / 1e9
+    return {
+        "value": value, "unit": UNIT, "ms_per_step": total_ms / steps, "steps": steps, "warmup": warmup,
+        "config": {"precision": "binary64 root polish + accumulators" if precision else "binary32",
+                   "photons_per_step": n_photon, "gensteps_per_step": len(gs), "hits_per_step": hits,
+                   "kernel": {"mode": KERNEL_MODES[tune["kernel_mode"]], "refill_min": tune["refill_min"],
+                              "refill_period": tune["refill_period"], "blocks_per_sm": tune.get("blocks_per_sm", 0),
+                              "chosen_by": "--form" if form else "autotuner on 10% sample"},
+                   "max_bounce": 31},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": (TRAFFIC_B_PER_PHOTON[traffic_key] * n_photon
+                                 if traffic_key in TRAFFIC_B_PER_PHOTON and not precision else None),
+                     "traffic_source": (TRAFFIC_SOURCE[traffic_key]
+                                        if traffic_key in TRAFFIC_B_PER_PHOTON and not precision else None),
+                     "kernel": KERNEL_NAMES[tune["kernel_mode"]], "bytes_per_photon": b_alg,
+                     "kernel_ms": sim_mean, "generate_ms": float(np.mean(gen_ms)), "peak_source": peak_kind},
+        "clocks": clk.summary() if clocks else None,
+        "_engine": eng, "_geom": geom, "_gs": gs, "_inp": inp, "_tune": tune,
+    }
+
+
+def fp64_error_sample(n=100_000, seed=5):
+    """Intersection distances of the 20,000-sensor geometry against the binary64 oracle (oracle/orc_csg64.c) on
+    n rays (half from inside r < 17 m, half from the water aimed at the sensors), binary32 and precision mode:
+    the largest |t - t64| in mm over rays whose closest boundary agrees."""
+    from eic_opticks_gb300 import engine as E, geometry as G
+    O = ge.load_oracle()
+    O.build()
+    arrays = G.large_sphere().arrays()
+    rng = np.random.default_rng(seed)
+    h = n // 2
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    r = np.concatenate([17000.0 * rng.uniform(0, 1, h) ** (1.0 / 3.0), rng.uniform(17900.0, 18900.0, n - h)])
+    pos = r[:, None] * u
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    aim = 19400.0 * u[h:] + rng.normal(scale=300.0, size=(n - h, 3))
+    a = aim - pos[h:]
+    d[h:] = a / np.linalg.norm(a, axis=1, keepdims=True)
+    pos, d = pos.astype(np.float32), d.astype(np.float32)
+    t0 = time.perf_counter()
+    t64, b64 = O.trace64(O.SimConfig(arrays), pos, d)
+    out = {"rays": n, "oracle": "binary64 restatement of the CSG intersection (orc_csg64.c)",
+           "oracle_s": time.perf_counter() - t0}
+    for precision in (0, 1):
+        eng = E.Engine(arrays, precision=precision)
+        t, b = eng.trace_rays(pos, d)
+        eng.close()
+        ok = (b == b64) & (t64 > 0) & (t > 0)
+        err = np.abs(t[ok].astype(np.float64) - t64[ok])
+        out["binary32" if precision == 0 else "precision_mode"] = {
+            "same_boundary": float(ok.mean()), "max_mm": float(err.max()),
+            "p99_99_mm": float(np.percentile(err, 99.99)), "above_1e-3_mm": float((err > 1e-3).mean())}
+    return out
+
+
+def other_configs(args, dist, rank, world, local):
+    """The remaining benchmark configurations on this GPU, each with its own device-resident and end-to-end
+    photons/s, roofline and CPU baseline: nested boxes (100k input photons), dispersive water Cerenkov (1,000
+    steps), the 17.7 m sphere with 20,000 instanced sensors (100M photons) in binary32 and in the precision mode,
+    with the precision mode's FP64 intersection error on a ray sample."""
+    out = {}
+    for kind, steps, warmup in (("nested_boxes", 50, 5), ("water_cube", 50, 5), ("large_sphere", 3, 3)):
+        m = measure_workload(kind, args, dist, rank, world, local, steps, warmup)
+        eng, geom, gs, inp = m.pop("_engine"), m.pop("_geom"), m.pop("_gs"), m.pop("_inp")
+        m.pop("_tune")
+        eng.close()
+        m.pop("clocks")
+        m["workload"] = WORKLOADS[kind]
+        if not args.no_cpu_baseline:
+            m["cpu_baseline"] = cpu_baseline(geom, gs, target_s=4.0, inp=inp)
+        out[kind] = m
+    m = measure_workload("large_sphere", args, dist, rank, world, local, 2, 3, precision=1)
+    for k in ("_engine",):
+        m.pop(k).close()
+    for k in ("_geom", "_gs", "_inp", "_tune", "clocks"):
+        m.pop(k)
+    m["workload"] = WORKLOADS["large_sphere"] + "_precision"
+    m["fp64_intersection_error"] = fp64_error_sample()
+    out["large_sphere_precision"] = m
+    return out
+
 
 def dist_init(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -454,6 +629,8 @@ def main():
                     help="events of the workload for the same-configuration plain vs batched comparison")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
                     help="1: binary64 root polish and position/time accumulators")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the figures of the other benchmark configurations (nested boxes, water, large sphere)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -473,115 +650,27 @@ def main():
         dist.barrier()
     ge.load_package()
     from eic_opticks_gb300 import engine as E
-    geom, gs, inp = workload(seed=1 + rank, num_gs=args.gensteps, kind=args.workload)
-    n_photon = int(gs.view(np.uint32)[:, 0, 3].astype(np.int64).sum())
-    n_inp = 0 if inp is None else len(inp)
-    eng = E.Engine(geom, device=local, precision=args.precision)
-    # kernel form picked by the autotuner on a 10% sample of the workload (setup, outside the timed region)
-    if args.form:
-        mode, refill, period = (int(x) for x in args.form.split(","))
-        eng.close()
-        eng = E.Engine(geom, device=local, precision=args.precision, kernel_mode=mode, refill_min=refill,
-                       refill_period=period)
-        tune = {"kernel_mode": mode, "refill_min": refill, "refill_period": period}
-    elif inp is None:
-        tune = eng.autotune(0, gs[: max(1, len(gs) // 10)], trials=2)
-    else:
-        tune = eng.autotune(0, gs, inp, trials=2)
-
-    d_gs = torch.from_numpy(gs.copy()).to(f"cuda:{local}")
-    d_inp = torch.from_numpy(inp.view(np.uint8).copy()).to(f"cuda:{local}") if inp is not None else None
-    inp_ptr = d_inp.data_ptr() if d_inp is not None else 0
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-
-    # ---- device-resident throughput (value) ----
-    for w in range(args.warmup):
-        eng.simulate_device(w, d_gs.data_ptr(), len(gs), inp_ptr, n_inp)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    ms, sim_ms, gen_ms, launches, hits = [], [], [], 0, 0
-    with ClockSampler(local) as clk:
-        for k in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            start.record()
-            hits = eng.simulate_device(1000 + k, d_gs.data_ptr(), len(gs), inp_ptr, n_inp)
-            end.record()
-            end.synchronize()
-            ms.append(start.elapsed_time(end))
-            st = eng.stats()
-            sim_ms.append(st["ms_simulate"])
-            gen_ms.append(st["ms_generate"])
-            launches += st["kernel_launches"]
-    torch.cuda.synchronize()
-    total_ms = sum(ms)
-    if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t[0])
-    value = world * n_photon * args.steps / (total_ms * 1e-3)
-
-    # ---- end to end through the C ABI with host buffers (e2e) ----
-    hits_host = None
-    e2e_ms = []
-    h2d = gs.nbytes + (inp.nbytes if inp is not None else 0)
-    for k in range(args.warmup + args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        nh = eng.simulate(2000 + k, gs, inp)
-        if hits_host is None or len(hits_host) < nh:
-            hits_host = pinned_photons(max(nh, 1) * 2)
-        eng.hits(out=hits_host[:nh])
-        dt = time.perf_counter() - t0
-        if k >= args.warmup:
-            e2e_ms.append(dt * 1e3)
-    d2h = nh * 64 + 32      # ordered hits + the counters read that sizes them
-    e2e_total = sum(e2e_ms)
-    if dist:
-        t = torch.tensor([e2e_total], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t[0])
-    e2e_value = world * n_photon * args.steps / (e2e_total * 1e-3)
+    form = tuple(int(x) for x in args.form.split(",")) if args.form else None
+    m = measure_workload(args.workload, args, dist, rank, world, local, args.steps, args.warmup, form=form,
+                         num_gs=args.gensteps, precision=args.precision, clocks=True)
+    eng, geom, gs, inp, tune = m.pop("_engine"), m.pop("_geom"), m.pop("_gs"), m.pop("_inp"), m.pop("_tune")
 
     if rank != 0:
         if dist:
             dist.barrier()
+        eng.close()
         return
 
-    hbm, peak_kind = peaks()
-    f_hit = hits / n_photon
-    b_alg = 96.0 / (n_photon / len(gs)) + 4 + 64 + 64 + 64 * f_hit + (64.0 if inp is not None else 0.0)
-    sim_mean = float(np.mean(sim_ms))
-    traffic_key = (args.workload, tune["kernel_mode"])
-    achieved = b_alg * n_photon / (sim_mean * 1e-3) / 1e9
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32" if not args.precision else "f32+f64",
+        "metric": METRIC, "value": m["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if not args.precision else "f32+f64",
         "data": "synthetic (seeded numpy gensteps with the reference genstep layout)",
-        "config": {"workload": (WORKLOADS[args.workload] if args.gensteps is None
-                                else WORKLOADS[args.workload] + "_%dgs" % args.gensteps),
-                   "precision": "binary64 root polish + accumulators" if args.precision else "binary32",
-                   "photons_per_step": n_photon, "gensteps_per_step": len(gs),
-                   "hits_per_step": hits, "path": "plain: one event per launch", "l2": "flushed (256 MB write) between timed steps",
-                   "kernel": {"mode": KERNEL_MODES[tune["kernel_mode"]],
-                              "refill_min": tune["refill_min"], "refill_period": tune["refill_period"],
-                              "chosen_by": "--form" if args.form else "autotuner on 10% sample"},
-                   "max_bounce": 31, "parallelism": "replicas" if world > 1 else "1 GPU"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": (TRAFFIC_B_PER_PHOTON[traffic_key] * n_photon
-                                 if traffic_key in TRAFFIC_B_PER_PHOTON and not args.precision else None),
-                     "traffic_source": (TRAFFIC_SOURCE[tune["kernel_mode"]]
-                                        if traffic_key in TRAFFIC_B_PER_PHOTON and not args.precision else None),
-                     "kernel": KERNEL_NAMES[tune["kernel_mode"]],
-                     "bytes_per_photon": b_alg,
-                     "kernel_ms": sim_mean, "generate_ms": float(np.mean(gen_ms)), "peak_source": peak_kind},
-        "clocks": clk.summary(),
+        "config": dict(m["config"], workload=(WORKLOADS[args.workload] if args.gensteps is None
+                                              else WORKLOADS[args.workload] + "_%dgs" % args.gensteps),
+                       path="plain: one event per launch", l2="flushed (256 MB write) between timed steps",
+                       parallelism="replicas" if world > 1 else "1 GPU"),
+        "e2e": m["e2e"], "gpu_launches": m["gpu_launches"], "roofline": m["roofline"], "clocks": m["clocks"],
     }
     if not args.no_serving and world == 1:
         line["serving"] = serving_bench()                                   # the 1e3-1e7 serving stream
@@ -601,6 +690,8 @@ def main():
                          "ms": 1e3 * (time.perf_counter() - t0)}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(geom, gs, inp=inp)
+    if not args.no_configs and world == 1 and args.gensteps is None and not args.precision:
+        line["configs"] = other_configs(args, dist, rank, world, local)
     print(json.dumps(line))
     if dist:
         dist.barrier()

@@ -480,6 +480,157 @@ GBO_DEV bool intersect_leaf(float4& is, const gbo_csgnode* node, const float4* p
 enum { CTRL_RETURN_MISS = 0, CTRL_RETURN_A = 1, CTRL_RETURN_B = 2, CTRL_RETURN_FLIP_B = 3, CTRL_LOOP_A = 4, CTRL_LOOP_B = 5 };
 enum { ST_ENTER = 0, ST_EXIT = 1, ST_MISS = 2 };
 
+// CSG_CLASSIFY, csg_classify.h:55: enter, exit or miss of a hit at |t| against the ray direction
+GBO_DEV int classify(float4 ise, float3 dir, float tmin)
+{
+    return fabsf(ise.w) > tmin ? (ise.x * dir.x + ise.y * dir.y + ise.z * dir.z < 0.f ? ST_ENTER : ST_EXIT) : ST_MISS;
+}
+
+// ---- list nodes : csg_intersect_node.h (the reference's OptiX build defines WITH_CONTIGUOUS) --------------------
+// A list header node holds subNum (q0.u.x) leaves starting subOffset (q0.u.y) nodes after the prim's root; the
+// leaves carry their own transforms.  Geometry creation checks that every sub is a leaf inside its prim.
+constexpr float LIST_EPSILON = 0.0001f;      // propagate_epsilon of csg_intersect_node.h
+constexpr int LIST_MAX_ENTER = 8;            // enter slots of intersect_node_contiguous (its arrays hold 8)
+
+// CSG_CONTIGUOUS, csg_intersect_node.h:390-626: a multi-union whose leaves overlap into one connected shape.  A
+// ray whose first hits all enter starts outside: the nearest enter is the answer.  Otherwise it starts inside:
+// the exit is the farthest first-exit, extended by the exits of the leaves it enters before reaching that exit,
+// taken in order of their enter distances (a leaf entered beyond the current exit is disjoint and skipped).
+GBO_DEV bool list_contiguous(float4& isect, const gbo_csgnode* node, const gbo_csgnode* root, const float4* plan,
+                              const gbo_qat4* itra, float t_min, float3 ro, float3 rd)
+{
+    const int num_sub = (int)__ldg(&node->q0.u[0]);
+    const int offset_sub = (int)__ldg(&node->q0.u[1]);
+    float4 nearest_enter = make_float4(0.f, 0.f, 0.f, RT_DEFAULT_MAX);
+    float4 farthest_exit = make_float4(0.f, 0.f, 0.f, t_min);
+    float4 sub;
+    int exit_count = 0;
+    for (int i = 0; i < num_sub; i++) {
+        if (!intersect_leaf(sub, root + offset_sub + i, plan, itra, t_min, ro, rd)) continue;
+        const int st = classify(sub, rd, t_min);
+        if (st == ST_ENTER) { if (sub.w < nearest_enter.w) nearest_enter = sub; }
+        else if (st == ST_EXIT) exit_count += 1;
+    }
+    if (exit_count == 0) {
+        const bool valid = nearest_enter.w > t_min && nearest_enter.w < RT_DEFAULT_MAX;
+        if (valid) isect = nearest_enter;
+        return valid;
+    }
+    int enter_count = 0;
+    float enter[LIST_MAX_ENTER];
+    int which[LIST_MAX_ENTER], order[LIST_MAX_ENTER];
+    for (int i = 0; i < num_sub; i++) {
+        if (!intersect_leaf(sub, root + offset_sub + i, plan, itra, t_min, ro, rd)) continue;
+        const int st = classify(sub, rd, t_min);
+        if (st == ST_ENTER) {
+            if (enter_count < LIST_MAX_ENTER) {
+                which[enter_count] = i;
+                order[enter_count] = enter_count;
+                enter[enter_count] = sub.w;
+                enter_count += 1;
+            }
+        } else if (st == ST_EXIT) {
+            exit_count += 1;
+            if (sub.w > farthest_exit.w) farthest_exit = sub;
+        }
+    }
+    // enter slots in ascending enter distance (a stable insertion sort of the slot indices)
+    for (int i = 1; i < enter_count; i++) {
+        const int key = order[i];
+        int j = i - 1;
+        while (j >= 0 && enter[order[j]] > enter[key]) { order[j + 1] = order[j]; j -= 1; }
+        order[j + 1] = key;
+    }
+    for (int i = 0; i < enter_count; i++) {
+        const float t_adv = enter[order[i]] + LIST_EPSILON;
+        if (!(t_adv < farthest_exit.w)) continue;
+        if (!intersect_leaf(sub, root + offset_sub + which[order[i]], plan, itra, t_adv, ro, rd)) continue;
+        if (classify(sub, rd, t_adv) == ST_EXIT) {
+            exit_count += 1;
+            if (sub.w > farthest_exit.w) farthest_exit = sub;
+        }
+    }
+    const bool valid = exit_count > 0 && farthest_exit.w > t_min;
+    if (valid) isect = farthest_exit;
+    return valid;
+}
+
+// CSG_DISCONTIGUOUS, csg_intersect_node.h:654-686: leaves that never overlap; the nearest leaf hit is the answer.
+GBO_DEV bool list_discontiguous(float4& isect, const gbo_csgnode* node, const gbo_csgnode* root, const float4* plan,
+                                 const gbo_qat4* itra, float t_min, float3 ro, float3 rd)
+{
+    const int num_sub = (int)__ldg(&node->q0.u[0]);
+    const int offset_sub = (int)__ldg(&node->q0.u[1]);
+    float4 closest = make_float4(0.f, 0.f, 0.f, RT_DEFAULT_MAX);
+    float4 sub;
+    for (int i = 0; i < num_sub; i++)
+        if (intersect_leaf(sub, root + offset_sub + i, plan, itra, t_min, ro, rd) && sub.w < closest.w) closest = sub;
+    const bool valid = closest.w < RT_DEFAULT_MAX;
+    if (valid) isect = closest;
+    return valid;
+}
+
+// CSG_OVERLAP, csg_intersect_node.h:819-895: a multi-intersection shaped like a ball.  Each leaf contributes its
+// enter (and the exit after it) or its exit; the shape is hit when every leaf was met and the farthest enter lies
+// before the nearest exit: that enter from outside, else the exit from inside.
+GBO_DEV bool list_overlap(float4& isect, const gbo_csgnode* node, const gbo_csgnode* root, const float4* plan,
+                           const gbo_qat4* itra, float t_min, float3 ro, float3 rd)
+{
+    const unsigned num_sub = __ldg(&node->q0.u[0]);
+    const unsigned offset_sub = __ldg(&node->q0.u[1]);
+    float4 farthest_enter = make_float4(0.f, 0.f, 0.f, t_min);
+    float4 nearest_exit = make_float4(0.f, 0.f, 0.f, RT_DEFAULT_MAX);
+    float4 sub;
+    unsigned enter_count = 0, exit_count = 0;
+    for (unsigned i = 0; i < num_sub; i++) {
+        const gbo_csgnode* leaf = root + offset_sub + i;
+        if (!intersect_leaf(sub, leaf, plan, itra, t_min, ro, rd)) continue;
+        const int st = classify(sub, rd, t_min);
+        if (st == ST_ENTER) {
+            enter_count += 1;
+            if (sub.w > farthest_enter.w) farthest_enter = sub;
+            const float t_adv = sub.w + LIST_EPSILON;
+            if (intersect_leaf(sub, leaf, plan, itra, t_adv, ro, rd) && classify(sub, rd, t_adv) == ST_EXIT) {
+                exit_count += 1;
+                if (sub.w < nearest_exit.w) nearest_exit = sub;
+            }
+        } else if (st == ST_EXIT) {
+            exit_count += 1;
+            if (sub.w < nearest_exit.w) nearest_exit = sub;
+        }
+    }
+    const bool overlap_all = farthest_enter.w < nearest_exit.w && max(enter_count, exit_count) == num_sub;
+    if (!overlap_all) return false;
+    if (farthest_enter.w > t_min && farthest_enter.w < RT_DEFAULT_MAX) { isect = farthest_enter; return true; }
+    if (nearest_exit.w > t_min && nearest_exit.w < RT_DEFAULT_MAX) { isect = nearest_exit; return true; }
+    return false;
+}
+
+// The three list kinds behind one out-of-line entry, so that the boolean tree and the prim dispatch each hold a
+// single call site (lists are rare; the call keeps their code and registers out of the common paths).  The result
+// is written through a copy, so that the caller's `isect` stays in registers.
+GBO_COLD bool intersect_list(float4& isect, const gbo_csgnode* node, const gbo_csgnode* root, const float4* plan,
+                             const gbo_qat4* itra, float t_min, float3 ro, float3 rd)
+{
+    switch (node_typecode(node)) {
+        case GBO_CSG_CONTIGUOUS:    return list_contiguous(isect, node, root, plan, itra, t_min, ro, rd);
+        case GBO_CSG_OVERLAP:       return list_overlap(isect, node, root, plan, itra, t_min, ro, rd);
+        case GBO_CSG_DISCONTIGUOUS: return list_discontiguous(isect, node, root, plan, itra, t_min, ro, rd);
+        default:                    return false;
+    }
+}
+
+// intersect_node, csg_intersect_node.h:913-938: a list header or a plain leaf
+GBO_DEV bool intersect_node(float4& isect, const gbo_csgnode* node, const gbo_csgnode* root, const float4* plan,
+                            const gbo_qat4* itra, float t_min, float3 ro, float3 rd, bool polish)
+{
+    if (node_typecode(node) >= GBO_CSG_LEAF) return intersect_leaf(isect, node, plan, itra, t_min, ro, rd, polish);
+    float4 c = isect;
+    const bool valid = intersect_list(c, node, root, plan, itra, t_min, ro, rd);
+    isect = c;
+    return valid;
+}
+
 GBO_DEV int lut_lookup(unsigned op, int sa, int sb, bool acloser)
 {
     // packed 4-bit actions indexed by 3*stateA+stateB, one word per boolean operation (csg_classify.h:86-101)
@@ -491,10 +642,6 @@ GBO_DEV int lut_lookup(unsigned op, int sa, int sb, bool acloser)
     return offset < 8 ? (int)((word >> (offset * 4)) & 0xfu) : CTRL_RETURN_MISS;
 }
 
-GBO_DEV int classify(float4 ise, float3 dir, float tmin)
-{
-    return fabsf(ise.w) > tmin ? (ise.x * dir.x + ise.y * dir.y + ise.z * dir.z < 0.f ? ST_ENTER : ST_EXIT) : ST_MISS;
-}
 
 GBO_DEV unsigned pack_slice(unsigned begin, unsigned end) { return ((begin & 0xffu) << 16) | ((end & 0xffu) << 24); }
 GBO_DEV unsigned postorder_next(unsigned i, unsigned elev) { return (i & 1u) ? i >> 1 : (i << elev) + (1u << elev); }
@@ -506,6 +653,8 @@ constexpr int TRANCHE_STACK = 4;
 // a miss instead of an unbounded loop.
 constexpr int MAX_TRANCHES = 256;
 
+// LISTS: the geometry holds CSG list nodes (their evaluation is compiled only into the kernel forms that need it)
+template <bool LISTS>
 GBO_DEV bool intersect_tree(float4& isect, const gbo_csgnode* node, const float4* plan, const gbo_qat4* itra,
                             float t_min, float3 ro, float3 rd, bool polish = false)
 {
@@ -538,8 +687,9 @@ GBO_DEV bool intersect_tree(float4& isect, const gbo_csgnode* node, const float4
             const unsigned typecode = node_typecode(nd);
             if (typecode == GBO_CSG_ZERO) { nodeIdx = postorder_next(nodeIdx, elevation); continue; }
             if (typecode >= GBO_CSG_NODE) {
-                float4 nd_isect;
-                intersect_leaf(nd_isect, nd, plan, itra, tmin, ro, rd, polish);
+                float4 nd_isect = make_float4(0.f, 0.f, 0.f, 0.f);
+                if constexpr (LISTS) intersect_node(nd_isect, nd, node, plan, itra, tmin, ro, rd, polish);
+                else intersect_leaf(nd_isect, nd, plan, itra, tmin, ro, rd, polish);
                 nd_isect.w = copysignf(nd_isect.w, nodeIdx % 2 == 0 ? -1.f : 1.f);
                 if (ccurr >= CSG_STACK - 1) { err = true; break; }
                 cdata[++ccurr] = nd_isect;
@@ -624,14 +774,16 @@ GBO_DEV int intersect_union_enter(float4& isect, const gbo_csgnode* node, const 
     return found ? 1 : 0;
 }
 
-// csg_intersect_tree.h:683-719 (list nodes are not supported)
+// csg_intersect_tree.h:683-719: a leaf, a boolean tree or (LISTS) a list prim (the list's own node is the root)
+template <bool LISTS>
 GBO_DEV bool intersect_prim(float4& isect, const gbo_csgnode* node, const float4* plan, const gbo_qat4* itra,
                             float t_min, float3 o, float3 d, bool polish = false)
 {
     const unsigned typecode = node_typecode(node);
     if (typecode >= GBO_CSG_LEAF) return intersect_leaf(isect, node, plan, itra, t_min, o, d, polish);
-    if (typecode < GBO_CSG_NODE) return intersect_tree(isect, node, plan, itra, t_min, o, d, polish);
+    if (typecode < GBO_CSG_NODE) return intersect_tree<LISTS>(isect, node, plan, itra, t_min, o, d, polish);
     isect = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (LISTS) return intersect_node(isect, node, node, plan, itra, t_min, o, d, polish);
     return false;
 }
 

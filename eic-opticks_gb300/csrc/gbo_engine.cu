@@ -93,13 +93,15 @@ struct Params {
     int* gen_hint;
     // start instance of each genstep's photons (k_genstep_hint), a traversal hint only; nullptr: none
     const int* gs_hint;
+    int walk_min;                           // pool kernels: parked lanes that trigger the gathered TLAS walks
 };
 
 GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng, int& hint);
 
-// Kernel forms: TREE when any prim is a CSG tree; PRECISE for the precision mode (binary64 root polish in the
-// quadric leaves, binary64 position / time accumulators).  The default form compiles none of the latter.
-template <bool TREE, bool PRECISE>
+// Kernel forms: TREE 1 when any prim is a CSG tree, 2 when CSG list nodes occur as well (their evaluation is
+// compiled only into that form); PRECISE for the precision mode (binary64 root polish in the quadric leaves,
+// binary64 position / time accumulators).  The default form compiles none of the latter.
+template <int TREE, bool PRECISE>
 __global__ void __launch_bounds__(SIM_BLOCK, (TREE || PRECISE) ? GBO_SIM_MINB_WIDE : GBO_SIM_MINB)
 k_simulate(const __grid_constant__ Params P)
 {
@@ -253,7 +255,7 @@ GBO_DEV void refill_pregenerated(const Params& P, unsigned long long* pool, unsi
 // PREGEN: the kernel-mode-2 form without the generator.  Without a call to the out-of-line generator, its
 // by-reference arguments no longer force the photon state through local memory (crystal event 751M -> 864M
 // photons/s).
-template <bool TREE, bool PRECISE, bool PREGEN>
+template <int TREE, bool PRECISE, bool PREGEN>
 __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P,
                                                              unsigned long long* pool, int refill_min, int period)
 {
@@ -271,6 +273,7 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
     // mode 2 (warp-uniform): the warp's claimed chunk of pregenerated photons [cbase, cbase + cn), cused taken
     long long cbase = 0;
     int cn = 0, cused = 0;
+    bool parked = false;            // the photon's step waits for a gathered TLAS walk
     for (;; it++) {
         // refill every `period` steps (or when the warp is empty): idle lanes take the next photon indices in lane
         // order; mode 2 claims them POOL_CHUNK at a time (one atomic per chunk) and loads them as generated, the
@@ -305,21 +308,35 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
             if (!pool_open) break;
             continue;
         }
+        // gathered TLAS walks: parked lanes walk once enough of them wait, or when no live lane is left to step
+        const unsigned parked_mask = __ballot_sync(0xffffffffu, parked);
+        const bool walk_now = parked_mask != 0u &&
+                              (__popc(parked_mask) >= P.walk_min || parked_mask == __ballot_sync(0xffffffffu, live));
         bool done = false;
         if (live) {
-            if (bounce < P.max_bounce && p.time < P.max_time) {
+            if (parked || (bounce < P.max_bounce && p.time < P.max_time)) {
                 const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
-                Hit h;
-                trace<TREE, PRECISE>(P.acc, p.pos, p.mom, tmin, P.tmax, hint, h);
-                if ((h.prim_boundary & 0xffffu) == 0xffffu) {
-                    done = true;
-                } else {
-                    hint = (int)(h.iindex_identity >> 16);
-                    h.normal = normalize(h.normal);
-                    const int command = propagate(P.tab, p, h, rng, PRECISE ? &acc : nullptr);
-                    bounce++;
-                    if (P.seq_out) seq_add(P.seq_out + idx, (unsigned)bounce, flag_of(p), boundary_of(p));
-                    done = command == CMD_BREAK;
+                // one call site: a query that may stop before its TLAS walk, or a parked lane's whole query (its
+                // hint instance tested again, then the walk) once the warp gathers the walks
+                Best b;
+                trace_begin(b, P.tmax);
+                int r = TRACE_WALK;
+                if (!parked || walk_now)
+                    r = trace_items<TREE, PRECISE>(P.acc, p.pos, p.mom, tmin, hint, !parked && P.walk_min > 1, b);
+                parked = r == TRACE_WALK;
+                if (!parked) {
+                    Hit h;
+                    trace_finish(P.acc, p.pos, p.mom, b, h);
+                    if ((h.prim_boundary & 0xffffu) == 0xffffu) {
+                        done = true;
+                    } else {
+                        hint = (int)(h.iindex_identity >> 16);
+                        h.normal = normalize(h.normal);
+                        const int command = propagate(P.tab, p, h, rng, PRECISE ? &acc : nullptr);
+                        bounce++;
+                        if (P.seq_out) seq_add(P.seq_out + idx, (unsigned)bounce, flag_of(p), boundary_of(p));
+                        done = command == CMD_BREAK;
+                    }
                 }
             } else {
                 done = true;
@@ -539,7 +556,7 @@ __global__ void k_tex_lookup(Tables t, const float2* xy, int n, int which, float
 
 // one thread per ray: the engine's closest-hit query (CSG/CSGScan.cu's _CSGScan_intersect plays this role for the
 // reference); t = -1 on a miss
-template <bool TREE, bool POLISH>
+template <int TREE, bool POLISH>
 __global__ void k_trace_rays(Accel acc, const float3* pos, const float3* dir, int n, float tmin, float tmax,
                              float* t_out, unsigned* boundary_out)
 {
@@ -664,8 +681,10 @@ struct gbo_engine {
     cudaTextureObject_t bnd_tex = 0, icdf_tex = 0;
     int bnd_nx = 0, bnd_ny = 0, hd_factor = 0;
     float nm0 = 60.f, nms = 1.f;
-    bool has_tree = false;
-    long long pool_grid[4] = {0, 0, 0, 0};  // resident blocks of k_simulate_pool per kernel form
+    int csg_form = 0;                       // 0: single-leaf prims, 1: boolean trees, 2: CSG list nodes too
+    int sms = 0;                            // streaming multiprocessors of the device
+    int pool_occ[6] = {0, 0, 0, 0, 0, 0};   // most resident blocks of k_simulate_pool per SM, per kernel form
+                                            // (index 2 x csg_form + precision)
     // event
     DBuf<gbo_quad6> gs;
     DBuf<unsigned long long> gs_end;
@@ -694,7 +713,7 @@ struct gbo_engine {
     gbo_stats stats{};
 };
 
-template <bool TREE, bool PRECISE>
+template <int TREE, bool PRECISE>
 static void launch_form(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s,
                         cudaEvent_t after_gen)
 {
@@ -703,9 +722,11 @@ static void launch_form(const gbo_engine* e, const Params& P, long long n, unsig
             k_generate<<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
             if (after_gen) cudaEventRecord(after_gen, s);
         }
-        const int form = (TREE ? 1 : 0) | (PRECISE ? 2 : 0);
+        const int form = 2 * TREE + (PRECISE ? 1 : 0);
         const long long need = (n + SIM_BLOCK - 1) / SIM_BLOCK;
-        const long long grid = need < e->pool_grid[form] ? need : e->pool_grid[form];
+        const int want = e->cfg.blocks_per_sm, occ = e->pool_occ[form] > 0 ? e->pool_occ[form] : 1;
+        const long long resident = (long long)e->sms * (want > 0 && want < occ ? want : occ);
+        const long long grid = need < resident ? need : resident;
         const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
         const int period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
         if (P.gen_photon)
@@ -725,12 +746,10 @@ static void launch_simulate(const gbo_engine* e, const Params& P, long long n, u
                             cudaEvent_t after_gen = nullptr)
 {
     const bool precise = e->cfg.precision != 0;
-    if (e->has_tree) {
-        if (precise) launch_form<true, true>(e, P, n, pool, s, after_gen);
-        else launch_form<true, false>(e, P, n, pool, s, after_gen);
-    } else {
-        if (precise) launch_form<false, true>(e, P, n, pool, s, after_gen);
-        else launch_form<false, false>(e, P, n, pool, s, after_gen);
+    switch (e->csg_form) {
+        case 2:  if (precise) launch_form<2, true>(e, P, n, pool, s, after_gen); else launch_form<2, false>(e, P, n, pool, s, after_gen); break;
+        case 1:  if (precise) launch_form<1, true>(e, P, n, pool, s, after_gen); else launch_form<1, false>(e, P, n, pool, s, after_gen); break;
+        default: if (precise) launch_form<0, true>(e, P, n, pool, s, after_gen); else launch_form<0, false>(e, P, n, pool, s, after_gen); break;
     }
 }
 
@@ -760,6 +779,7 @@ int gbo_config_default(gbo_config* c)
     c->refill_min = 4;
     c->blocks_per_sm = 0;
     c->refill_period = 1;
+    c->walk_min = 1;
     c->max_slot = 0;
     long long iv;
     float fv;
@@ -849,7 +869,27 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
         const unsigned gt = g->node[n].q3.u[3] & 0x7fffffffu;
         if (tc >= GBO_CSG_UNION && tc <= GBO_CSG_DIFFERENCE) {}
         if (gt > (unsigned)g->num_itra) return fail(GBO_ERR_ARG, "node %d transform %u beyond %d itra", n, gt, g->num_itra);
-        if (tc >= GBO_CSG_NODE && tc < GBO_CSG_LEAF) return fail(GBO_ERR_ARG, "node %d: CSG list nodes are not supported", n);
+    }
+    // list nodes: every sub a leaf inside the prim that holds the list (the device code indexes subs from the root)
+    for (int p = 0; p < g->num_prim; p++) {
+        const int noff = g->prim[p].q0.i[1], nn = g->prim[p].q0.i[0];
+        if (g->node[noff].q3.u[2] < GBO_CSG_NODE) {         // boolean tree: a complete binary tree inside the prim
+            const unsigned tree_n = g->node[noff].q0.u[0];
+            if (tree_n < 1 || tree_n > (unsigned)nn || tree_n > 255u || ((tree_n + 1) & tree_n) != 0)
+                return fail(GBO_ERR_ARG, "prim %d: tree of %u nodes in a prim of %d nodes", p, tree_n, nn);
+        }
+        for (int k = 0; k < nn; k++) {
+            const gbo_csgnode& nd = g->node[noff + k];
+            const unsigned tc = nd.q3.u[2];
+            if (tc < GBO_CSG_NODE || tc >= GBO_CSG_LEAF) continue;
+            if (tc > GBO_CSG_OVERLAP) return fail(GBO_ERR_ARG, "prim %d node %d: typecode %u is not a CSG list", p, k, tc);
+            const unsigned num_sub = nd.q0.u[0], off = nd.q0.u[1];
+            if (off < 1 || (long long)off + num_sub > (long long)nn)
+                return fail(GBO_ERR_ARG, "prim %d node %d: list subs [%u,+%u) outside the prim's %d nodes", p, k, off, num_sub, nn);
+            for (unsigned j = 0; j < num_sub; j++)
+                if (g->node[noff + off + j].q3.u[2] < GBO_CSG_LEAF)
+                    return fail(GBO_ERR_ARG, "prim %d node %d: list sub %u is not a leaf", p, k, j);
+        }
     }
 
     gbo_engine* e = new gbo_engine();
@@ -867,9 +907,12 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
         return fail(GBO_ERR_CUDA, "cudaMallocHost failed");
     }
     for (int p = 0; p < g->num_prim; p++) {
-        const int noff = g->prim[p].q0.i[1];
-        const unsigned tc = g->node[noff].q3.u[2];
-        if (tc < GBO_CSG_NODE) e->has_tree = true;
+        const int noff = g->prim[p].q0.i[1], nn = g->prim[p].q0.i[0];
+        for (int k = 0; k < nn; k++) {
+            const unsigned tc = g->node[noff + k].q3.u[2];
+            if (tc >= GBO_CSG_NODE && tc < GBO_CSG_LEAF) e->csg_form = 2;                  // a list node
+            else if (tc < GBO_CSG_NODE && k == 0 && e->csg_form < 1) e->csg_form = 1;     // a boolean tree
+        }
     }
     TRY(upload(e->tlas, acc.tlas2.data(), acc.tlas2.size(), e->stream));
     TRY(upload(e->tlas_index, acc.tlas_index.data(), acc.tlas_index.size(), e->stream));
@@ -897,17 +940,19 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     TRY(make_texture(&e->icdf_array, &e->icdf_tex, g->icdf, g->icdf_nx, g->icdf_ny, false));
     TRY(e->counters.ensure(4));
     {
-        int sms = 0, b[4] = {0, 0, 0, 0};
+        int sms = 0, b[6] = {0, 0, 0, 0, 0, 0};
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_simulate_pool<false, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_simulate_pool<true, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_simulate_pool<false, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_simulate_pool<true, true, true>, SIM_BLOCK, 0) != cudaSuccess) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_simulate_pool<0, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_simulate_pool<0, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_simulate_pool<1, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_simulate_pool<1, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[4], k_simulate_pool<2, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[5], k_simulate_pool<2, true, true>, SIM_BLOCK, 0) != cudaSuccess) {
             gbo_engine_destroy(e);
             return fail(GBO_ERR_CUDA, "occupancy query failed");
         }
-        const int want = e->cfg.blocks_per_sm;
-        for (int f = 0; f < 4; f++) e->pool_grid[f] = (long long)sms * (want > 0 && want < b[f] ? want : (b[f] > 0 ? b[f] : 1));
+        e->sms = sms;
+        for (int f = 0; f < 6; f++) e->pool_occ[f] = b[f];
     }
     if (cudaStreamSynchronize(e->stream) != cudaSuccess) {
         gbo_engine_destroy(e);
@@ -951,6 +996,7 @@ static Params make_params(gbo_engine* e)
     P.eps0_mask = e->cfg.epsilon0_mask;
     P.hitmask = e->cfg.hit_mask;
     P.seed = e->cfg.rng_seed;
+    P.walk_min = e->cfg.walk_min < 1 ? 1 : (e->cfg.walk_min > 32 ? 32 : e->cfg.walk_min);
     return P;
 }
 
@@ -1295,11 +1341,17 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
     if (!e || !out) return fail(GBO_ERR_ARG, "gbo_autotune: null argument");
     if (trials < 1) trials = 1;
     std::memset(out, 0, sizeof(*out));
-    struct Cand { int mode, refill, period; };
-    std::vector<Cand> cands = {{1, 32, 1}};
+    // candidates: (kernel mode, refill threshold, refill period, resident blocks per SM; 0 = the occupancy maximum)
+    struct Cand { int mode, refill, period, blocks; };
+    std::vector<Cand> cands = {{1, 32, 1, 0}};
     for (int r : {1, 2, 4, 8, 16, 32})
-        for (int p : {1, 4}) cands.push_back({0, r, p});
-    for (int r : {1, 2, 4, 8, 16}) cands.push_back({2, r, 1});
+        for (int p : {1, 4}) cands.push_back({0, r, p, 0});
+    for (int r : {1, 2, 4, 8, 16}) cands.push_back({2, r, 1, 0});
+    const int form = 2 * e->csg_form + (e->cfg.precision ? 1 : 0);
+    for (int b = 1; b < e->pool_occ[form] && cands.size() < 32; b++) {       // fewer resident blocks than fit
+        cands.push_back({2, 4, 1, b});
+        if (cands.size() < 32) cands.push_back({0, 4, 1, b});
+    }
     const gbo_config saved = e->cfg;
     float best = 1e30f;
     Cand pick = cands[0];
@@ -1307,6 +1359,7 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         e->cfg.kernel_mode = cands[c].mode;
         e->cfg.refill_min = cands[c].refill;
         e->cfg.refill_period = cands[c].period;
+        e->cfg.blocks_per_sm = cands[c].blocks;
         float ms = 1e30f;
         for (int t = 0; t <= trials; t++) {
             int rc = gbo_simulate(e, event_id, gs, num_gs, input_photon, num_input_photon);
@@ -1316,6 +1369,7 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         out->cand_mode[c] = cands[c].mode;
         out->cand_refill[c] = cands[c].refill;
         out->cand_period[c] = cands[c].period;
+        out->cand_blocks[c] = cands[c].blocks;
         out->cand_ms[c] = ms;
         out->num_candidates = (int32_t)(c + 1);
         if (ms < best) { best = ms; pick = cands[c]; }
@@ -1324,9 +1378,11 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
     e->cfg.kernel_mode = pick.mode;
     e->cfg.refill_min = pick.refill;
     e->cfg.refill_period = pick.period;
+    e->cfg.blocks_per_sm = pick.blocks;
     out->kernel_mode = pick.mode;
     out->refill_min = pick.refill;
     out->refill_period = pick.period;
+    out->blocks_per_sm = pick.blocks;
     return GBO_OK;
 }
 
@@ -1389,7 +1445,7 @@ int gbo_trace_rays(gbo_engine* e, const float* pos, const float* dir, int32_t n,
     std::memcpy(in.data(), pos, (size_t)n * 12);
     std::memcpy(in.data() + (size_t)n * 3, dir, (size_t)n * 12);
     std::vector<float> out((size_t)n * 2);
-    const int form = (e->has_tree ? 1 : 0) | (e->cfg.precision ? 2 : 0);
+    const int form = 2 * e->csg_form + (e->cfg.precision ? 1 : 0);
     int rc = with_scratch(in.size() * 4, in.data(), out.size() * 4, out.data(), [&](void* d_in, void* d_out) {
         const float3* dp = (const float3*)d_in;
         const float3* dd = (const float3*)((float*)d_in + (size_t)n * 3);
@@ -1397,10 +1453,12 @@ int gbo_trace_rays(gbo_engine* e, const float* pos, const float* dir, int32_t n,
         unsigned* db = (unsigned*)((float*)d_out + n);
         const unsigned g = (unsigned)((n + 127) / 128);
         switch (form) {
-            case 0: k_trace_rays<false, false><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
-            case 1: k_trace_rays<true, false><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
-            case 2: k_trace_rays<false, true><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
-            default: k_trace_rays<true, true><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            case 0: k_trace_rays<0, false><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            case 1: k_trace_rays<0, true><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            case 2: k_trace_rays<1, false><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            case 3: k_trace_rays<1, true><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            case 4: k_trace_rays<2, false><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            default: k_trace_rays<2, true><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
         }
     });
     if (rc) return rc;
@@ -1458,7 +1516,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
 // The one-thread-per-photon program with a bounded hit append: hits beyond the staging capacity are counted
 // but not stored, and the host reports the overflow.
-template <bool TREE>
+template <int TREE>
 __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_bounded(const __grid_constant__ Params P, long long cap)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1589,8 +1647,9 @@ int gbo_simulate_noalloc(gbo_engine* e, int32_t event_id, const void* d_gs, int6
     const long long nblk = (words + SCAN_WORDS - 1) / SCAN_WORDS;
     if (total > 0) {
         const long long blocks = ((long long)total + SIM_BLOCK - 1) / SIM_BLOCK;
-        if (e->has_tree) k_simulate_bounded<true><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P, NA_MAX_HIT);
-        else k_simulate_bounded<false><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P, NA_MAX_HIT);
+        if (e->csg_form == 2) k_simulate_bounded<2><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P, NA_MAX_HIT);
+        else if (e->csg_form == 1) k_simulate_bounded<1><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P, NA_MAX_HIT);
+        else k_simulate_bounded<0><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P, NA_MAX_HIT);
         CU(cudaGetLastError());
         k_word_prefix<<<(unsigned)nblk, SCAN_WORDS, 0, s>>>(bitmap, words, word_prefix, block_sum);
         k_block_offsets<<<1, 1024, 0, s>>>(block_sum, nblk, block_offset, counters + 1);

@@ -116,9 +116,10 @@ GBO_DEV InstDev load_inst(const InstDev* p)
     return d;
 }
 
+// TREE: 0 when every prim is a single leaf, 1 with boolean trees, 2 with CSG list nodes as well
 // POLISH (precision mode): binary64 Newton polish of the quadric roots of sphere, zsphere and cylinder leaves
 // d_inv (optional): the correctly rounded reciprocals of d's components, for a single box3 leaf to reuse
-template <bool TREE, bool POLISH>
+template <int TREE, bool POLISH>
 GBO_DEV bool prim_hit(float4& is, const Accel& a, int node_word, float t_min, float3 o, float3 d,
                       const float3* d_inv = nullptr)
 {
@@ -128,7 +129,7 @@ GBO_DEV bool prim_hit(float4& is, const Accel& a, int node_word, float t_min, fl
             const int r = intersect_union_enter(is, root, a.plan, a.itra, t_min, o, d, POLISH);
             if (r >= 0) return r == 1;
         }
-        return intersect_prim(is, root, a.plan, a.itra, t_min, o, d, POLISH);
+        return intersect_prim<(TREE >= 2)>(is, root, a.plan, a.itra, t_min, o, d, POLISH);
     }
     if (node_typecode(root) >= GBO_CSG_LEAF) return intersect_leaf(is, root, a.plan, a.itra, t_min, o, d, POLISH, d_inv);
     is = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -143,7 +144,7 @@ struct Best {
     unsigned pb;
 };
 
-template <bool TREE, bool POLISH>
+template <int TREE, bool POLISH>
 GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float tmin, Best& b)
 {
     const InstDev d = load_inst(a.inst + ii);
@@ -164,6 +165,10 @@ GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float
         if (!have64) { inst_ray64(a.inst64 + 12 * (size_t)ii, pos, dir, po, pd); have64 = true; }
         // the prim-box reciprocals are those of the ray the leaf sees unless the precision mode re-transformed it
         if (!prim_hit<TREE, POLISH>(is, a, __float_as_int(pb0.w), tmin, po, pd, POLISH ? nullptr : &oinv)) continue;
+        // OptiX accepts a reported hit only inside the ray's [tmin, tmax] interval: a convex polyhedron behind the
+        // ray reports a valid t of 0 (csg_intersect_leaf_convexpolyhedron.h:87-104 writes no t when both planes
+        // lie at or below t_min)
+        if (!(is.w >= tmin)) continue;
         const unsigned key = ((unsigned)ii << 16) | (unsigned)k2;
         if (is.w < b.t || (is.w == b.t && b.key != 0xffffffffu && key < b.key)) {
             b.t = is.w; b.key = key; b.is = is; b.inst = ii; b.pb = __float_as_uint(pb1.w);
@@ -189,7 +194,143 @@ GBO_DEV int pop_item(const int* stack, int& sp, bool& root_next)
     return item;
 }
 
-template <bool TREE, bool POLISH = false>
+enum { TRACE_DONE = 0, TRACE_WALK = 1 };
+
+// The query's item loop, from the hint instance (or from the TLAS root when there is none), the best hit kept in
+// `b` (set by trace_begin).  With stop_at_root the loop returns TRACE_WALK instead of entering the TLAS: the caller
+// defers the query (the photon-pool kernel gathers the walks of several lanes of a warp so that they run together)
+// and runs it again later without the stop; the result is that of one uninterrupted query.
+template <int TREE, bool POLISH>
+GBO_DEV int trace_items(const Accel& a, float3 pos, float3 dir, float tmin, int hint, bool stop_at_root, Best& b)
+{
+    // the world-frame reciprocal direction serves the TLAS and list-neighbour box tests, which a step that stays
+    // inside its hint instance never reaches: computed on the way out of the hint item
+    float3 inv = f3(0.f, 0.f, 0.f);
+    int stack[TRAVERSAL_STACK];
+    int sp = 0;
+    constexpr int NONE = ITEM_NONE;
+    int item = 0;
+    int ov_first = 0;
+    bool root_next = false;         // the TLAS root waits under the hint item (kept out of the local-memory stack)
+    if (hint >= 0) {
+        root_next = true;
+        item = leaf_item(HINT_FIRST, 1);
+    } else {
+        if (stop_at_root) return TRACE_WALK;
+        inv = safe_inv(dir);
+    }
+    // while-while traversal (Aila & Laine 2009): every lane first descends inner nodes until it holds a leaf, then
+    // the lanes process their leaves together, so the expensive instance / CSG work runs with the warp converged;
+    // each lane still visits its items in the same order as a one-item-per-iteration loop.  Leaf items are TLAS
+    // leaves, the photon's previous instance (HINT_FIRST) or that instance's overlap list (OVERLAP_FIRST), all
+    // tested at the single test_instance call site.
+    while (item != NONE) {
+        while (item >= 0) {
+            const float4* nq = reinterpret_cast<const float4*>(a.tlas + item);
+            const float4 l0 = __ldg(nq), h0 = __ldg(nq + 1), l1 = __ldg(nq + 2), h1 = __ldg(nq + 3);
+            float t0, t1;
+            const int c0 = __float_as_int(h0.w), c1 = __float_as_int(h1.w);
+            const bool v0 = c0 >= 0 && slab(l0, h0, pos, inv, tmin, b.t, t0);
+            const bool v1 = c1 >= 0 && slab(l1, h1, pos, inv, tmin, b.t, t1);
+            const int it0 = c0 > 0 ? leaf_item(__float_as_int(l0.w), c0) : __float_as_int(l0.w);
+            const int it1 = c1 > 0 ? leaf_item(__float_as_int(l1.w), c1) : __float_as_int(l1.w);
+            if (v0 && v1) {                         // nearer child next, the other on the stack
+                const bool near0 = t0 <= t1;
+                item = near0 ? it0 : it1;
+                if (sp < TRAVERSAL_STACK) stack[sp++] = near0 ? it1 : it0;
+            } else if (v0) {
+                item = it0;
+            } else if (v1) {
+                item = it1;
+            } else {
+                item = pop_item(stack, sp, root_next);
+            }
+        }
+        while (item < 0 && item != NONE) {
+            const int code = -item - 1;
+            const int first = code >> 8, count = code & 0xff;
+#pragma unroll 1
+            for (int k = 0; k < count; k++) {
+                const int ii = first == HINT_FIRST ? hint
+                             : first == OVERLAP_FIRST ? __ldg(a.overlap + ov_first + k) : __ldg(a.tlas_index + first + k);
+                if (first < OVERLAP_FIRST && ii == hint) continue;
+                if (first == OVERLAP_FIRST || count > 1) {
+                    // the instance's padded world box first: a list neighbour or a leaf sibling whose box the
+                    // segment (tmin, best] misses holds no closer hit, and skips the transform and prim tests
+                    const float4 wlo = __ldg(a.inst_box + 2 * ii), whi = __ldg(a.inst_box + 2 * ii + 1);
+                    float tn;
+                    if (!slab(wlo, whi, pos, inv, tmin, b.t, tn)) continue;
+                }
+                test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b);
+            }
+            if (first == HINT_FIRST) {
+                // when the previous instance's closest hit keeps the whole segment inside its box, only the instances
+                // whose boxes overlap that box can hold a closer hit: their short list replaces the TLAS
+                const float4 blo = __ldg(a.inst_box + 2 * hint), bhi = __ldg(a.inst_box + 2 * hint + 1);
+                const int ocount = __float_as_int(bhi.w);
+                const float3 e = pos + b.t * dir;
+                if (ocount >= 0 && inside_box(blo, bhi, pos) && inside_box(blo, bhi, e)) {
+                    ov_first = __float_as_int(blo.w);
+                    sp = 0;
+                    root_next = false;
+                    item = NONE;
+                    if (ocount > 0) { item = leaf_item(OVERLAP_FIRST, ocount); inv = safe_inv(dir); }
+                    continue;
+                }
+                // a container (long overlap list): a segment inside its clear ball meets no other instance
+                if (ocount < 0) {
+                    const float4 cb = __ldg(a.clear + hint);
+                    if (cb.w > 0.f && inside_ball(cb, pos) && inside_ball(cb, e)) {
+                        sp = 0;
+                        root_next = false;
+                        item = NONE;
+                        continue;
+                    }
+                }
+                if (stop_at_root) return TRACE_WALK;      // the TLAS walk, deferred by the caller
+                inv = safe_inv(dir);                // the TLAS walk follows
+            }
+            item = pop_item(stack, sp, root_next);
+        }
+    }
+    return TRACE_DONE;
+}
+
+GBO_DEV void trace_begin(Best& b, float tmax)
+{
+    b.t = tmax; b.key = 0xffffffffu; b.is = make_float4(0.f, 0.f, 0.f, 0.f); b.inst = -1; b.pb = 0u;
+}
+
+// The hit record of a finished query: closest-hit packing of CSGOptiX7.cu:749-847 (normal to the world frame,
+// instance-frame z for the lpos sign, iindex|identity, globalPrimIdx|boundary) or the miss record.
+GBO_DEV void trace_finish(const Accel& a, float3 pos, float3 dir, const Best& b, Hit& h)
+{
+    if (b.inst < 0) {
+        h.normal = f3(0.f, 0.f, 0.f);
+        h.t = 1.f;
+        h.lposz = 0.f;
+        h.iindex_identity = 0xffffffffu;
+        h.prim_boundary = 0xffffffffu;
+        return;
+    }
+    const InstDev d = load_inst(a.inst + b.inst);
+    float3 n = f3(b.is.x, b.is.y, b.is.z);
+    float lz;
+    if (d.is_identity) {
+        lz = pos.z + b.is.w * dir.z;
+    } else {
+        n = inst_normal(d, n);
+        lz = (d.c2[0] * pos.x + d.c2[1] * pos.y + d.c2[2] * pos.z + d.c2[3]) +
+             b.is.w * (d.c2[0] * dir.x + d.c2[1] * dir.y + d.c2[2] * dir.z);
+    }
+    h.normal = n;
+    h.t = b.is.w;
+    h.lposz = lz;
+    h.iindex_identity = ((d.iindex & 0xffffu) << 16) | (d.identity & 0xffffu);
+    h.prim_boundary = b.pb;
+}
+
+template <int TREE, bool POLISH = false>
 GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tmax, int hint, Hit& h)
 {
     Best b;

@@ -43,13 +43,14 @@ class Config(C.Structure):
                 ("tmax", C.c_float), ("debug_tag", C.c_int32), ("record_photon", C.c_int32),
                 ("record_seq", C.c_int32), ("max_photon", C.c_int64), ("kernel_mode", C.c_int32),
                 ("refill_min", C.c_int32), ("blocks_per_sm", C.c_int32), ("refill_period", C.c_int32),
-                ("max_slot", C.c_int64), ("precision", C.c_int32), ("reserved", C.c_int32)]
+                ("max_slot", C.c_int64), ("precision", C.c_int32), ("walk_min", C.c_int32)]
 
 
 class TuneResult(C.Structure):
     _fields_ = [("kernel_mode", C.c_int32), ("refill_min", C.c_int32), ("refill_period", C.c_int32),
                 ("num_candidates", C.c_int32), ("cand_mode", C.c_int32 * 32), ("cand_refill", C.c_int32 * 32),
-                ("cand_period", C.c_int32 * 32), ("cand_ms", C.c_float * 32)]
+                ("cand_period", C.c_int32 * 32), ("cand_ms", C.c_float * 32), ("blocks_per_sm", C.c_int32),
+                ("cand_blocks", C.c_int32 * 32)]
 
 
 class Stats(C.Structure):
@@ -65,11 +66,13 @@ EXPORTS = ["gbo_config_default", "gbo_engine_create", "gbo_engine_destroy", "gbo
 _lib = None
 
 
-def load(path=LIB):
-    """Load the library (built by ``eic_opticks_gb300.build``); raises if it is missing."""
+def load(path=None):
+    """Load the library (built by ``eic_opticks_gb300.build``); raises if it is missing.  GBO_ENGINE_LIBRARY may
+    name another build of the same sources (the parity tests' --fmad=false build)."""
     global _lib
     if _lib is not None:
         return _lib
+    path = path or os.environ.get("GBO_ENGINE_LIBRARY") or LIB
     if not os.path.exists(path):
         raise GBOError("libgbopticks.so not built (%s): run __graft_entry__.build()" % path)
     lib = C.CDLL(path)
@@ -238,10 +241,12 @@ class Engine:
         _check(self.lib.gbo_autotune(self.handle, int(event_id), gs.ctypes.data_as(C.c_void_p), len(gs),
                                      inp.ctypes.data_as(C.c_void_p) if inp is not None else None,
                                      len(inp) if inp is not None else 0, int(trials), C.byref(r)), "gbo_autotune")
-        cands = [dict(mode=r.cand_mode[i], refill=r.cand_refill[i], period=r.cand_period[i], ms=r.cand_ms[i])
-                 for i in range(r.num_candidates)]
+        cands = [dict(mode=r.cand_mode[i], refill=r.cand_refill[i], period=r.cand_period[i],
+                      blocks_per_sm=r.cand_blocks[i], ms=r.cand_ms[i]) for i in range(r.num_candidates)]
         self.config.kernel_mode, self.config.refill_min, self.config.refill_period = r.kernel_mode, r.refill_min, r.refill_period
-        return dict(kernel_mode=r.kernel_mode, refill_min=r.refill_min, refill_period=r.refill_period, candidates=cands)
+        self.config.blocks_per_sm = r.blocks_per_sm
+        return dict(kernel_mode=r.kernel_mode, refill_min=r.refill_min, refill_period=r.refill_period,
+                    blocks_per_sm=r.blocks_per_sm, candidates=cands)
 
     def texture_lookup(self, which, xy):
         xy = np.ascontiguousarray(xy, dtype=np.float32)

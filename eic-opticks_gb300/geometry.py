@@ -191,6 +191,15 @@ def operation(op, left, right):
     return dict(typecode=op, left=left, right=right)
 
 
+def csg_list(typecode, leaves):
+    """A CSG list node (CSG_CONTIGUOUS multi-union of overlapping leaves, CSG_DISCONTIGUOUS union of disjoint
+    leaves, CSG_OVERLAP multi-intersection; CSG/csg_intersect_node.h): a prim of its own or a leaf of a boolean
+    tree.  Its leaves are stored after the prim's tree nodes and addressed by subNum / subOffset (CSGNode.h:210)."""
+    assert typecode in (L.CSG_CONTIGUOUS, L.CSG_DISCONTIGUOUS, L.CSG_OVERLAP) and leaves
+    assert all("left" not in x and "subs" not in x for x in leaves)
+    return dict(typecode=typecode, subs=list(leaves))
+
+
 def _transform_bbox(bb, m):
     if m is None:
         return bb
@@ -265,6 +274,7 @@ class Geometry:
             nodes = _tree_nodes(tree) if "left" in tree else [tree]
             node_offset = len(self._nodes)
             bbs = []
+            subs = []                      # leaves of list nodes, stored after the tree nodes
             for nd in nodes:
                 rec = np.zeros((4, 4), dtype=np.float32)
                 ints = rec.view(np.uint32)
@@ -274,36 +284,39 @@ class Geometry:
                 elif "left" in nd:
                     ints[3, 2] = nd["typecode"]
                     ints[1, 2] = bnd
-                else:
-                    rec[0, :] = nd["q0"]
-                    rec[1, 0:2] = nd["q1xy"]
-                    if nd.get("planes") is not None:             # planeIdx, planeNum (CSGNode::setPlaneIdx/Num)
-                        ints[0, 0] = len(self.plan)
-                        ints[0, 1] = len(nd["planes"])
-                        self.plan = np.concatenate([self.plan, nd["planes"].astype(np.float32)])
-                    ints[1, 2] = bnd
+                elif "subs" in nd:
                     ints[3, 2] = nd["typecode"]
-                    tidx = 0
-                    if nd.get("transform") is not None:
-                        self._tran.append(nd["transform"])
-                        tidx = len(self._tran)          # 1-based
-                    ints[3, 3] = (tidx & 0x7FFFFFFF) | (0x80000000 if nd.get("complement") else 0)
-                    bb = _transform_bbox(nd["bbox"], nd.get("transform"))
+                    ints[1, 2] = bnd
+                    ints[0, 0] = len(nd["subs"])                 # subNum
+                    ints[0, 1] = len(nodes) + len(subs)          # subOffset from the prim's root
+                    sb = np.array([_transform_bbox(x["bbox"], x.get("transform")) for x in nd["subs"]])
+                    bb = (*sb[:, 0:3].min(axis=0), *sb[:, 3:6].max(axis=0))
+                    if nd["typecode"] == L.CSG_OVERLAP:         # an intersection lies inside every leaf
+                        bb = (*sb[:, 0:3].max(axis=0), *sb[:, 3:6].min(axis=0))
                     rec[2, :] = bb[0:4]
                     rec[3, 0:2] = bb[4:6]
-                    if not nd.get("complement"):
+                    bbs.append(bb)
+                    subs.extend(nd["subs"])
+                else:
+                    rec, bb = self._leaf_record(nd, bnd)
+                    if bb is not None:
                         bbs.append(bb)
+                    ints = rec.view(np.uint32)
                 ints[1, 3] = len(self._nodes) - node_offset
                 self._nodes.append(rec)
             if len(nodes) > 1:
                 self._nodes[node_offset].view(np.uint32)[0, 0] = len(nodes)   # subNum on the root
                 self._nodes[node_offset].view(np.uint32)[0, 1] = 0
+            for leaf in subs:
+                rec, _ = self._leaf_record(leaf, bnd)
+                rec.view(np.uint32)[1, 3] = len(self._nodes) - node_offset
+                self._nodes.append(rec)
             bb = np.array(bbs)
             plo, phi = bb[:, 0:3].min(axis=0), bb[:, 3:6].max(axis=0)
             lo, hi = np.minimum(lo, plo), np.maximum(hi, phi)
             prec = np.zeros((4, 4), dtype=np.float32)
             pi = prec.view(np.int32)
-            pi[0, 0] = len(nodes)
+            pi[0, 0] = len(nodes) + len(subs)
             pi[0, 1] = node_offset
             pu = prec.view(np.uint32)
             pu[1, 2] = len(self._solids)
@@ -317,6 +330,28 @@ class Geometry:
         extent = float(np.max(hi - lo) / 2)
         self._solids.append((label, len(prims), prim_offset, (*center, extent)))
         return len(self._solids) - 1
+
+    def _leaf_record(self, nd, bnd):
+        """The CSGNode record of a leaf and its bounding box (None for a complemented leaf)."""
+        rec = np.zeros((4, 4), dtype=np.float32)
+        ints = rec.view(np.uint32)
+        rec[0, :] = nd["q0"]
+        rec[1, 0:2] = nd["q1xy"]
+        if nd.get("planes") is not None:             # planeIdx, planeNum (CSGNode::setPlaneIdx/Num)
+            ints[0, 0] = len(self.plan)
+            ints[0, 1] = len(nd["planes"])
+            self.plan = np.concatenate([self.plan, nd["planes"].astype(np.float32)])
+        ints[1, 2] = bnd
+        ints[3, 2] = nd["typecode"]
+        tidx = 0
+        if nd.get("transform") is not None:
+            self._tran.append(nd["transform"])
+            tidx = len(self._tran)          # 1-based
+        ints[3, 3] = (tidx & 0x7FFFFFFF) | (0x80000000 if nd.get("complement") else 0)
+        bb = _transform_bbox(nd["bbox"], nd.get("transform"))
+        rec[2, :] = bb[0:4]
+        rec[3, 0:2] = bb[4:6]
+        return rec, (None if nd.get("complement") else bb)
 
     def add_instance(self, solid, transform=None, sensor_identifier=-1, sensor_index=-1):
         m = np.eye(4) if transform is None else np.asarray(transform, dtype=np.float64)

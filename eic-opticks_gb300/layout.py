@@ -67,6 +67,7 @@ T_DISC, T_LINE, T_POINT, T_CIRCLE, T_RECTANGLE, T_SPHERE_MARSAGLIA, T_SPHERE = 1
 CSG_ZERO, CSG_UNION, CSG_INTERSECTION, CSG_DIFFERENCE = 0, 1, 2, 3
 CSG_SPHERE, CSG_ZSPHERE, CSG_CYLINDER, CSG_CONE, CSG_BOX3 = 101, 103, 105, 108, 110
 CSG_CONVEXPOLYHEDRON, CSG_HYPERBOLOID, CSG_PHICUT, CSG_HALFSPACE = 112, 117, 121, 125
+CSG_CONTIGUOUS, CSG_DISCONTIGUOUS, CSG_OVERLAP = 11, 12, 13          # list nodes (csg_intersect_node.h)
 
 # ems surface types : sysrap/smatsur.h:8-15
 EMS_MATERIAL, EMS_NOSURFACE, EMS_SURFACE, EMS_ZPLUS_SENSOR_A = 0, 1, 2, 3

@@ -87,14 +87,19 @@ typedef struct gbo_config {
     int32_t  precision;             /* 0: binary32 as the reference (default); 1: binary64 Newton polish of every
                                        accepted sphere / zsphere / cylinder root and binary64 position/time
                                        accumulators */
-    int32_t  reserved;
+    int32_t  walk_min;              /* pool kernels: a lane whose step needs a walk of the instance tree parks until
+                                       this many lanes of its warp need one (or no other lane can step), so the walks
+                                       run together; 1: no parking (1) */
 } gbo_config;
 
-/* Result of gbo_autotune: the kernel form chosen and the simulate time of every candidate tried. */
+/* Result of gbo_autotune: the kernel form chosen (kernel mode, refill threshold, refill period = compaction period,
+ * resident blocks per SM = block shape, 0 meaning the occupancy maximum) and the simulate time of every candidate. */
 typedef struct gbo_tune_result {
     int32_t kernel_mode, refill_min, refill_period, num_candidates;
     int32_t cand_mode[32], cand_refill[32], cand_period[32];
     float   cand_ms[32];
+    int32_t blocks_per_sm;
+    int32_t cand_blocks[32];
 } gbo_tune_result;
 
 typedef struct gbo_stats {
@@ -144,7 +149,9 @@ const char* gbo_last_error(void);
 
 /* gbo_autotune : no counterpart in the reference (its launch shape is fixed by OptiX).  Runs the given sample
  * event with every candidate kernel form (one thread per photon; photon pool with refill thresholds 1..32 and
- * refill periods 1, 4), `trials` timed runs each after one warm-up, and keeps the fastest in the engine's config. */
+ * refill periods 1, 4; pool over pregenerated photons with refill thresholds 1..16; both pools with fewer resident
+ * blocks per SM than fit), `trials` timed runs each after one warm-up, and keeps the fastest in the engine's
+ * config.  Every candidate gives the same photons (the kernel form decides only which lane runs a photon, when). */
 int         gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs,
                          const gbo_sphoton* input_photon, int64_t num_input_photon, int32_t trials,
                          gbo_tune_result* out);

@@ -159,9 +159,13 @@ def simulate(cfg, gs, input_photon=None, event_index=0, photon_offset=0, nthread
 _refdev = None
 
 
-def ref_device_available():
-    """True when the reference-header device build (ref_device.cubin) is present."""
-    return os.path.exists(REFDEV_CUBIN)
+def ref_device_cubin(variant=""):
+    return REFDEV_CUBIN if not variant else os.path.join(HERE, "_ref", "ref_device_%s.cubin" % variant)
+
+
+def ref_device_available(variant=""):
+    """True when the reference-header device build (ref_device[_variant].cubin) is present."""
+    return os.path.exists(ref_device_cubin(variant))
 
 
 def ref_device_lib():
@@ -175,13 +179,15 @@ def ref_device_lib():
     return _refdev
 
 
-def ref_device_simulate(cfg, gs, input_photon=None, event_index=0):
+def ref_device_simulate(cfg, gs, input_photon=None, event_index=0, variant=""):
     """Run the reference's own headers, compiled by nvcc for the GPU (ref_device.cu), over every photon of ``gs``
-    on the current GPU, one thread per photon.  Returns (photons, seq, kernel_ms)."""
+    on the current GPU, one thread per photon.  variant "nofma": the build without multiply-add contraction.
+    Returns (photons, seq, kernel_ms)."""
     from importlib import import_module
     L = import_module("eic_opticks_gb300.layout")
-    if not ref_device_available():
-        raise RuntimeError("reference device build oracle/_ref/ref_device.cubin not present")
+    cubin = ref_device_cubin(variant)
+    if not os.path.exists(cubin):
+        raise RuntimeError("reference device build %s not present" % cubin)
     gs = np.ascontiguousarray(gs, dtype=np.float32)
     counts = gs.view(np.uint32)[:, 0, 3].astype(np.int64)
     seed = np.ascontiguousarray(np.repeat(np.arange(len(gs), dtype=np.int32), counts))
@@ -196,7 +202,7 @@ def ref_device_simulate(cfg, gs, input_photon=None, event_index=0):
                      dtype=np.int32)
     ms = C.c_float(0.0)
     lib_ = ref_device_lib()
-    rc = lib_.ref_device_simulate(REFDEV_CUBIN.encode(), C.byref(cfg.sim), _ptr(sizes), _ptr(gs), C.c_int64(len(gs)),
+    rc = lib_.ref_device_simulate(cubin.encode(), C.byref(cfg.sim), _ptr(sizes), _ptr(gs), C.c_int64(len(gs)),
                                   _ptr(seed), _ptr(input_photon) if input_photon is not None else None,
                                   C.c_uint64(0), C.c_int32(event_index), C.c_int64(n), _ptr(out), _ptr(sq),
                                   C.byref(ms))

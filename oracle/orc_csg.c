@@ -434,6 +434,131 @@ static inline int classify(v4 ise, v3 dir, float tmin)
     return fabsf(ise.w) > tmin ? (ise.x * dir.x + ise.y * dir.y + ise.z * dir.z < 0.f ? ST_ENTER : ST_EXIT) : ST_MISS;
 }
 
+/* ---- list nodes : csg_intersect_node.h (compiled WITH_CONTIGUOUS in the reference's OptiX build) ----
+ * A header node lists subNum (q0.u[0]) leaves at root + subOffset (q0.u[1]). */
+#define LIST_EPSILON 0.0001f
+#define LIST_MAX_ENTER 8      /* enter slots of intersect_node_contiguous */
+
+/* intersect_node_contiguous : csg_intersect_node.h:390-626 */
+static int list_contiguous(v4* isect, const gbo_csgnode* node, const gbo_csgnode* root, const float* plan,
+                           const gbo_qat4* itra, float t_min, v3 ro, v3 rd)
+{
+    const int num_sub = (int)node->q0.u[0];
+    const int offset_sub = (int)node->q0.u[1];
+    v4 nearest_enter = V4(0.f, 0.f, 0.f, RT_DEFAULT_MAX);
+    v4 farthest_exit = V4(0.f, 0.f, 0.f, t_min);
+    v4 sub;
+    int exit_count = 0;
+    for (int i = 0; i < num_sub; i++) {                       /* zeroth pass: nearest enter, count exits */
+        if (!intersect_leaf(&sub, root + offset_sub + i, plan, itra, t_min, ro, rd)) continue;
+        int st = classify(sub, rd, t_min);
+        if (st == ST_ENTER) { if (sub.w < nearest_enter.w) nearest_enter = sub; }
+        else if (st == ST_EXIT) exit_count += 1;
+    }
+    if (exit_count == 0) {                                    /* outside the compound */
+        int valid = nearest_enter.w > t_min && nearest_enter.w < RT_DEFAULT_MAX;
+        if (valid) *isect = nearest_enter;
+        return valid;
+    }
+    int enter_count = 0;
+    float enter[LIST_MAX_ENTER];
+    int which[LIST_MAX_ENTER], order[LIST_MAX_ENTER];
+    for (int i = 0; i < num_sub; i++) {                       /* first pass: enters, farthest first exit */
+        if (!intersect_leaf(&sub, root + offset_sub + i, plan, itra, t_min, ro, rd)) continue;
+        int st = classify(sub, rd, t_min);
+        if (st == ST_ENTER) {
+            if (enter_count < LIST_MAX_ENTER) {
+                which[enter_count] = i;
+                order[enter_count] = enter_count;
+                enter[enter_count] = sub.w;
+                enter_count += 1;
+            }
+        } else if (st == ST_EXIT) {
+            exit_count += 1;
+            if (sub.w > farthest_exit.w) farthest_exit = sub;
+        }
+    }
+    for (int i = 1; i < enter_count; i++) {                  /* enter slots by ascending distance */
+        int key = order[i];
+        int j = i - 1;
+        while (j >= 0 && enter[order[j]] > enter[key]) { order[j + 1] = order[j]; j -= 1; }
+        order[j + 1] = key;
+    }
+    for (int i = 0; i < enter_count; i++) {                   /* second pass: exits of contiguous enters */
+        float t_adv = enter[order[i]] + LIST_EPSILON;
+        if (!(t_adv < farthest_exit.w)) continue;
+        if (!intersect_leaf(&sub, root + offset_sub + which[order[i]], plan, itra, t_adv, ro, rd)) continue;
+        if (classify(sub, rd, t_adv) == ST_EXIT) {
+            exit_count += 1;
+            if (sub.w > farthest_exit.w) farthest_exit = sub;
+        }
+    }
+    int valid = exit_count > 0 && farthest_exit.w > t_min;
+    if (valid) *isect = farthest_exit;
+    return valid;
+}
+
+/* intersect_node_discontiguous : csg_intersect_node.h:654-686 */
+static int list_discontiguous(v4* isect, const gbo_csgnode* node, const gbo_csgnode* root, const float* plan,
+                              const gbo_qat4* itra, float t_min, v3 ro, v3 rd)
+{
+    const int num_sub = (int)node->q0.u[0];
+    const int offset_sub = (int)node->q0.u[1];
+    v4 closest = V4(0.f, 0.f, 0.f, RT_DEFAULT_MAX);
+    v4 sub;
+    for (int i = 0; i < num_sub; i++)
+        if (intersect_leaf(&sub, root + offset_sub + i, plan, itra, t_min, ro, rd) && sub.w < closest.w) closest = sub;
+    int valid = closest.w < RT_DEFAULT_MAX;
+    if (valid) *isect = closest;
+    return valid;
+}
+
+/* intersect_node_overlap : csg_intersect_node.h:819-895 */
+static int list_overlap(v4* isect, const gbo_csgnode* node, const gbo_csgnode* root, const float* plan,
+                        const gbo_qat4* itra, float t_min, v3 ro, v3 rd)
+{
+    const unsigned num_sub = node->q0.u[0];
+    const unsigned offset_sub = node->q0.u[1];
+    v4 farthest_enter = V4(0.f, 0.f, 0.f, t_min);
+    v4 nearest_exit = V4(0.f, 0.f, 0.f, RT_DEFAULT_MAX);
+    v4 sub;
+    unsigned enter_count = 0, exit_count = 0;
+    for (unsigned i = 0; i < num_sub; i++) {
+        const gbo_csgnode* leaf = root + offset_sub + i;
+        if (!intersect_leaf(&sub, leaf, plan, itra, t_min, ro, rd)) continue;
+        int st = classify(sub, rd, t_min);
+        if (st == ST_ENTER) {
+            enter_count += 1;
+            if (sub.w > farthest_enter.w) farthest_enter = sub;
+            float t_adv = sub.w + LIST_EPSILON;
+            if (intersect_leaf(&sub, leaf, plan, itra, t_adv, ro, rd) && classify(sub, rd, t_adv) == ST_EXIT) {
+                exit_count += 1;
+                if (sub.w < nearest_exit.w) nearest_exit = sub;
+            }
+        } else if (st == ST_EXIT) {
+            exit_count += 1;
+            if (sub.w < nearest_exit.w) nearest_exit = sub;
+        }
+    }
+    unsigned most = enter_count > exit_count ? enter_count : exit_count;
+    if (!(farthest_enter.w < nearest_exit.w && most == num_sub)) return 0;
+    if (farthest_enter.w > t_min && farthest_enter.w < RT_DEFAULT_MAX) { *isect = farthest_enter; return 1; }
+    if (nearest_exit.w > t_min && nearest_exit.w < RT_DEFAULT_MAX) { *isect = nearest_exit; return 1; }
+    return 0;
+}
+
+/* intersect_node : csg_intersect_node.h:913-938 */
+static int intersect_node(v4* isect, const gbo_csgnode* node, const gbo_csgnode* root, const float* plan,
+                          const gbo_qat4* itra, float t_min, v3 ro, v3 rd)
+{
+    switch (nd_typecode(node)) {
+        case GBO_CSG_CONTIGUOUS:    return list_contiguous(isect, node, root, plan, itra, t_min, ro, rd);
+        case GBO_CSG_OVERLAP:       return list_overlap(isect, node, root, plan, itra, t_min, ro, rd);
+        case GBO_CSG_DISCONTIGUOUS: return list_discontiguous(isect, node, root, plan, itra, t_min, ro, rd);
+        default:                    return intersect_leaf(isect, node, plan, itra, t_min, ro, rd);
+    }
+}
+
 #define PACK4(a, b, c, d) ((((a) & 0xffu) << 0) | (((b) & 0xffu) << 8) | (((c) & 0xffu) << 16) | (((d) & 0xffu) << 24))
 #define UNPACK4_2(p) (((p) >> 16) & 0xffu)
 #define UNPACK4_3(p) (((p) >> 24) & 0xffu)
@@ -481,7 +606,7 @@ static int intersect_tree(v4* isect, const gbo_csgnode* node, const float* plan,
             int node_or_leaf = typecode >= GBO_CSG_NODE;
             if (node_or_leaf) {
                 v4 nd_isect = V4(0.f, 0.f, 0.f, 0.f);
-                intersect_leaf(&nd_isect, nd, plan, itra, tmin, ro, rd);   /* lists are not supported */
+                intersect_node(&nd_isect, nd, node, plan, itra, tmin, ro, rd);
                 nd_isect.w = copysignf(nd_isect.w, nodeIdx % 2 == 0 ? -1.f : 1.f);
                 CSG_PUSH(nd_isect, nodeIdx);
                 if (ierr) break;
@@ -546,14 +671,14 @@ static int intersect_tree(v4* isect, const gbo_csgnode* node, const float* plan,
 #undef CSG_POP0
 }
 
-/* intersect_prim : csg_intersect_tree.h:683-719 (lists are not restated) */
+/* intersect_prim : csg_intersect_tree.h:683-719 (a list prim's header node is its own root) */
 int orc_intersect_prim(v4* isect, const gbo_csgnode* node, const float* plan, const gbo_qat4* itra,
                        float t_min, v3 o, v3 d)
 {
     unsigned typecode = nd_typecode(node);
     if (typecode >= GBO_CSG_LEAF) return intersect_leaf(isect, node, plan, itra, t_min, o, d);
     if (typecode < GBO_CSG_NODE) return intersect_tree(isect, node, plan, itra, t_min, o, d);
-    return 0;
+    return intersect_node(isect, node, node, plan, itra, t_min, o, d);
 }
 
 int orc_intersect_prim_c(const gbo_csgnode* node, const float* plan, const gbo_qat4* itra, float t_min,
@@ -595,7 +720,9 @@ void orc_trace(const orc_geom* g, v3 pos, v3 dir, float tmin, float tmax, gbo_pr
             const gbo_csgnode* root = g->node + pr->q0.i[1];
             v4 is = V4(0.f, 0.f, 0.f, 0.f);
             int valid = orc_intersect_prim(&is, root, g->plan, g->itra, tmin, oo, od);
-            if (valid && is.w < best_t) {   /* strict: ties keep the lower (instance, prim) */
+            /* OptiX accepts a reported hit only inside the ray's [tmin, tmax] interval (a convex polyhedron can
+               report a valid t of 0 for a ray leaving it); strict: ties keep the lower (instance, prim) */
+            if (valid && is.w >= tmin && is.w < best_t) {
                 best_t = is.w; best_inst = ii; best_prim = pi; best_isect = is;
                 best_lpos = vadd(oo, vscale(is.w, od));
             }

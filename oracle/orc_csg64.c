@@ -341,7 +341,7 @@ static double trace64(const orc_geom* g, const inst64* I, d3 P, d3 Dv, double tm
             const gbo_csgprim* pr = &g->prim[so->primOffset + k];
             const gbo_csgnode* root = g->node + pr->q0.i[1];
             d4 is;
-            if (prim64(&is, root, g->itra, tmin, o, d) && is.w < best) {
+            if (prim64(&is, root, g->itra, tmin, o, d) && is.w >= tmin && is.w < best) {
                 best = is.w;
                 found = 1;
                 if (boundary) *boundary = root->q1.u[2];

@@ -84,7 +84,8 @@ static __device__ void ref_trace(const ref_dev_params& P, float3 pos, float3 dir
             const CSGNode* root = node + pr.nodeOffset();
             float4 isect = make_float4(0.f, 0.f, 0.f, 0.f);
             bool valid = intersect_prim(isect, root, (const float4*)P.plan, (const qat4*)P.itra, tmin, oo, od, false);
-            if (valid && isect.w < best_t) {
+            // optixReportIntersection accepts a hit only inside the ray's [tmin, tmax] interval
+            if (valid && isect.w >= tmin && isect.w < best_t) {
                 best_t = isect.w; best_inst = ii; best_prim = pi; best = isect;
                 best_lpos = oo + isect.w * od;
             }

@@ -120,7 +120,8 @@ static void ref_trace(const orc_geom* g, float3 pos, float3 dir, float tmin, flo
             const CSGNode* root = (const CSGNode*)(g->node + pr.q0.i[1]);
             float4 isect = make_float4(0.f, 0.f, 0.f, 0.f);
             bool valid = intersect_prim(isect, root, (const float4*)g->plan, (const qat4*)g->itra, tmin, oo, od, false);
-            if (valid && isect.w < best_t) {
+            // optixReportIntersection accepts a hit only inside the ray's [tmin, tmax] interval
+            if (valid && isect.w >= tmin && isect.w < best_t) {
                 best_t = isect.w; best_inst = ii; best_prim = pi; best = isect;
                 best_lpos = oo + isect.w * od;
             }

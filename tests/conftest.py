@@ -38,10 +38,25 @@ def golden_arrays(z):
 
 
 SIM_FIXTURES = ["nested_boxes", "nested_boxes_sensor", "crystal_array", "water_cube", "torch", "large_sphere_small",
-                "gdml_raindrop", "gdml_sipm8x8", "gdml_sphere_leak", "gdml_basic_detector"]
+                "gdml_raindrop", "gdml_sipm8x8", "gdml_sphere_leak", "gdml_basic_detector", "csg_lists"]
 
+
+# every shape of csg.npz: leaves, boolean trees, the convex polyhedron and the three list node kinds
+CSG_SHAPES = ["sphere", "zsphere", "cylinder", "cone", "box3", "hyperboloid", "halfspace", "phicut", "ellipsoid",
+              "difference", "intersection", "union3", "convexpolyhedron", "contiguous", "discontiguous", "overlap",
+              "difference_list"]
 
 INT_WORDS = [7, 12, 13, 14, 15]            # hitcount_iindex, orient_boundary_flag, identity, index, flagmask
+
+
+def strict_fractions(a, b):
+    """Fractions of photons whose positions agree within 1e-3 mm and times within 1e-3 ns (or one ulp of the value
+    where that is larger)."""
+    if len(a) == 0:
+        return 1.0, 1.0
+    pos_ok = np.all(np.abs(a["pos"] - b["pos"]) <= np.maximum(1e-3, np.spacing(np.abs(b["pos"]))), axis=1)
+    t_ok = np.abs(a["time"] - b["time"]) <= np.maximum(1e-3, np.spacing(np.abs(b["time"])))
+    return float(pos_ok.mean()), float(t_ok.mean())
 
 
 def assert_photons_agree(a, b, pos_mm=1e-2, time_ns=1e-3, unit=1e-4):

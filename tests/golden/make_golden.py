@@ -2,7 +2,7 @@
 
 Run from the repository root in a checkout where the reference tree is available:
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    GBO_REFERENCE_DIR=<reference checkout> make -C oracle ref && python tests/golden/make_golden.py [philox csg sims]
 
 The fixtures are outputs of oracle/_ref/libref.so, which compiles the reference's qsim.h / csg_intersect_*.h
 headers unmodified and calls curand's own host Philox.  Each fixture stores its inputs (geometry arrays,
@@ -38,8 +38,25 @@ def philox():
     save("philox.npz", cases=cases, uniforms=out)
 
 
+def trd_planes(hx1, hy1, hx2, hy2, hz):
+    """Outward face planes (nx, ny, nz, d) and box of a trd: half lengths (hx1, hy1) at z = -hz, (hx2, hy2) at +hz."""
+    v = np.array([(sx * hx, sy * hy, z) for z, hx, hy in ((-hz, hx1, hy1), (hz, hx2, hy2))
+                  for sx in (-1, 1) for sy in (-1, 1)], dtype=np.float64)
+    faces = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    centre = v.mean(axis=0)
+    planes = []
+    for f in faces:
+        n = np.cross(v[f[1]] - v[f[0]], v[f[2]] - v[f[0]])
+        n /= np.linalg.norm(n)
+        if np.dot(n, v[f[0]] - centre) < 0:
+            n = -n
+        planes.append((*n, float(np.dot(n, v[f[0]]))))
+    return planes, (*v.min(axis=0), *v.max(axis=0))
+
+
 def csg_shapes():
     """The CSG shapes of csg.npz, each a prim to intersect in its own frame."""
+    trd, trd_box = trd_planes(60.0, 50.0, 30.0, 20.0, 80.0)
     return {
         "sphere": G.sphere(100), "zsphere": G.zsphere(100, -30, 60), "cylinder": G.cylinder(50, -80, 80),
         "cone": G.cone(80, -50, 20, 70), "box3": G.box3(50, 80, 120),
@@ -52,6 +69,19 @@ def csg_shapes():
         "union3": G.operation(L.CSG_UNION, G.operation(L.CSG_UNION, G.with_transform(G.sphere(254), G.scale(1, 1, 184 / 254)),
                                                        G.with_transform(G.cylinder(127, -100, 100), G.translate(0, 0, -184))),
                               G.with_transform(G.cylinder(50, -30, 30), G.translate(0, 0, -313))),
+        # added after the shapes above so that their rays stay the same
+        "convexpolyhedron": G.convexpolyhedron(trd, trd_box),
+        "contiguous": G.csg_list(L.CSG_CONTIGUOUS, [
+            G.box3(150, 150, 150), G.cylinder(60, -160, 160),
+            G.with_transform(G.box3(100, 100, 100), G.translate(90, 90, 40))]),
+        "discontiguous": G.csg_list(L.CSG_DISCONTIGUOUS, [
+            G.with_transform(G.sphere(70), G.translate(-120, 0, 0)),
+            G.with_transform(G.box3(100, 100, 100), G.translate(120, 0, 0)),
+            G.with_transform(G.cylinder(50, -50, 50), G.translate(0, 130, 0))]),
+        "overlap": G.csg_list(L.CSG_OVERLAP, [G.sphere(120), G.box3(180, 180, 180), G.cylinder(100, -200, 200)]),
+        "difference_list": G.operation(L.CSG_DIFFERENCE, G.box3(240, 240, 240), G.csg_list(L.CSG_DISCONTIGUOUS, [
+            G.with_transform(G.cylinder(30, -130, 130), G.translate(-60, 0, 0)),
+            G.with_transform(G.cylinder(30, -130, 130), G.translate(60, 0, 0))])),
     }
 
 
@@ -71,12 +101,14 @@ def csg():
         res = np.zeros((n, 4), dtype=np.float32)
         valid = np.zeros(n, dtype=np.int8)
         itra = a["itra"] if len(a["itra"]) else np.zeros((1, 4, 4), np.float32)
+        plan = a["plan"] if len(a["plan"]) else np.zeros((1, 4), np.float32)
         for i in range(n):
-            v, r = O.intersect_prim(a["node"], np.zeros((1, 4), np.float32), itra, 0.05, o[i], d[i], use_ref=True)
+            v, r = O.intersect_prim(a["node"], plan, itra, 0.05, o[i], d[i], use_ref=True)
             valid[i] = v
             res[i] = r
         out[name + "_node"] = a["node"]
         out[name + "_itra"] = itra
+        out[name + "_plan"] = plan
         out[name + "_o"] = o
         out[name + "_d"] = d
         out[name + "_isect"] = res
@@ -99,6 +131,30 @@ def sim_case(name, geom, gs, photons=None, event_index=0):
     save("sim_%s.npz" % name, **kw)
 
 
+def lists_geometry():
+    """A geometry of the list and polyhedron shapes of csg_shapes(), each a glass instance in a vacuum box: the
+    multi-union carries a sensor surface, the trd a polished surface, the others plain glass."""
+    shapes = csg_shapes()
+    g = G.Geometry("csg_lists")
+    vac = G.Material("Vacuum", rindex=1.0)
+    glass = G.Material("Glass", rindex=1.5, abslength=2e3)
+    b_world = g.boundary(vac, None, None, vac)
+    b_sensor = g.boundary(vac, G.Surface.sensor("ListSensor", 0.5), None, glass)
+    b_mirror = g.boundary(vac, G.Surface.polished("TrdMirror", 0.9), None, glass)
+    b_glass = g.boundary(vac, None, None, glass)
+    s_world = g.add_solid("world", [(G.box3(1400, 1400, 1400), b_world)])
+    placed = [("contiguous", b_sensor, (-320, 0, 0)), ("convexpolyhedron", b_mirror, (320, 0, 0)),
+              ("overlap", b_glass, (0, 320, 0)), ("difference_list", b_glass, (0, -320, 0)),
+              ("discontiguous", b_glass, (0, 0, 320))]
+    g.add_instance(s_world)
+    for k, (name, bnd, at) in enumerate(placed):
+        s = g.add_solid(name[:15], [(shapes[name], bnd)])
+        g.add_instance(s, G.translate(*at), sensor_identifier=k if name == "contiguous" else -1,
+                       sensor_index=k if name == "contiguous" else -1)
+    g.icdf = G.default_icdf()
+    return g
+
+
 def sims():
     ph = GS.isotropic_photons(3000)
     sim_case("nested_boxes", G.nested_boxes(), GS.input_photon_genstep(len(ph)), ph)
@@ -114,7 +170,19 @@ def sims():
     sim_case("large_sphere_small", ls, GS.sphere_scint_gensteps(10, 100, seed=11, radius=1700.0))
 
 
+def sims_lists():
+    gsl = np.concatenate([GS.torch_gensteps(1, 1000, torch_type=t, pos=(0, 0, 0), radius=10.0)
+                          for t in (L.T_SPHERE, L.T_SPHERE_MARSAGLIA)])
+    sim_case("csg_lists", lists_geometry(), gsl, event_index=1)
+
+
 if __name__ == "__main__":
-    philox()
-    csg()
-    sims()
+    what = sys.argv[1:] or ["philox", "csg", "sims"]
+    if "philox" in what:
+        philox()
+    if "csg" in what:
+        csg()
+    if "sims" in what:
+        sims()
+    if "sims" in what or "lists" in what:
+        sims_lists()

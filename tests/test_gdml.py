@@ -186,3 +186,36 @@ def test_csgfoundry_round_trip(oracle, tmp_path):
     a, _ = oracle.simulate(oracle.SimConfig(arrays), gs)
     b, _ = oracle.simulate(oracle.SimConfig(back), gs)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_csgfoundry_loader_reads_reference_np_folder(oracle):
+    """A folder written by the reference's own NP writer (sysrap/NP.hh, CSGFoundry::save_ layout with the
+    SSim/stree/standard tables and their metadata; tests/golden/make_csgfoundry_golden.py) loads to exactly the
+    arrays it was written from, and simulates the same photons."""
+    from conftest import GOLDEN
+    from eic_opticks_gb300 import csgfoundry
+    z = load_golden("sim_csg_lists.npz")
+    a = csgfoundry.load(os.path.join(GOLDEN, "csgfoundry_np", "csg_lists"))
+    for k in ("node", "prim", "inst", "itra", "plan", "bnd", "optical", "icdf"):
+        assert np.array_equal(np.asarray(a[k]).view(np.uint8), np.asarray(z[k]).view(np.uint8)), k
+    assert np.array_equal(a["solid"].view(np.uint8), z["solid"].view(np.uint8))
+    assert a["hd_factor"] == int(z["hd_factor"]) and tuple(a["domain"]) == tuple(float(x) for x in z["domain"])
+    out, _ = oracle.simulate(oracle.SimConfig(a), z["gs"], event_index=int(z["event_index"]))
+    assert np.array_equal(out.view(np.uint32), z["photon"].view(np.uint32))
+
+
+@pytest.mark.skipif(not os.environ.get("GBO_REFERENCE_DIR"), reason="reference tree not available (GBO_REFERENCE_DIR)")
+def test_reference_np_folder_fixture_is_current(tmp_path):
+    """The committed folder is what the reference's NP writer writes today, file for file."""
+    import importlib.util
+    from conftest import GOLDEN
+    spec = importlib.util.spec_from_file_location("mcg", os.path.join(GOLDEN, "make_csgfoundry_golden.py"))
+    mcg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mcg)
+    fresh = mcg.main(str(tmp_path), os.environ["GBO_REFERENCE_DIR"])
+    committed = os.path.join(GOLDEN, "csgfoundry_np", "csg_lists")
+    for base, _, files in os.walk(committed):
+        for f in files:
+            rel = os.path.relpath(os.path.join(base, f), committed)
+            with open(os.path.join(committed, rel), "rb") as x, open(os.path.join(fresh, rel), "rb") as y:
+                assert x.read() == y.read(), rel

@@ -1,0 +1,64 @@
+"""gbo_autotune: the project's tuner of the kernel form (kernel mode, refill threshold, compaction period, resident
+blocks per SM).  It keeps the fastest candidate it measured, and no candidate changes any photon's history, flags,
+index or hit decision (a kernel form decides only which lane runs a photon, and when)."""
+import numpy as np
+import pytest
+
+from conftest import assert_photons_agree, golden_arrays, load_golden, strict_fractions
+
+
+def assert_forms_agree(a, b, fixture):
+    """Two kernel forms' photons: integer words identical; float words within the kernel-form bounds, or, on a
+    geometry whose mirrored paths amplify last-bit differences (ptxas fuses mul+add per kernel), positions and times
+    within 1e-3 mm / 1e-3 ns for at least as many photons as the reference's own source built with and without
+    contraction agree on (recorded in the reference-device fixture)."""
+    try:
+        assert_photons_agree(a, b)
+    except AssertionError:
+        d = load_golden("dev_" + fixture[len("sim_"):])
+        pos, t = strict_fractions(a, b)
+        assert pos >= min(0.999, float(d["self_pos"])) and t >= min(0.999, float(d["self_time"])), (pos, t)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def E():
+    import __graft_entry__ as ge
+    ge.build()
+    from eic_opticks_gb300 import engine
+    return engine
+
+
+@pytest.mark.parametrize("fixture", ["sim_crystal_array.npz", "sim_large_sphere_small.npz"])
+def test_autotune_keeps_fastest_and_results_unchanged(E, fixture):
+    z = load_golden(fixture)
+    arrays = golden_arrays(z)
+    eng = E.Engine(arrays)
+    r = eng.autotune(0, z["gs"], trials=2)
+    cands = r["candidates"]
+    ms = np.array([c["ms"] for c in cands])
+    best = cands[int(np.argmin(ms))]
+    print("%s: %d candidates, fastest %.3f ms (mode %d refill %d period %d blocks %d), slowest %.3f ms"
+          % (fixture, len(cands), ms.min(), best["mode"], best["refill"], best["period"], best["blocks_per_sm"],
+             ms.max()))
+    assert (r["kernel_mode"], r["refill_min"], r["refill_period"], r["blocks_per_sm"]) == \
+        (best["mode"], best["refill"], best["period"], best["blocks_per_sm"])
+    assert any(c["blocks_per_sm"] > 0 for c in cands)          # block shapes are among the candidates
+    assert len({(c["mode"], c["refill"], c["period"], c["blocks_per_sm"]) for c in cands}) == len(cands)
+    eng.close()
+    # every candidate form gives the same photons (histories, flags, indices, hits exactly; floats within a few ulp
+    # between separately compiled kernels)
+    ref = None
+    for c in cands:
+        eng = E.Engine(arrays, record_photon=1, record_seq=1, kernel_mode=c["mode"], refill_min=c["refill"],
+                       refill_period=c["period"], blocks_per_sm=c["blocks_per_sm"])
+        eng.simulate(int(z["event_index"]), z["gs"])
+        got = (eng.photons(), eng.seq(), eng.hits())
+        eng.close()
+        if ref is None:
+            ref = got
+            continue
+        assert np.array_equal(got[1].view(np.uint64), ref[1].view(np.uint64))
+        assert np.array_equal(got[2]["index"], ref[2]["index"])
+        assert_forms_agree(got[0], ref[0], fixture)

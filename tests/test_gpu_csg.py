@@ -1,14 +1,15 @@
-"""Every CSG shape of the reference-build fixture (tests/golden/csg.npz: 12 shapes x 2000 rays, intersect_prim of the
+"""Every CSG shape of the reference-build fixture (tests/golden/csg.npz: 17 shapes x 2000 rays, intersect_prim of the
 reference's csg_intersect_*.h compiled for the host) traced by the engine: a one-prim geometry per shape, the same
-rays, the engine's closest-hit distance against the reference's.  Covers every leaf type on the GPU, the boolean
-tree algorithm and the union fast path."""
+rays, the engine's closest-hit distance against the reference's.  Covers every leaf type on the GPU (the convex
+polyhedron included), the boolean tree algorithm, the union fast path, the three CSG list node kinds and a list
+inside a boolean tree."""
 import os
 import sys
 
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import CSG_SHAPES, load_golden
 
 pytestmark = pytest.mark.gpu
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
@@ -22,8 +23,7 @@ def E():
     return engine
 
 
-@pytest.mark.parametrize("name", ["sphere", "zsphere", "cylinder", "cone", "box3", "hyperboloid", "halfspace",
-                                  "phicut", "ellipsoid", "difference", "intersection", "union3"])
+@pytest.mark.parametrize("name", CSG_SHAPES)
 def test_engine_trace_matches_reference_intersect(E, name):
     import make_golden as MG
     from eic_opticks_gb300 import geometry as G

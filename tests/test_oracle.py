@@ -10,7 +10,7 @@ The bar is bit-exact: the oracle is a binary32 restatement in the reference's op
 import numpy as np
 import pytest
 
-from conftest import SIM_FIXTURES, golden_arrays, load_golden
+from conftest import CSG_SHAPES, SIM_FIXTURES, golden_arrays, load_golden
 
 
 def test_philox_matches_curand_golden(oracle):
@@ -26,13 +26,11 @@ def test_philox_uniform_range(oracle):
     assert abs(u.mean() - 0.5) < 0.005
 
 
-@pytest.mark.parametrize("name", ["sphere", "zsphere", "cylinder", "cone", "box3", "hyperboloid", "halfspace",
-                                  "phicut", "ellipsoid", "difference", "intersection", "union3"])
+@pytest.mark.parametrize("name", CSG_SHAPES)
 def test_csg_intersect_golden(oracle, name):
     z = load_golden("csg.npz")
-    node, itra = z[name + "_node"], z[name + "_itra"]
+    node, itra, plan = z[name + "_node"], z[name + "_itra"], z[name + "_plan"]
     o, d, want, valid = z[name + "_o"], z[name + "_d"], z[name + "_isect"], z[name + "_valid"]
-    plan = np.zeros((1, 4), np.float32)
     for i in range(len(o)):
         v, got = oracle.intersect_prim(node, plan, itra, 0.05, o[i], d[i])
         assert v == bool(valid[i]), (name, i)
