@@ -285,7 +285,8 @@ def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
                   GS.water_cerenkov_gensteps(G.water_cube(), 2000, seed=99))
         r = eng.autotune(0, sample, trials=2)
         tuned[kind] = {"mode": KERNEL_MODES[r["kernel_mode"]], "refill_min": r["refill_min"],
-                       "refill_period": r["refill_period"], "blocks_per_sm": r["blocks_per_sm"]}
+                       "refill_period": r["refill_period"], "blocks_per_sm": r["blocks_per_sm"],
+                       "walk_min": r["walk_min"]}
     photons = {id(ev[2]): int(ev[2].view(np.uint32)[:, 0, 3].astype(np.int64).sum()) for ev in events}
     total_photons = sum(photons.values())
     for kind, eid, gs in events[:4]:                          # warm-up
@@ -389,7 +390,8 @@ def same_config_batching(geom, kind, n_events, tune, submitters=16):
     events = [workload(seed=100 + k, kind=kind)[1:] for k in range(n_events)]
     photons = sum(int(g.view(np.uint32)[:, 0, 3].astype(np.int64).sum()) for g, _ in events)
     eng = E.Engine(geom, kernel_mode=tune["kernel_mode"], refill_min=tune["refill_min"],
-                   refill_period=tune["refill_period"], blocks_per_sm=tune.get("blocks_per_sm", 0))
+                   refill_period=tune["refill_period"], blocks_per_sm=tune.get("blocks_per_sm", 0),
+                   walk_min=tune.get("walk_min", 1))
     eng.simulate(0, *events[0])
     t0 = time.perf_counter()
     for k, (g, inp) in enumerate(events):
@@ -441,10 +443,11 @@ def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=N
     n_photon = int(gs.view(np.uint32)[:, 0, 3].astype(np.int64).sum())
     n_inp = 0 if inp is None else len(inp)
     if form:
-        mode, refill, period = form
+        mode, refill, period, blocks, walk = (tuple(form) + (0, 1))[:5]
         eng = E.Engine(geom, device=local, precision=precision, kernel_mode=mode, refill_min=refill,
-                       refill_period=period)
-        tune = {"kernel_mode": mode, "refill_min": refill, "refill_period": period, "blocks_per_sm": 0}
+                       refill_period=period, blocks_per_sm=blocks, walk_min=walk)
+        tune = {"kernel_mode": mode, "refill_min": refill, "refill_period": period, "blocks_per_sm": blocks,
+                "walk_min": walk}
     else:
         # kernel form picked by the autotuner on a 10% sample of the workload (setup, outside the timed region)
         eng = E.Engine(geom, device=local, precision=precision)
@@ -523,6 +526,7 @@ def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=N
                    "photons_per_step": n_photon, "gensteps_per_step": len(gs), "hits_per_step": hits,
                    "kernel": {"mode": KERNEL_MODES[tune["kernel_mode"]], "refill_min": tune["refill_min"],
                               "refill_period": tune["refill_period"], "blocks_per_sm": tune.get("blocks_per_sm", 0),
+                              "walk_min": tune.get("walk_min", 1),
                               "chosen_by": "--form" if form else "autotuner on 10% sample"},
                    "max_bounce": 31},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -623,8 +627,8 @@ def main():
                     help="gensteps per event (default: the workload's own, 2000 for the crystal array)")
     ap.add_argument("--workload", default="crystal_array", choices=sorted(WORKLOADS))
     ap.add_argument("--form", default=None,
-                    help="kernel form MODE,REFILL,PERIOD instead of the autotuner's choice (MODE 0: photon pool, "
-                         "1: one thread per photon, 2: photon pool over pregenerated photons)")
+                    help="kernel form MODE,REFILL,PERIOD[,BLOCKS_PER_SM[,WALK_MIN]] instead of the autotuner's choice "
+                         "(MODE 0: photon pool, 1: one thread per photon, 2: photon pool over pregenerated photons)")
     ap.add_argument("--batch-events", type=int, default=None,
                     help="events of the workload for the same-configuration plain vs batched comparison")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1],

@@ -1341,16 +1341,18 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
     if (!e || !out) return fail(GBO_ERR_ARG, "gbo_autotune: null argument");
     if (trials < 1) trials = 1;
     std::memset(out, 0, sizeof(*out));
-    // candidates: (kernel mode, refill threshold, refill period, resident blocks per SM; 0 = the occupancy maximum)
-    struct Cand { int mode, refill, period, blocks; };
-    std::vector<Cand> cands = {{1, 32, 1, 0}};
+    // candidates: (kernel mode, refill threshold, refill period, resident blocks per SM (0: the occupancy maximum),
+    // lanes gathered per TLAS walk (1: none))
+    struct Cand { int mode, refill, period, blocks, walk; };
+    std::vector<Cand> cands = {{1, 32, 1, 0, 1}};
     for (int r : {1, 2, 4, 8, 16, 32})
-        for (int p : {1, 4}) cands.push_back({0, r, p, 0});
-    for (int r : {1, 2, 4, 8, 16}) cands.push_back({2, r, 1, 0});
+        for (int p : {1, 4}) cands.push_back({0, r, p, 0, 1});
+    for (int r : {1, 2, 4, 8, 16}) cands.push_back({2, r, 1, 0, 1});
+    for (int w : {16, 24, 32}) cands.push_back({2, 4, 1, 0, w});
     const int form = 2 * e->csg_form + (e->cfg.precision ? 1 : 0);
     for (int b = 1; b < e->pool_occ[form] && cands.size() < 32; b++) {       // fewer resident blocks than fit
-        cands.push_back({2, 4, 1, b});
-        if (cands.size() < 32) cands.push_back({0, 4, 1, b});
+        cands.push_back({2, 4, 1, b, 1});
+        if (cands.size() < 32) cands.push_back({0, 4, 1, b, 1});
     }
     const gbo_config saved = e->cfg;
     float best = 1e30f;
@@ -1360,6 +1362,7 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         e->cfg.refill_min = cands[c].refill;
         e->cfg.refill_period = cands[c].period;
         e->cfg.blocks_per_sm = cands[c].blocks;
+        e->cfg.walk_min = cands[c].walk;
         float ms = 1e30f;
         for (int t = 0; t <= trials; t++) {
             int rc = gbo_simulate(e, event_id, gs, num_gs, input_photon, num_input_photon);
@@ -1370,6 +1373,7 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         out->cand_refill[c] = cands[c].refill;
         out->cand_period[c] = cands[c].period;
         out->cand_blocks[c] = cands[c].blocks;
+        out->cand_walk[c] = cands[c].walk;
         out->cand_ms[c] = ms;
         out->num_candidates = (int32_t)(c + 1);
         if (ms < best) { best = ms; pick = cands[c]; }
@@ -1379,10 +1383,12 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
     e->cfg.refill_min = pick.refill;
     e->cfg.refill_period = pick.period;
     e->cfg.blocks_per_sm = pick.blocks;
+    e->cfg.walk_min = pick.walk;
     out->kernel_mode = pick.mode;
     out->refill_min = pick.refill;
     out->refill_period = pick.period;
     out->blocks_per_sm = pick.blocks;
+    out->walk_min = pick.walk;
     return GBO_OK;
 }
 

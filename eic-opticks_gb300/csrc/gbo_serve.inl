@@ -396,6 +396,9 @@ void serve_loop(gbo_server* sv)
                 }
                 if (!rc && cudaEventRecord(sl.ev_done, sl.stream) != cudaSuccess) rc = fail(GBO_ERR_CUDA, "event record failed");
                 if (rc) { finish_slot(sv, sl, rc); continue; }
+                // the batch's kernels are done: a waiting big event may start in another slot while these hits
+                // download, so the GPU does not idle through the copy
+                if (sl.big) { big_counter(sv->e->device)--; sl.big = false; }
                 sl.phase = 2;
             } else if (sl.phase == 2) {
                 busy = true;
@@ -407,8 +410,8 @@ void serve_loop(gbo_server* sv)
         // admit waiting events into idle slots: at once when the GPU has nothing in flight, otherwise only once
         // enough photons wait to fill the GPU (min_batch_photon), so that batches do not degenerate to single events.
         // A big event (at least target_batch_photon photons, enough to fill the GPU alone) never starts beside
-        // another big one, where the two would share the SMs and each take twice as long; small events may pass a
-        // waiting big one into the free slot.
+        // another big one's kernels, where the two would share the SMs and each take twice as long (it may start
+        // while the other's hits download); small events may pass a waiting big one into the free slot.
         for (Slot& sl : sv->slots) {
             if (sl.phase != 0) continue;
             int in_flight = 0;

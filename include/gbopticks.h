@@ -93,13 +93,16 @@ typedef struct gbo_config {
 } gbo_config;
 
 /* Result of gbo_autotune: the kernel form chosen (kernel mode, refill threshold, refill period = compaction period,
- * resident blocks per SM = block shape, 0 meaning the occupancy maximum) and the simulate time of every candidate. */
+ * resident blocks per SM = block shape with 0 the occupancy maximum, lanes gathered per TLAS walk = walk queue) and
+ * the simulate time of every candidate. */
 typedef struct gbo_tune_result {
     int32_t kernel_mode, refill_min, refill_period, num_candidates;
     int32_t cand_mode[32], cand_refill[32], cand_period[32];
     float   cand_ms[32];
     int32_t blocks_per_sm;
     int32_t cand_blocks[32];
+    int32_t walk_min;
+    int32_t cand_walk[32];
 } gbo_tune_result;
 
 typedef struct gbo_stats {
@@ -149,9 +152,10 @@ const char* gbo_last_error(void);
 
 /* gbo_autotune : no counterpart in the reference (its launch shape is fixed by OptiX).  Runs the given sample
  * event with every candidate kernel form (one thread per photon; photon pool with refill thresholds 1..32 and
- * refill periods 1, 4; pool over pregenerated photons with refill thresholds 1..16; both pools with fewer resident
- * blocks per SM than fit), `trials` timed runs each after one warm-up, and keeps the fastest in the engine's
- * config.  Every candidate gives the same photons (the kernel form decides only which lane runs a photon, when). */
+ * refill periods 1, 4; pool over pregenerated photons with refill thresholds 1..16 and with 16, 24 or 32 lanes
+ * gathered per TLAS walk; both pools with fewer resident blocks per SM than fit), `trials` timed runs each after
+ * one warm-up, and keeps the fastest in the engine's config.  Every candidate gives the same photons (the kernel
+ * form decides only which lane runs a photon, and when). */
 int         gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs,
                          const gbo_sphoton* input_photon, int64_t num_input_photon, int32_t trials,
                          gbo_tune_result* out);
