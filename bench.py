@@ -233,7 +233,10 @@ def reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / max(1, len(times)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample_gensteps_per_step": sample_gs},
+            "config": {"workload": WORKLOAD, "sample_gensteps_per_step": sample_gs,
+                       "sample": "per-photon rate on a bounded sample of the same event: each step simulates %d of its "
+                                 "%d gensteps (one per host thread, each with its event photon offset), so the photons "
+                                 "are exactly the event's own" % (sample_gs, len(gs))},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
                              "sample": "%d gensteps per step, one per thread (~%d photons)"
                                        % (sample_gs, photons // max(1, len(times)))},

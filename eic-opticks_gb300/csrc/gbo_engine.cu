@@ -96,12 +96,14 @@ struct Params {
     int walk_min;                           // pool kernels: parked lanes that trigger the gathered TLAS walks
 };
 
-GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng, int& hint);
+template <class R>
+GBO_GEN void generate(const Params& P, long long idx, Photon& p, R& rng, int& hint);
 
 // Kernel forms: TREE 1 when any prim is a CSG tree, 2 when CSG list nodes occur as well (their evaluation is
 // compiled only into that form); PRECISE for the precision mode (binary64 root polish in the quadric leaves,
-// binary64 position / time accumulators).  The default form compiles none of the latter.
-template <int TREE, bool PRECISE>
+// binary64 position / time accumulators).  The default form compiles none of the latter.  RCALL: Philox blocks by
+// an out-of-line call instead of inlined rounds (RngT).
+template <int TREE, bool PRECISE, bool RCALL>
 __global__ void __launch_bounds__(SIM_BLOCK, (TREE || PRECISE) ? GBO_SIM_MINB_WIDE : GBO_SIM_MINB)
 k_simulate(const __grid_constant__ Params P)
 {
@@ -110,7 +112,7 @@ k_simulate(const __grid_constant__ Params P)
     Photon p;
     bool is_hit = false;
     if (active) {
-        Rng rng;
+        RngT<RCALL> rng;
         Acc64 acc;
         int hint;
         generate(P, idx, p, rng, hint);
@@ -151,7 +153,8 @@ k_simulate(const __grid_constant__ Params P)
 // ---- persistent form: lanes refill from a photon pool so a warp never idles behind its longest photon --------
 
 // `hint` receives the start instance found for the photon's genstep (-1 when none was computed)
-GBO_GEN void generate(const Params& P, long long idx, Photon& p, Rng& rng, int& hint)
+template <class R>
+GBO_GEN void generate(const Params& P, long long idx, Photon& p, R& rng, int& hint)
 {
     int lo = 0, hi = P.num_gs - 1;
     while (lo < hi) {
@@ -203,7 +206,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_generate(const __grid_constant__ 
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= P.num_photon) return;
     Photon p;
-    Rng rng;
+    RngT<false> rng;
     int hint;
     generate(P, idx, p, rng, hint);
     store_photon(P.gen_photon + idx, p);
@@ -213,9 +216,9 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_generate(const __grid_constant__ 
 
 // Kernel-mode-2 refill (warp-uniform chunk state cbase, cn, cused): idle lanes take the next pregenerated photons in
 // lane order, the warp claiming POOL_CHUNK more with one atomic when its chunk runs short.
-template <bool PRECISE>
+template <bool PRECISE, class R>
 GBO_DEV void refill_pregenerated(const Params& P, unsigned long long* pool, unsigned idle, unsigned lane, unsigned lt,
-                                 bool& live, long long& idx, Photon& p, Rng& rng, int& hint, Acc64& acc, int& bounce,
+                                 bool& live, long long& idx, Photon& p, R& rng, int& hint, Acc64& acc, int& bounce,
                                  long long& cbase, int& cn, int& cused, bool& pool_open)
 {
     const int n_idle = __popc(idle), rank = __popc(idle & lt), avail = cn - cused;
@@ -255,7 +258,7 @@ GBO_DEV void refill_pregenerated(const Params& P, unsigned long long* pool, unsi
 // PREGEN: the kernel-mode-2 form without the generator.  Without a call to the out-of-line generator, its
 // by-reference arguments no longer force the photon state through local memory (crystal event 751M -> 864M
 // photons/s).
-template <int TREE, bool PRECISE, bool PREGEN>
+template <int TREE, bool PRECISE, bool PREGEN, bool RCALL>
 __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P,
                                                              unsigned long long* pool, int refill_min, int period)
 {
@@ -268,7 +271,7 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
     int hint = -1;
     int it = 0;
     Photon p;
-    Rng rng;
+    RngT<RCALL> rng;
     Acc64 acc;
     // mode 2 (warp-uniform): the warp's claimed chunk of pregenerated photons [cbase, cbase + cn), cused taken
     long long cbase = 0;
@@ -540,7 +543,7 @@ __global__ void k_rng_sequence(uint64_t seed, uint64_t subsequence0, uint64_t po
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= num_seq) return;
-    Rng r;
+    RngT<false> r;
     rng_init(r, seed, subsequence0 + (uint64_t)i, position);
     for (int k = 0; k < per_seq; k++) out[(size_t)i * per_seq + k] = uniform(r);
 }
@@ -683,8 +686,8 @@ struct gbo_engine {
     float nm0 = 60.f, nms = 1.f;
     int csg_form = 0;                       // 0: single-leaf prims, 1: boolean trees, 2: CSG list nodes too
     int sms = 0;                            // streaming multiprocessors of the device
-    int pool_occ[6] = {0, 0, 0, 0, 0, 0};   // most resident blocks of k_simulate_pool per SM, per kernel form
-                                            // (index 2 x csg_form + precision)
+    int pool_occ[7] = {0, 0, 0, 0, 0, 0, 0};    // most resident blocks of k_simulate_pool per SM, per kernel form
+                                                // (kernel_form())
     // event
     DBuf<gbo_quad6> gs;
     DBuf<unsigned long long> gs_end;
@@ -713,7 +716,17 @@ struct gbo_engine {
     gbo_stats stats{};
 };
 
-template <int TREE, bool PRECISE>
+// Kernel form index: 2 x csg_form + precision, 6 for the single-leaf binary32 kernels with Philox blocks by call.
+// The CSG-tree forms always call (their code is large enough to miss in the instruction cache otherwise); the
+// single-leaf forms inline the rounds unless gbo_config.rng_call asks for the call (binary32 only).
+static int kernel_form(const gbo_engine* e)
+{
+    const bool precise = e->cfg.precision != 0;
+    if (e->csg_form == 0 && !precise && e->cfg.rng_call == 1) return 6;
+    return 2 * e->csg_form + (precise ? 1 : 0);
+}
+
+template <int TREE, bool PRECISE, bool RCALL>
 static void launch_form(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s,
                         cudaEvent_t after_gen)
 {
@@ -722,7 +735,7 @@ static void launch_form(const gbo_engine* e, const Params& P, long long n, unsig
             k_generate<<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
             if (after_gen) cudaEventRecord(after_gen, s);
         }
-        const int form = 2 * TREE + (PRECISE ? 1 : 0);
+        const int form = kernel_form(e);
         const long long need = (n + SIM_BLOCK - 1) / SIM_BLOCK;
         const int want = e->cfg.blocks_per_sm, occ = e->pool_occ[form] > 0 ? e->pool_occ[form] : 1;
         const long long resident = (long long)e->sms * (want > 0 && want < occ ? want : occ);
@@ -730,11 +743,11 @@ static void launch_form(const gbo_engine* e, const Params& P, long long n, unsig
         const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
         const int period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
         if (P.gen_photon)
-            k_simulate_pool<TREE, PRECISE, true><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
+            k_simulate_pool<TREE, PRECISE, true, RCALL><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
         else
-            k_simulate_pool<TREE, PRECISE, false><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
+            k_simulate_pool<TREE, PRECISE, false, RCALL><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
     } else {
-        k_simulate<TREE, PRECISE><<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
+        k_simulate<TREE, PRECISE, RCALL><<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
     }
 }
 
@@ -745,11 +758,14 @@ static void launch_form(const gbo_engine* e, const Params& P, long long n, unsig
 static void launch_simulate(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s,
                             cudaEvent_t after_gen = nullptr)
 {
-    const bool precise = e->cfg.precision != 0;
-    switch (e->csg_form) {
-        case 2:  if (precise) launch_form<2, true>(e, P, n, pool, s, after_gen); else launch_form<2, false>(e, P, n, pool, s, after_gen); break;
-        case 1:  if (precise) launch_form<1, true>(e, P, n, pool, s, after_gen); else launch_form<1, false>(e, P, n, pool, s, after_gen); break;
-        default: if (precise) launch_form<0, true>(e, P, n, pool, s, after_gen); else launch_form<0, false>(e, P, n, pool, s, after_gen); break;
+    switch (kernel_form(e)) {
+        case 0:  launch_form<0, false, false>(e, P, n, pool, s, after_gen); break;
+        case 1:  launch_form<0, true, false>(e, P, n, pool, s, after_gen); break;
+        case 2:  launch_form<1, false, true>(e, P, n, pool, s, after_gen); break;
+        case 3:  launch_form<1, true, true>(e, P, n, pool, s, after_gen); break;
+        case 4:  launch_form<2, false, true>(e, P, n, pool, s, after_gen); break;
+        case 5:  launch_form<2, true, true>(e, P, n, pool, s, after_gen); break;
+        default: launch_form<0, false, true>(e, P, n, pool, s, after_gen); break;
     }
 }
 
@@ -780,6 +796,7 @@ int gbo_config_default(gbo_config* c)
     c->blocks_per_sm = 0;
     c->refill_period = 1;
     c->walk_min = 1;
+    c->rng_call = 0;
     c->max_slot = 0;
     long long iv;
     float fv;
@@ -940,19 +957,20 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     TRY(make_texture(&e->icdf_array, &e->icdf_tex, g->icdf, g->icdf_nx, g->icdf_ny, false));
     TRY(e->counters.ensure(4));
     {
-        int sms = 0, b[6] = {0, 0, 0, 0, 0, 0};
+        int sms = 0, b[7] = {0, 0, 0, 0, 0, 0, 0};
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_simulate_pool<0, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_simulate_pool<0, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_simulate_pool<1, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_simulate_pool<1, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[4], k_simulate_pool<2, false, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[5], k_simulate_pool<2, true, true>, SIM_BLOCK, 0) != cudaSuccess) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_simulate_pool<0, false, true, false>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_simulate_pool<0, true, true, false>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_simulate_pool<1, false, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_simulate_pool<1, true, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[4], k_simulate_pool<2, false, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[5], k_simulate_pool<2, true, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[6], k_simulate_pool<0, false, true, true>, SIM_BLOCK, 0) != cudaSuccess) {
             gbo_engine_destroy(e);
             return fail(GBO_ERR_CUDA, "occupancy query failed");
         }
         e->sms = sms;
-        for (int f = 0; f < 6; f++) e->pool_occ[f] = b[f];
+        for (int f = 0; f < 7; f++) e->pool_occ[f] = b[f];
     }
     if (cudaStreamSynchronize(e->stream) != cudaSuccess) {
         gbo_engine_destroy(e);
@@ -1342,17 +1360,21 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
     if (trials < 1) trials = 1;
     std::memset(out, 0, sizeof(*out));
     // candidates: (kernel mode, refill threshold, refill period, resident blocks per SM (0: the occupancy maximum),
-    // lanes gathered per TLAS walk (1: none))
-    struct Cand { int mode, refill, period, blocks, walk; };
-    std::vector<Cand> cands = {{1, 32, 1, 0, 1}};
+    // lanes gathered per TLAS walk (1: none), Philox blocks by call in the single-leaf binary32 form)
+    struct Cand { int mode, refill, period, blocks, walk, rcall; };
+    std::vector<Cand> cands = {{1, 32, 1, 0, 1, 0}};
     for (int r : {1, 2, 4, 8, 16, 32})
-        for (int p : {1, 4}) cands.push_back({0, r, p, 0, 1});
-    for (int r : {1, 2, 4, 8, 16}) cands.push_back({2, r, 1, 0, 1});
-    for (int w : {16, 24, 32}) cands.push_back({2, 4, 1, 0, w});
+        for (int p : {1, 4}) cands.push_back({0, r, p, 0, 1, 0});
+    for (int r : {1, 2, 4, 8, 16}) cands.push_back({2, r, 1, 0, 1, 0});
+    for (int w : {16, 24, 32}) cands.push_back({2, 4, 1, 0, w, 0});
+    if (e->csg_form == 0 && !e->cfg.precision)
+        for (const Cand& c : std::vector<Cand>{{1, 32, 1, 0, 1, 1}, {0, 4, 1, 0, 1, 1}, {0, 4, 4, 0, 1, 1},
+                                               {2, 1, 1, 0, 1, 1}, {2, 4, 1, 0, 1, 1}})
+            cands.push_back(c);
     const int form = 2 * e->csg_form + (e->cfg.precision ? 1 : 0);
     for (int b = 1; b < e->pool_occ[form] && cands.size() < 32; b++) {       // fewer resident blocks than fit
-        cands.push_back({2, 4, 1, b, 1});
-        if (cands.size() < 32) cands.push_back({0, 4, 1, b, 1});
+        cands.push_back({2, 4, 1, b, 1, 0});
+        if (cands.size() < 32) cands.push_back({0, 4, 1, b, 1, 0});
     }
     const gbo_config saved = e->cfg;
     float best = 1e30f;
@@ -1363,6 +1385,7 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         e->cfg.refill_period = cands[c].period;
         e->cfg.blocks_per_sm = cands[c].blocks;
         e->cfg.walk_min = cands[c].walk;
+        e->cfg.rng_call = cands[c].rcall;
         float ms = 1e30f;
         for (int t = 0; t <= trials; t++) {
             int rc = gbo_simulate(e, event_id, gs, num_gs, input_photon, num_input_photon);
@@ -1374,6 +1397,7 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         out->cand_period[c] = cands[c].period;
         out->cand_blocks[c] = cands[c].blocks;
         out->cand_walk[c] = cands[c].walk;
+        out->cand_rng_call[c] = cands[c].rcall;
         out->cand_ms[c] = ms;
         out->num_candidates = (int32_t)(c + 1);
         if (ms < best) { best = ms; pick = cands[c]; }
@@ -1384,11 +1408,13 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
     e->cfg.refill_period = pick.period;
     e->cfg.blocks_per_sm = pick.blocks;
     e->cfg.walk_min = pick.walk;
+    e->cfg.rng_call = pick.rcall;
     out->kernel_mode = pick.mode;
     out->refill_min = pick.refill;
     out->refill_period = pick.period;
     out->blocks_per_sm = pick.blocks;
     out->walk_min = pick.walk;
+    out->rng_call = pick.rcall;
     return GBO_OK;
 }
 
@@ -1529,7 +1555,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_simulate_bounded(const __grid_con
     Photon p;
     bool is_hit = false;
     if (idx < P.num_photon) {
-        Rng rng;
+        RngT<(TREE >= 1)> rng;
         int hint;
         generate(P, idx, p, rng, hint);
         int bounce = 0;

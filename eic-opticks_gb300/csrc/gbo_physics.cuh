@@ -129,7 +129,8 @@ GBO_DEV float3 uniform_sphere(float u0, float u1)   // qsim.h:177-183
 
 // ---- generators ----------------------------------------------------------------------------------------------
 
-GBO_DEV void gen_torch(Photon& p, Rng& rng, const float4* g, uint64_t photon_id)
+template <class R>
+GBO_DEV void gen_torch(Photon& p, R& rng, const float4* g, uint64_t photon_id)
 {
     const float4 q0 = g[0], q1 = g[1], q2 = g[2], q3 = g[3], q4 = g[4], q5 = g[5];
     const float3 gpos = f3(q1.x, q1.y, q1.z);
@@ -234,7 +235,8 @@ GBO_DEV void gen_torch(Photon& p, Rng& rng, const float4* g, uint64_t photon_id)
     set_flag(p, GBO_TORCH);
 }
 
-GBO_DEV void gen_scint(const Tables& t, Photon& p, Rng& rng, const float4* g)
+template <class R>
+GBO_DEV void gen_scint(const Tables& t, Photon& p, R& rng, const float4* g)
 {
     const float u0 = uniform(rng), u1 = uniform(rng), u2 = uniform(rng), u3 = uniform(rng);
     const float cost = 1.f - 2.f * u0;
@@ -258,7 +260,8 @@ GBO_DEV void gen_scint(const Tables& t, Photon& p, Rng& rng, const float4* g)
     set_flag(p, GBO_SCINTILLATION);
 }
 
-GBO_DEV void gen_cerenkov(const Tables& t, Photon& p, Rng& rng, const float4* g)
+template <class R>
+GBO_DEV void gen_cerenkov(const Tables& t, Photon& p, R& rng, const float4* g)
 {
     const float4 q0 = g[0], q1 = g[1], q2 = g[2], q3 = g[3], q4 = g[4], q5 = g[5];
     const unsigned matline = __float_as_uint(q0.z);
@@ -315,7 +318,8 @@ GBO_DEV void gen_cerenkov(const Tables& t, Photon& p, Rng& rng, const float4* g)
 
 // ---- physics of one step -------------------------------------------------------------------------------------
 
-GBO_DEV void rayleigh_scatter(Photon& p, Rng& rng)
+template <class R>
+GBO_DEV void rayleigh_scatter(Photon& p, R& rng)
 {
     float3 direction = f3(0.f, 0.f, 0.f), polarization = f3(0.f, 0.f, 0.f);
     bool looping = true;
@@ -346,7 +350,8 @@ GBO_DEV void rayleigh_scatter(Photon& p, Rng& rng)
     p.pol = polarization;
 }
 
-GBO_DEV int propagate_to_boundary(const Tables& t, Photon& p, const State& s, float distance_to_boundary, Rng& rng,
+template <class R>
+GBO_DEV int propagate_to_boundary(const Tables& t, Photon& p, const State& s, float distance_to_boundary, R& rng,
                                   unsigned& flag, Acc64* acc = nullptr)
 {
     const float absorption_length = s.material1.y;
@@ -388,7 +393,8 @@ GBO_DEV int propagate_to_boundary(const Tables& t, Photon& p, const State& s, fl
     return CMD_BOUNDARY;
 }
 
-GBO_DEV int propagate_at_boundary(const Tables& t, Photon& p, const State& s, float3 normal, Rng& rng, unsigned& flag)
+template <class R>
+GBO_DEV int propagate_at_boundary(const Tables& t, Photon& p, const State& s, float3 normal, R& rng, unsigned& flag)
 {
     const float n1 = s.material1.x;
     const float n2 = s.material2.x;
@@ -437,7 +443,8 @@ GBO_DEV int propagate_at_boundary(const Tables& t, Photon& p, const State& s, fl
     return CMD_CONTINUE;
 }
 
-GBO_DEV float3 random_direction_marsaglia(Rng& rng)
+template <class R>
+GBO_DEV float3 random_direction_marsaglia(R& rng)
 {
     float u = 0.f, v = 0.f, b = 2.f;
     for (int k = 0; k < LOOP_CAP && b > 1.f; k++) {
@@ -450,7 +457,8 @@ GBO_DEV float3 random_direction_marsaglia(Rng& rng)
     return f3(a * u, a * v, 2.f * b - 1.f);
 }
 
-GBO_DEV int propagate_at_surface(const Tables& t, Photon& p, const State& s, float3 normal, Rng& rng, unsigned& flag)
+template <class R>
+GBO_DEV int propagate_at_surface(const Tables& t, Photon& p, const State& s, float3 normal, R& rng, unsigned& flag)
 {
     const float detect = s.surface.x;
     const float absorb = s.surface.y;
@@ -489,7 +497,8 @@ GBO_DEV int propagate_at_surface(const Tables& t, Photon& p, const State& s, flo
 }
 
 // qsim::propagate : one step given the normalized intersect
-GBO_DEV int propagate(const Tables& t, Photon& p, const Hit& h, Rng& rng, Acc64* acc = nullptr)
+template <class R>
+GBO_DEV int propagate(const Tables& t, Photon& p, const Hit& h, R& rng, Acc64* acc = nullptr)
 {
     const unsigned boundary = h.prim_boundary & 0xffffu;
     const unsigned identity = h.iindex_identity & 0xffffu;
@@ -502,9 +511,10 @@ GBO_DEV int propagate(const Tables& t, Photon& p, const Hit& h, Rng& rng, Acc64*
     int command = propagate_to_boundary(t, p, s, h.t, rng, flag, acc);
     if (command == CMD_BOUNDARY) {
         const int ems = (int)s.optical.y;
+        // qsim.h:2284-2305: a surface, or the back (lpos z < 0) of a z-plus sensor, takes propagate_at_surface (one
+        // call site, so its code is inlined once)
         if (ems == GBO_EMS_NOSURFACE) command = propagate_at_boundary(t, p, s, h.normal, rng, flag);
-        else if (ems == GBO_EMS_SURFACE) command = propagate_at_surface(t, p, s, h.normal, rng, flag);
-        else if (h.lposz < 0.f) command = propagate_at_surface(t, p, s, h.normal, rng, flag);
+        else if (ems == GBO_EMS_SURFACE || h.lposz < 0.f) command = propagate_at_surface(t, p, s, h.normal, rng, flag);
         else if (ems == GBO_EMS_ZPLUS_SENSOR_A) {
             skip(rng, 1);
             flag = GBO_SURFACE_DETECT;

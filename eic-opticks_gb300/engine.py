@@ -43,14 +43,16 @@ class Config(C.Structure):
                 ("tmax", C.c_float), ("debug_tag", C.c_int32), ("record_photon", C.c_int32),
                 ("record_seq", C.c_int32), ("max_photon", C.c_int64), ("kernel_mode", C.c_int32),
                 ("refill_min", C.c_int32), ("blocks_per_sm", C.c_int32), ("refill_period", C.c_int32),
-                ("max_slot", C.c_int64), ("precision", C.c_int32), ("walk_min", C.c_int32)]
+                ("max_slot", C.c_int64), ("precision", C.c_int32), ("walk_min", C.c_int32),
+                ("rng_call", C.c_int32), ("reserved", C.c_int32)]
 
 
 class TuneResult(C.Structure):
     _fields_ = [("kernel_mode", C.c_int32), ("refill_min", C.c_int32), ("refill_period", C.c_int32),
                 ("num_candidates", C.c_int32), ("cand_mode", C.c_int32 * 32), ("cand_refill", C.c_int32 * 32),
                 ("cand_period", C.c_int32 * 32), ("cand_ms", C.c_float * 32), ("blocks_per_sm", C.c_int32),
-                ("cand_blocks", C.c_int32 * 32), ("walk_min", C.c_int32), ("cand_walk", C.c_int32 * 32)]
+                ("cand_blocks", C.c_int32 * 32), ("walk_min", C.c_int32), ("cand_walk", C.c_int32 * 32),
+                ("rng_call", C.c_int32), ("cand_rng_call", C.c_int32 * 32)]
 
 
 class Stats(C.Structure):
@@ -242,12 +244,13 @@ class Engine:
                                      inp.ctypes.data_as(C.c_void_p) if inp is not None else None,
                                      len(inp) if inp is not None else 0, int(trials), C.byref(r)), "gbo_autotune")
         cands = [dict(mode=r.cand_mode[i], refill=r.cand_refill[i], period=r.cand_period[i],
-                      blocks_per_sm=r.cand_blocks[i], walk_min=r.cand_walk[i], ms=r.cand_ms[i])
+                      blocks_per_sm=r.cand_blocks[i], walk_min=r.cand_walk[i], rng_call=r.cand_rng_call[i],
+                      ms=r.cand_ms[i])
                  for i in range(r.num_candidates)]
         self.config.kernel_mode, self.config.refill_min, self.config.refill_period = r.kernel_mode, r.refill_min, r.refill_period
-        self.config.blocks_per_sm, self.config.walk_min = r.blocks_per_sm, r.walk_min
+        self.config.blocks_per_sm, self.config.walk_min, self.config.rng_call = r.blocks_per_sm, r.walk_min, r.rng_call
         return dict(kernel_mode=r.kernel_mode, refill_min=r.refill_min, refill_period=r.refill_period,
-                    blocks_per_sm=r.blocks_per_sm, walk_min=r.walk_min, candidates=cands)
+                    blocks_per_sm=r.blocks_per_sm, walk_min=r.walk_min, rng_call=r.rng_call, candidates=cands)
 
     def texture_lookup(self, which, xy):
         xy = np.ascontiguousarray(xy, dtype=np.float32)

@@ -90,11 +90,16 @@ typedef struct gbo_config {
     int32_t  walk_min;              /* pool kernels: a lane whose step needs a walk of the instance tree parks until
                                        this many lanes of its warp need one (or no other lane can step), so the walks
                                        run together; 1: no parking (1) */
+    int32_t  rng_call;              /* kernels of geometries without CSG trees, binary32: 0 (default) inlines the
+                                       Philox rounds at every draw site, 1 computes each block of four draws by an
+                                       out-of-line call (smaller code; the CSG-tree kernels always do).  Same numbers
+                                       either way */
+    int32_t  reserved;
 } gbo_config;
 
 /* Result of gbo_autotune: the kernel form chosen (kernel mode, refill threshold, refill period = compaction period,
- * resident blocks per SM = block shape with 0 the occupancy maximum, lanes gathered per TLAS walk = walk queue) and
- * the simulate time of every candidate. */
+ * resident blocks per SM = block shape with 0 the occupancy maximum, lanes gathered per TLAS walk = walk queue,
+ * Philox by call) and the simulate time of every candidate. */
 typedef struct gbo_tune_result {
     int32_t kernel_mode, refill_min, refill_period, num_candidates;
     int32_t cand_mode[32], cand_refill[32], cand_period[32];
@@ -103,6 +108,8 @@ typedef struct gbo_tune_result {
     int32_t cand_blocks[32];
     int32_t walk_min;
     int32_t cand_walk[32];
+    int32_t rng_call;
+    int32_t cand_rng_call[32];
 } gbo_tune_result;
 
 typedef struct gbo_stats {

@@ -20,15 +20,21 @@ _spec = importlib.util.spec_from_file_location("make_device_golden",
 mdg = importlib.util.module_from_spec(_spec)
 _spec.loader.exec_module(mdg)
 
-KERNEL_MODES = (2, 1, 0)
+# (kernel mode, Philox blocks by call): the three kernel modes, and the two main ones with Philox by call (a
+# separate kernel form for geometries without CSG trees)
+FORMS = ((2, 0), (1, 0), (0, 0), (2, 1), (1, 1))
+
+
+def form_key(mode, rng_call):
+    return "mode%d%s" % (mode, "_call" if rng_call else "")
 
 
 def run(arrays, gs, inp, ev):
     out = {}
-    for mode in KERNEL_MODES:
-        eng = E.Engine(arrays, record_photon=1, record_seq=1, kernel_mode=mode)
+    for mode, rng_call in FORMS:
+        eng = E.Engine(arrays, record_photon=1, record_seq=1, kernel_mode=mode, rng_call=rng_call)
         eng.simulate(ev, gs, inp)
-        out[mode] = mdg.record_digest(eng.photons(), eng.seq()["seqhis"])
+        out[form_key(mode, rng_call)] = mdg.record_digest(eng.photons(), eng.seq()["seqhis"])
         eng.close()
     return out
 
@@ -39,12 +45,12 @@ def main(path):
     for name in mdg.SIM_FIXTURES:
         z = np.load(os.path.join(ROOT, "tests", "golden", "sim_%s.npz" % name))
         inp = z["input_photon"] if len(z["input_photon"]) else None
-        for mode, d in run(mdg.golden_arrays(z), z["gs"], inp, int(z["event_index"])).items():
-            res["%s_mode%d" % (name, mode)] = d
+        for form, d in run(mdg.golden_arrays(z), z["gs"], inp, int(z["event_index"])).items():
+            res["%s_%s" % (name, form)] = d
     for name in mdg.CONFIGS:
         arrays, gs, inp, ev = mdg.config_inputs(name)
-        for mode, d in run(arrays, gs, inp, ev).items():
-            res["%s_mode%d" % (name, mode)] = d
+        for form, d in run(arrays, gs, inp, ev).items():
+            res["%s_%s" % (name, form)] = d
     np.savez(path, **res)
 
 

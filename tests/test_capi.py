@@ -69,3 +69,27 @@ def test_event_api_argument_errors_without_gpu(lib):
     assert lib.gbo_event_num_hits(None, ctypes.c_uint64(1)) < 0
     assert lib.gbo_event_copy_hits(None, ctypes.c_uint64(1), None, ctypes.c_size_t(0)) == 1
     assert lib.gbo_event_release(None, ctypes.c_uint64(1)) == 1
+
+
+def test_ctypes_mirrors_match_the_header(tmp_path):
+    """Every ctypes structure of the Python binding has the size and field offsets the C compiler gives the header's
+    struct (a field added on one side only would shift every later field)."""
+    import subprocess
+    from eic_opticks_gb300 import engine as E
+    pairs = [("gbo_config", E.Config), ("gbo_tune_result", E.TuneResult), ("gbo_stats", E.Stats),
+             ("gbo_geometry_desc", E.GeometryDesc)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbopticks.h"', "int main(void) {"]
+    for cname, py in pairs:
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = dict(l.split() for l in subprocess.check_output([str(exe)]).decode().split("\n") if l)
+    for cname, py in pairs:
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got["%s.%s" % (cname, f)]) == getattr(py, f).offset, (cname, f)
