@@ -130,8 +130,10 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-KERNEL_MODES = {0: "photon pool", 1: "one thread per photon", 2: "photon pool over pregenerated photons"}
-KERNEL_NAMES = {0: "k_simulate_pool", 1: "k_simulate", 2: "k_generate + k_simulate_pool"}
+KERNEL_MODES = {0: "photon pool", 1: "one thread per photon", 2: "photon pool over pregenerated photons",
+                3: "wavefront (per-step passes over pregenerated photons)"}
+KERNEL_NAMES = {0: "k_simulate_pool", 1: "k_simulate", 2: "k_generate + k_simulate_pool",
+                3: "k_generate + k_wf_start + k_wf_trace + k_wf_step"}
 
 WORKLOADS = {
     "nested_boxes": "nested_boxes_torch_100k_input_photons",
@@ -289,18 +291,27 @@ def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
         r = eng.autotune(0, sample, trials=2)
         tuned[kind] = {"mode": KERNEL_MODES[r["kernel_mode"]], "refill_min": r["refill_min"],
                        "refill_period": r["refill_period"], "blocks_per_sm": r["blocks_per_sm"],
-                       "walk_min": r["walk_min"]}
+                       "walk_min": r["walk_min"], "rng_call": r["rng_call"]}
     photons = {id(ev[2]): int(ev[2].view(np.uint32)[:, 0, 3].astype(np.int64).sum()) for ev in events}
     total_photons = sum(photons.values())
     for kind, eid, gs in events[:4]:                          # warm-up
         engines[kind].simulate(eid, gs)
-    # ---- plain capacity (closed loop)
+    # ---- plain capacity (closed loop), each event's own time kept for the bound below
+    event_s = []
     t0 = time.perf_counter()
     for kind, eid, gs in events:
+        a = time.perf_counter()
         engines[kind].simulate(eid, gs)
         engines[kind].hits()
+        event_s.append(time.perf_counter() - a)
     plain_s = time.perf_counter() - t0
     plain_rate = total_photons / plain_s
+    # Photon-weighted upper bound of batched / plain: batching can at best run every photon at the rate the largest
+    # events of its kind reach alone (they fill the GPU), so the stream takes at least sum(photons / peak rate).
+    peak = {}
+    for (kind, _, gs), s in zip(events, event_s):
+        peak[kind] = max(peak.get(kind, 0.0), photons[id(gs)] / s)
+    bound = plain_s / sum(photons[id(gs)] / peak[kind] for kind, _, gs in events)
     servers = {k: E.Server(e, slots=2) for k, e in engines.items()}
 
     def run_batched(arrivals):
@@ -372,6 +383,9 @@ def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
         "events": len(events), "photons": total_photons, "submitter_threads": submitters,
         "plain_photons_per_s": plain_rate, "batched_photons_per_s": batched_rate,
         "batched_over_plain": batched_rate / plain_rate,
+        "batched_over_plain_bound": bound,
+        "bound_rule": "plain time / sum over events of photons / (rate of the fastest plain event of its kind)",
+        "peak_photons_per_s": peak,
         "batched_without_graph_photons_per_s": total_photons / direct_s,
         "graph": {k: {"launches": v["graph_launches"], "instantiations": v["graph_instantiations"]}
                   for k, v in graph_stats.items()},
@@ -380,7 +394,7 @@ def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
         "plain_latency_ms": {"p50": 1e3 * pct(lat_p, 50), "p99": 1e3 * pct(lat_p, 99)},
         "batches": {k: v["batches"] for k, v in stats.items()},
         "kernel": tuned,
-        "server": {"slots": 2, "target_batch_photon": 4 << 20, "min_batch_photon": 2 << 20,
+        "server": {"slots": 2, "target_batch_photon": 4 << 20, "min_batch_photon": 2 << 20, "max_wait_us": 1000,
                    "hbm_budget_bytes": 120 << 30},
     }
 
@@ -394,7 +408,7 @@ def same_config_batching(geom, kind, n_events, tune, submitters=16):
     photons = sum(int(g.view(np.uint32)[:, 0, 3].astype(np.int64).sum()) for g, _ in events)
     eng = E.Engine(geom, kernel_mode=tune["kernel_mode"], refill_min=tune["refill_min"],
                    refill_period=tune["refill_period"], blocks_per_sm=tune.get("blocks_per_sm", 0),
-                   walk_min=tune.get("walk_min", 1))
+                   walk_min=tune.get("walk_min", 1), rng_call=tune.get("rng_call", 0))
     eng.simulate(0, *events[0])
     t0 = time.perf_counter()
     for k, (g, inp) in enumerate(events):
@@ -446,11 +460,11 @@ def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=N
     n_photon = int(gs.view(np.uint32)[:, 0, 3].astype(np.int64).sum())
     n_inp = 0 if inp is None else len(inp)
     if form:
-        mode, refill, period, blocks, walk = (tuple(form) + (0, 1))[:5]
+        mode, refill, period, blocks, walk, rcall = (tuple(form) + (0, 1, 0)[len(form) - 3:])[:6]
         eng = E.Engine(geom, device=local, precision=precision, kernel_mode=mode, refill_min=refill,
-                       refill_period=period, blocks_per_sm=blocks, walk_min=walk)
+                       refill_period=period, blocks_per_sm=blocks, walk_min=walk, rng_call=rcall)
         tune = {"kernel_mode": mode, "refill_min": refill, "refill_period": period, "blocks_per_sm": blocks,
-                "walk_min": walk}
+                "walk_min": walk, "rng_call": rcall}
     else:
         # kernel form picked by the autotuner on a 10% sample of the workload (setup, outside the timed region)
         eng = E.Engine(geom, device=local, precision=precision)
@@ -529,7 +543,7 @@ def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=N
                    "photons_per_step": n_photon, "gensteps_per_step": len(gs), "hits_per_step": hits,
                    "kernel": {"mode": KERNEL_MODES[tune["kernel_mode"]], "refill_min": tune["refill_min"],
                               "refill_period": tune["refill_period"], "blocks_per_sm": tune.get("blocks_per_sm", 0),
-                              "walk_min": tune.get("walk_min", 1),
+                              "walk_min": tune.get("walk_min", 1), "rng_call": tune.get("rng_call", 0),
                               "chosen_by": "--form" if form else "autotuner on 10% sample"},
                    "max_bounce": 31},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -630,8 +644,9 @@ def main():
                     help="gensteps per event (default: the workload's own, 2000 for the crystal array)")
     ap.add_argument("--workload", default="crystal_array", choices=sorted(WORKLOADS))
     ap.add_argument("--form", default=None,
-                    help="kernel form MODE,REFILL,PERIOD[,BLOCKS_PER_SM[,WALK_MIN]] instead of the autotuner's choice "
-                         "(MODE 0: photon pool, 1: one thread per photon, 2: photon pool over pregenerated photons)")
+                    help="kernel form MODE,REFILL,PERIOD[,BLOCKS_PER_SM[,WALK_MIN[,RNG_CALL]]] instead of the "
+                         "autotuner's choice (MODE 0: photon pool, 1: one thread per photon, 2: photon pool over "
+                         "pregenerated photons, 3: wavefront)")
     ap.add_argument("--batch-events", type=int, default=None,
                     help="events of the workload for the same-configuration plain vs batched comparison")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1],

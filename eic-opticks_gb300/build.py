@@ -21,10 +21,10 @@ LIB = os.path.join(HERE, "libgbopticks.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["gbo_engine.cu", "gbo_merge.cu"]
+CU_SOURCES = ["gbo_engine.cu", "gbo_sim_tree0.cu", "gbo_sim_tree1.cu", "gbo_sim_tree2.cu", "gbo_merge.cu"]
 CPP_SOURCES = ["gbo_accel.cpp"]
 HEADERS = ["gbo_device.cuh", "gbo_csg.cuh", "gbo_physics.cuh", "gbo_trace.cuh", "gbo_accel.h", "gbo_serve.inl",
-           "gbo_merge.h"]
+           "gbo_merge.h", "gbo_sim.cuh", "gbo_sim_forms.inl"]
 
 
 def _newer(target, deps):

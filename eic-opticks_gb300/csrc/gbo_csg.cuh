@@ -16,7 +16,7 @@ namespace gbo {
 
 // Leaf types the benchmark and test geometries use rarely stay out of line, to keep the traversal loop's code (and
 // the instruction cache it needs) small; the common ones (sphere, zsphere, cylinder, box3) are inlined.
-#define GBO_COLD __device__ __noinline__
+#define GBO_COLD static __device__ __noinline__
 
 constexpr float RT_DEFAULT_MAX = 1.e27f;
 

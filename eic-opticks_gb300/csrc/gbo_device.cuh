@@ -86,7 +86,7 @@ GBO_DEV void skip(RngT<CALL>& r, unsigned n) { r.pos += n; }
 
 // One Philox block out of line (RngT<true>): arguments and result travel in registers (no address is taken), and the
 // call runs once per four draws.
-__device__ __noinline__ uint4 philox_block(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1)
+static __device__ __noinline__ uint4 philox_block(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1)
 {
     uint32_t o[4];
     philox10(c0, c1, c2, c3, k0, k1, o);

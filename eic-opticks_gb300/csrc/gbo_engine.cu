@@ -1,4 +1,5 @@
-// gbo_engine.cu : simulate kernel, hit compaction kernels and the C ABI of libgbopticks.so.
+// gbo_engine.cu : engine lifecycle, event flow, hit compaction kernels and the C ABI of libgbopticks.so (the
+// simulation kernels themselves are in gbo_sim.cuh, compiled per CSG form by gbo_sim_tree*.cu).
 //
 // One event = one pass of the photon program of CSGOptiX/CSGOptiX7.cu:405-503 over every photon its gensteps
 // describe, then hit selection (sysrap/SU.cu:89-92,155-160 via qudarap/QEvt.cc:934-967,1113-1131).
@@ -6,9 +7,11 @@
 // Device-side flow of an event:
 //   k_genstep_prefix   inclusive prefix of genstep numphoton (replaces the seed array of QEvt.cu:181-237: a
 //                      photon finds its genstep by binary search, so no per-photon seed buffer is written)
-//   k_simulate<TREE>   one thread per photon: Philox stream, generate, bounce loop of trace + propagate, final
-//                      record; a warp ballot writes one 32-bit hit-bitmap word per 32 photons and hit photons are
-//                      appended (warp-aggregated atomics) to an unordered buffer unless the full photon array is kept
+//   k_generate         kernel mode 2: every photon of the launch generated up front
+//   k_simulate_pool    persistent photon pool (or k_simulate, one thread per photon): bounce loop of trace +
+//                      propagate, final record; a warp ballot writes one 32-bit hit-bitmap word per 32 photons and
+//                      hit photons are appended (warp-aggregated atomics) to an unordered buffer unless the full
+//                      photon array is kept
 //   k_word_prefix      per-word popcount prefix inside 256-word blocks + block totals
 //   k_block_offsets    exclusive scan of the block totals (one block) -> number of hits
 //   k_gather_*         hits written in photon order (the order thrust::copy_if gives the reference)
@@ -25,180 +28,12 @@
 
 #include "../../include/gbopticks.h"
 #include "gbo_accel.h"
-#include "gbo_trace.cuh"
+#include "gbo_sim.cuh"
 #include "gbo_merge.h"
 
 namespace gbo {
 
-#ifndef GBO_SIM_MINB
-#define GBO_SIM_MINB 5              // minimum resident blocks per SM asked of ptxas for the one-thread simulate kernel
-                                    // (binary32, no CSG trees): 5 x 128 threads (96 registers) measured fastest
-#endif
-#ifndef GBO_SIM_MINB_WIDE
-#define GBO_SIM_MINB_WIDE 1         // the same for its CSG-tree and precision forms, which need their registers
-#endif
-#ifndef GBO_POOL_MINB
-#define GBO_POOL_MINB 4             // the same for the persistent photon-pool kernel: 4 x 128 threads per SM (128
-                                    // registers) measured 12 % faster than ptxas' unbounded choice on the crystal event
-#endif
-#ifndef GBO_POOL_MINB_TREE
-#define GBO_POOL_MINB_TREE 3        // the pool kernel's form for geometries with CSG trees: 3 x 128 threads per SM
-                                    // (168 registers, no spills) measured 3 % faster than 4 (128 registers, 860 B of
-                                    // spills) on the 20,000-sensor event
-#endif
-#ifdef GBO_POOL_MAXNREG                // register budget of the pool kernel instead of its launch bounds
-#define GBO_POOL_BOUNDS __maxnreg__(GBO_POOL_MAXNREG)
-#else
-#define GBO_POOL_BOUNDS __launch_bounds__(SIM_BLOCK, TREE ? GBO_POOL_MINB_TREE : GBO_POOL_MINB)
-#endif
-#ifdef GBO_GENERATE_INLINE
-#define GBO_GEN GBO_DEV
-#else
-#define GBO_GEN __device__ __noinline__   // photon generation runs once per photon: kept out of the bounce loop's code
-#endif
-constexpr int SIM_BLOCK = 128;
 constexpr int SCAN_WORDS = 256;     // words per block in k_word_prefix
-
-struct Params {
-    Accel acc;
-    Tables tab;
-    int max_bounce;
-    float max_time, tmin, tmin0, tmax;
-    uint32_t eps0_mask, hitmask;
-    uint64_t seed, position0;
-    const float4* gs;
-    const unsigned long long* gs_end;     // inclusive prefix of numphoton
-    int num_gs;
-    long long num_photon;
-    unsigned long long photon_offset;
-    const gbo_sphoton* input_photon;
-    gbo_sphoton* photon_out;
-    gbo_seq* seq_out;
-    gbo_sphoton* hit_unordered;
-    unsigned long long* hit_count;
-    uint32_t* bitmap;
-    // several events in one launch: event e owns gensteps [ev_gs_begin[e], ev_gs_begin[e+1]) and launch photons
-    // [ev_photon_begin[e], ev_photon_begin[e+1]); its photons use stream position ev_pos0[e] and event-local indices
-    int num_events;                         // 0: single event (photon_offset, position0 above)
-    const int* ev_gs_begin;
-    const unsigned long long* ev_photon_begin;
-    const unsigned long long* ev_pos0;
-    const unsigned long long* ev_photon_offset;     // event-local index of each entry's first photon (a piece of a
-                                                    // sliced event starts past 0); nullptr: all 0
-    unsigned long long* hit_gidx;           // launch index of each unordered hit (batched launches)
-    // pregenerated photons (kernel mode 2): k_generate writes each photon as generated and its random-stream
-    // place (draws consumed, subsequence); the pool kernel's refills read them instead of generating
-    gbo_sphoton* gen_photon;
-    ulonglong2* gen_rng;
-    int* gen_hint;
-    // start instance of each genstep's photons (k_genstep_hint), a traversal hint only; nullptr: none
-    const int* gs_hint;
-    int walk_min;                           // pool kernels: parked lanes that trigger the gathered TLAS walks
-};
-
-template <class R>
-GBO_GEN void generate(const Params& P, long long idx, Photon& p, R& rng, int& hint);
-
-// Kernel forms: TREE 1 when any prim is a CSG tree, 2 when CSG list nodes occur as well (their evaluation is
-// compiled only into that form); PRECISE for the precision mode (binary64 root polish in the quadric leaves,
-// binary64 position / time accumulators).  The default form compiles none of the latter.  RCALL: Philox blocks by
-// an out-of-line call instead of inlined rounds (RngT).
-template <int TREE, bool PRECISE, bool RCALL>
-__global__ void __launch_bounds__(SIM_BLOCK, (TREE || PRECISE) ? GBO_SIM_MINB_WIDE : GBO_SIM_MINB)
-k_simulate(const __grid_constant__ Params P)
-{
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = idx < P.num_photon;
-    Photon p;
-    bool is_hit = false;
-    if (active) {
-        RngT<RCALL> rng;
-        Acc64 acc;
-        int hint;
-        generate(P, idx, p, rng, hint);
-        if (PRECISE) acc_init(acc, p);
-
-        int bounce = 0;
-        if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
-        while (bounce < P.max_bounce && p.time < P.max_time) {
-            const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
-            Hit h;
-            trace<TREE, PRECISE>(P.acc, p.pos, p.mom, tmin, P.tmax, hint, h);
-            if ((h.prim_boundary & 0xffffu) == 0xffffu) break;
-            hint = (int)(h.iindex_identity >> 16);
-            h.normal = normalize(h.normal);
-            const int command = propagate(P.tab, p, h, rng, PRECISE ? &acc : nullptr);
-            bounce++;
-            if (P.seq_out) seq_add(P.seq_out + idx, (unsigned)bounce, flag_of(p), boundary_of(p));
-            if (command == CMD_BREAK) break;
-        }
-        is_hit = (p.flagmask & P.hitmask) == P.hitmask;
-        if (P.photon_out) store_photon(P.photon_out + idx, p);
-    }
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned mask = __ballot_sync(0xffffffffu, is_hit);
-    const long long word = idx >> 5;
-    if (lane == 0 && word * 32 < P.num_photon) P.bitmap[word] = mask;
-    if (P.hit_unordered && mask) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(P.hit_count, (unsigned long long)__popc(mask));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (is_hit) {
-            store_photon(P.hit_unordered + base + __popc(mask & ((1u << lane) - 1u)), p);
-            if (P.hit_gidx) P.hit_gidx[base + __popc(mask & ((1u << lane) - 1u))] = (unsigned long long)idx;
-        }
-    }
-}
-
-// ---- persistent form: lanes refill from a photon pool so a warp never idles behind its longest photon --------
-
-// `hint` receives the start instance found for the photon's genstep (-1 when none was computed)
-template <class R>
-GBO_GEN void generate(const Params& P, long long idx, Photon& p, R& rng, int& hint)
-{
-    int lo = 0, hi = P.num_gs - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (__ldg(P.gs_end + mid) > (unsigned long long)idx) hi = mid; else lo = mid + 1;
-    }
-    hint = P.gs_hint ? __ldg(P.gs_hint + lo) : -1;
-    const float4* g = P.gs + 6 * (size_t)lo;
-    float4 gq[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) gq[k] = __ldg(g + k);
-    unsigned long long photon_idx = P.photon_offset + (unsigned long long)idx;
-    uint64_t pos0 = P.position0;
-    if (P.num_events > 0) {
-        int a = 0, z = P.num_events - 1;          // event owning genstep lo
-        while (a < z) {
-            const int m = (a + z + 1) >> 1;
-            if (__ldg(P.ev_gs_begin + m) <= lo) a = m; else z = m - 1;
-        }
-        photon_idx = (unsigned long long)idx - __ldg(P.ev_photon_begin + a);
-        if (P.ev_photon_offset) photon_idx += __ldg(P.ev_photon_offset + a);
-        pos0 = __ldg(P.ev_pos0 + a);
-    }
-    rng_init(rng, P.seed, photon_idx, pos0);
-    p.pos = f3(0.f, 0.f, 0.f); p.time = 0.f; p.mom = f3(0.f, 0.f, 0.f); p.hitcount_iindex = 0u;
-    p.pol = f3(0.f, 0.f, 0.f); p.wavelength = 0.f;
-    p.orient_boundary_flag = 0u; p.identity = 0u; p.index = 0u; p.flagmask = 0u;
-    const int gencode = __float_as_int(gq[0].x);
-    switch (gencode) {
-        case GBO_GS_TORCH: gen_torch(p, rng, gq, photon_idx); break;
-        case GBO_GS_CERENKOV:
-        case GBO_GS_G4Cerenkov_modified: gen_cerenkov(P.tab, p, rng, gq); break;
-        case GBO_GS_SCINTILLATION:
-        case GBO_GS_DsG4Scintillation_r4695: gen_scint(P.tab, p, rng, gq); break;
-        case GBO_GS_INPUT_PHOTON:
-            if (P.input_photon) { load_photon(p, P.input_photon + idx); set_flag(p, GBO_TORCH); }
-            else { set_flag(p, GBO_NAN_ABORT); p.time = __int_as_float(0x7f800000); }   // hosts refuse this case
-            break;
-        default: break;
-    }
-    set_index(p, photon_idx);
-}
-
-constexpr int POOL_CHUNK = 32;      // pregenerated photons a warp claims at once (kernel mode 2)
 
 // every photon of the launch generated up front, converged, so that the pool kernel's refills are plain loads
 __global__ void __launch_bounds__(SIM_BLOCK) k_generate(const __grid_constant__ Params P)
@@ -212,159 +47,6 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_generate(const __grid_constant__ 
     store_photon(P.gen_photon + idx, p);
     P.gen_rng[idx] = make_ulonglong2(rng.pos, ((unsigned long long)rng.sub_hi << 32) | rng.sub_lo);
     P.gen_hint[idx] = hint;
-}
-
-// Kernel-mode-2 refill (warp-uniform chunk state cbase, cn, cused): idle lanes take the next pregenerated photons in
-// lane order, the warp claiming POOL_CHUNK more with one atomic when its chunk runs short.
-template <bool PRECISE, class R>
-GBO_DEV void refill_pregenerated(const Params& P, unsigned long long* pool, unsigned idle, unsigned lane, unsigned lt,
-                                 bool& live, long long& idx, Photon& p, R& rng, int& hint, Acc64& acc, int& bounce,
-                                 long long& cbase, int& cn, int& cused, bool& pool_open)
-{
-    const int n_idle = __popc(idle), rank = __popc(idle & lt), avail = cn - cused;
-    long long nb = 0;
-    int nn = 0;
-    if (avail < n_idle) {
-        unsigned long long b = 0;
-        if (lane == 0) b = atomicAdd(pool, (unsigned long long)POOL_CHUNK);
-        nb = (long long)__shfl_sync(0xffffffffu, b, 0);
-        const long long left = P.num_photon - nb;
-        nn = left <= 0 ? 0 : (left < POOL_CHUNK ? (int)left : POOL_CHUNK);
-    }
-    if (!live) {
-        const long long j = rank < avail ? cbase + cused + rank : (rank - avail < nn ? nb + (rank - avail) : -1);
-        if (j >= 0) {
-            idx = j;
-            load_photon_streamed(p, P.gen_photon + idx);
-            const ulonglong2 r = __ldcg(P.gen_rng + idx);
-            rng_init(rng, P.seed, r.y, r.x);
-            hint = __ldcg(P.gen_hint + idx);
-            if (PRECISE) acc_init(acc, p);
-            bounce = 0;
-            if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
-            live = true;
-        }
-    }
-    if (avail < n_idle) {
-        cbase = nb;
-        cn = nn;
-        cused = n_idle - avail < nn ? n_idle - avail : nn;
-        if (nn == 0) pool_open = false;         // drained: every claimed photon has been handed out
-    } else {
-        cused += n_idle;
-    }
-}
-
-// PREGEN: the kernel-mode-2 form without the generator.  Without a call to the out-of-line generator, its
-// by-reference arguments no longer force the photon state through local memory (crystal event 751M -> 864M
-// photons/s).
-template <int TREE, bool PRECISE, bool PREGEN, bool RCALL>
-__global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P,
-                                                             unsigned long long* pool, int refill_min, int period)
-{
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned lt = (1u << lane) - 1u;
-    bool live = false;
-    bool pool_open = true;
-    long long idx = -1;
-    int bounce = 0;
-    int hint = -1;
-    int it = 0;
-    Photon p;
-    RngT<RCALL> rng;
-    Acc64 acc;
-    // mode 2 (warp-uniform): the warp's claimed chunk of pregenerated photons [cbase, cbase + cn), cused taken
-    long long cbase = 0;
-    int cn = 0, cused = 0;
-    bool parked = false;            // the photon's step waits for a gathered TLAS walk
-    for (;; it++) {
-        // refill every `period` steps (or when the warp is empty): idle lanes take the next photon indices in lane
-        // order; mode 2 claims them POOL_CHUNK at a time (one atomic per chunk) and loads them as generated, the
-        // other pool mode claims exactly the idle lanes' count and generates them
-        const unsigned idle = __ballot_sync(0xffffffffu, !live);
-        const bool refill = pool_open && (idle == 0xffffffffu || (it % period == 0 && __popc(idle) >= refill_min));
-        if (PREGEN || P.gen_photon) {
-            if (refill)
-                refill_pregenerated<PRECISE>(P, pool, idle, lane, lt, live, idx, p, rng, hint, acc, bounce, cbase, cn,
-                                             cused, pool_open);
-        } else if constexpr (!PREGEN) {
-            if (refill) {
-                unsigned long long base = 0;
-                const int leader = __ffs(idle) - 1;
-                if ((int)lane == leader) base = atomicAdd(pool, (unsigned long long)__popc(idle));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (base + __popc(idle) >= (unsigned long long)P.num_photon) pool_open = false;
-                if (!live) {
-                    const unsigned long long mine = base + __popc(idle & lt);
-                    if (mine < (unsigned long long)P.num_photon) {
-                        idx = (long long)mine;
-                        generate(P, idx, p, rng, hint);
-                        if (PRECISE) acc_init(acc, p);
-                        bounce = 0;
-                        if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
-                        live = true;
-                    }
-                }
-            }
-        }
-        if (!__any_sync(0xffffffffu, live)) {
-            if (!pool_open) break;
-            continue;
-        }
-        // gathered TLAS walks: parked lanes walk once enough of them wait, or when no live lane is left to step
-        const unsigned parked_mask = __ballot_sync(0xffffffffu, parked);
-        const bool walk_now = parked_mask != 0u &&
-                              (__popc(parked_mask) >= P.walk_min || parked_mask == __ballot_sync(0xffffffffu, live));
-        bool done = false;
-        if (live) {
-            if (parked || (bounce < P.max_bounce && p.time < P.max_time)) {
-                const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
-                // one call site: a query that may stop before its TLAS walk, or a parked lane's whole query (its
-                // hint instance tested again, then the walk) once the warp gathers the walks
-                Best b;
-                trace_begin(b, P.tmax);
-                int r = TRACE_WALK;
-                if (!parked || walk_now)
-                    r = trace_items<TREE, PRECISE>(P.acc, p.pos, p.mom, tmin, hint, !parked && P.walk_min > 1, b);
-                parked = r == TRACE_WALK;
-                if (!parked) {
-                    Hit h;
-                    trace_finish(P.acc, p.pos, p.mom, b, h);
-                    if ((h.prim_boundary & 0xffffu) == 0xffffu) {
-                        done = true;
-                    } else {
-                        hint = (int)(h.iindex_identity >> 16);
-                        h.normal = normalize(h.normal);
-                        const int command = propagate(P.tab, p, h, rng, PRECISE ? &acc : nullptr);
-                        bounce++;
-                        if (P.seq_out) seq_add(P.seq_out + idx, (unsigned)bounce, flag_of(p), boundary_of(p));
-                        done = command == CMD_BREAK;
-                    }
-                }
-            } else {
-                done = true;
-            }
-        }
-        const bool is_hit = done && (p.flagmask & P.hitmask) == P.hitmask;
-        if (done) {
-            if (is_hit) atomicOr(P.bitmap + (idx >> 5), 1u << (idx & 31));
-            if (P.photon_out) store_photon(P.photon_out + idx, p);
-            live = false;
-        }
-        if (P.hit_unordered) {
-            const unsigned hm = __ballot_sync(0xffffffffu, is_hit);
-            if (hm) {
-                const int leader = __ffs(hm) - 1;
-                unsigned long long base = 0;
-                if ((int)lane == leader) base = atomicAdd(P.hit_count, (unsigned long long)__popc(hm));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (is_hit) {
-                    store_photon(P.hit_unordered + base + __popc(hm & lt), p);
-                    if (P.hit_gidx) P.hit_gidx[base + __popc(hm & lt)] = (unsigned long long)idx;
-                }
-            }
-        }
-    }
 }
 
 // Start instance of each genstep's photons: of the instances whose padded world box holds the genstep position
@@ -557,21 +239,6 @@ __global__ void k_tex_lookup(Tables t, const float2* xy, int n, int which, float
     else out[i] = make_float4(tex2D<float>(t.icdf_tex, c.x, c.y), 0.f, 0.f, 0.f);
 }
 
-// one thread per ray: the engine's closest-hit query (CSG/CSGScan.cu's _CSGScan_intersect plays this role for the
-// reference); t = -1 on a miss
-template <int TREE, bool POLISH>
-__global__ void k_trace_rays(Accel acc, const float3* pos, const float3* dir, int n, float tmin, float tmax,
-                             float* t_out, unsigned* boundary_out)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    Hit h;
-    trace<TREE, POLISH>(acc, pos[i], dir[i], tmin, tmax, -1, h);
-    const bool miss = (h.prim_boundary & 0xffffu) == 0xffffu;
-    t_out[i] = miss ? -1.f : h.t;
-    boundary_out[i] = miss ? 0xffffffffu : (h.prim_boundary & 0xffffu);
-}
-
 __global__ void k_scint_wavelength(Tables t, const float* u, int n, float* out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -625,6 +292,28 @@ struct DBuf {
         return 0;
     }
     void release() { if (ptr) cudaFree(ptr); ptr = nullptr; cap = 0; }
+};
+
+// Kernel mode 3's device state for n photons and max_bounce steps (hit records, the two step lists and the walk
+// queue, the step counters), held in three buffers that grow as needed.
+struct WavefrontBufs {
+    DBuf<float4> hit;
+    DBuf<int> list;
+    DBuf<unsigned long long> count;
+    void release() { hit.release(); list.release(); count.release(); }
+    int ensure(long long n, int max_bounce, Wavefront& w)
+    {
+        int rc;
+        if ((rc = hit.ensure(2 * (size_t)n)) || (rc = list.ensure(3 * (size_t)n)) ||
+            (rc = count.ensure(2 * (size_t)(max_bounce + 1))))
+            return rc;
+        w.hit = hit.ptr;
+        w.list[0] = list.ptr;
+        w.list[1] = list.ptr + n;
+        w.walk = list.ptr + 2 * n;
+        w.count = count.ptr;
+        return 0;
+    }
 };
 
 template <typename T>
@@ -700,9 +389,10 @@ struct gbo_engine {
     gbo::MergeScratch* merge_scratch = nullptr;     // the merge's work buffers, kept between events
     gbo_server* event_server = nullptr;             // started by the first gbo_event_submit
     std::mutex event_server_mu;
-    DBuf<gbo_sphoton> gen_photon;           // kernel mode 2: pregenerated photons, their random-stream places and
-    DBuf<ulonglong2> gen_rng;               // start instances
+    DBuf<gbo_sphoton> gen_photon;           // kernel modes 2 and 3: pregenerated photons, their random-stream places
+    DBuf<ulonglong2> gen_rng;               // and start instances (kernel mode 3: the live photons' state)
     DBuf<int> gen_hint;
+    WavefrontBufs wf;                       // kernel mode 3
     DBuf<int> gs_hint;                      // start instance per genstep
     long long num_merged = -1;
     DBuf<uint32_t> bitmap, word_prefix, block_sum;
@@ -716,9 +406,16 @@ struct gbo_engine {
     gbo_stats stats{};
 };
 
-// Kernel form index: 2 x csg_form + precision, 6 for the single-leaf binary32 kernels with Philox blocks by call.
-// The CSG-tree forms always call (their code is large enough to miss in the instruction cache otherwise); the
-// single-leaf forms inline the rounds unless gbo_config.rng_call asks for the call (binary32 only).
+// Simulation kernels one launch_simulate issues over n photons (the generation kernel counted by the caller): one,
+// or in kernel mode 3 the wavefront's start pass and three passes per step.
+static int simulate_kernels(const gbo_engine* e, long long n)
+{
+    if (e->cfg.kernel_mode == 3 && !e->cfg.precision && n < 0x7fffffffll) return 1 + 3 * e->cfg.max_bounce;
+    return 1;
+}
+
+// Kernel form index: 2 x csg_form + precision, 6 for the single-leaf binary32 kernels with Philox blocks by call
+// (the CSG-tree forms always call; gbo_config.rng_call chooses for the single-leaf binary32 form).
 static int kernel_form(const gbo_engine* e)
 {
     const bool precise = e->cfg.precision != 0;
@@ -726,11 +423,23 @@ static int kernel_form(const gbo_engine* e)
     return 2 * e->csg_form + (precise ? 1 : 0);
 }
 
-template <int TREE, bool PRECISE, bool RCALL>
-static void launch_form(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s,
-                        cudaEvent_t after_gen)
+// One launch of the simulation kernel over n photons in the engine's kernel form (pool or one thread per photon,
+// CSG trees or not, precision mode or not); `pool` is the photon-pool counter, zeroed by the caller.  With
+// P.gen_photon set (kernel modes 2 and 3) the generation kernel runs first and the pool kernel (or the wavefront
+// passes, over `wf`) reads its photons; `after_gen` (optional) is recorded between the two.
+static void launch_simulate(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s,
+                            cudaEvent_t after_gen = nullptr, const Wavefront* wf = nullptr)
 {
-    if (e->cfg.kernel_mode != 1) {
+    SimLaunch L{};
+    L.n = n;
+    L.pool = pool;
+    L.stream = s;
+    L.kernel_mode = e->cfg.kernel_mode;
+    L.precise = e->cfg.precision != 0;
+    L.rng_call = e->cfg.rng_call == 1;
+    L.sms = e->sms;
+    if (wf) L.wf = *wf;
+    if (L.kernel_mode != 1) {
         if (P.gen_photon && n > 0) {
             k_generate<<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
             if (after_gen) cudaEventRecord(after_gen, s);
@@ -739,33 +448,14 @@ static void launch_form(const gbo_engine* e, const Params& P, long long n, unsig
         const long long need = (n + SIM_BLOCK - 1) / SIM_BLOCK;
         const int want = e->cfg.blocks_per_sm, occ = e->pool_occ[form] > 0 ? e->pool_occ[form] : 1;
         const long long resident = (long long)e->sms * (want > 0 && want < occ ? want : occ);
-        const long long grid = need < resident ? need : resident;
-        const int refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
-        const int period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
-        if (P.gen_photon)
-            k_simulate_pool<TREE, PRECISE, true, RCALL><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
-        else
-            k_simulate_pool<TREE, PRECISE, false, RCALL><<<(unsigned)grid, SIM_BLOCK, 0, s>>>(P, pool, refill, period);
-    } else {
-        k_simulate<TREE, PRECISE, RCALL><<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
+        L.grid = need < resident ? need : resident;
+        L.refill = e->cfg.refill_min < 1 ? 1 : (e->cfg.refill_min > 32 ? 32 : e->cfg.refill_min);
+        L.period = e->cfg.refill_period < 1 ? 1 : e->cfg.refill_period;
     }
-}
-
-// One launch of the simulation kernel over n photons in the engine's kernel form (pool or one thread per photon,
-// CSG trees or not, precision mode or not); `pool` is the photon-pool counter, zeroed by the caller.  With
-// P.gen_photon set (kernel mode 2) the generation kernel runs first and the pool kernel reads its photons;
-// `after_gen` (optional) is recorded between the two.
-static void launch_simulate(const gbo_engine* e, const Params& P, long long n, unsigned long long* pool, cudaStream_t s,
-                            cudaEvent_t after_gen = nullptr)
-{
-    switch (kernel_form(e)) {
-        case 0:  launch_form<0, false, false>(e, P, n, pool, s, after_gen); break;
-        case 1:  launch_form<0, true, false>(e, P, n, pool, s, after_gen); break;
-        case 2:  launch_form<1, false, true>(e, P, n, pool, s, after_gen); break;
-        case 3:  launch_form<1, true, true>(e, P, n, pool, s, after_gen); break;
-        case 4:  launch_form<2, false, true>(e, P, n, pool, s, after_gen); break;
-        case 5:  launch_form<2, true, true>(e, P, n, pool, s, after_gen); break;
-        default: launch_form<0, false, true>(e, P, n, pool, s, after_gen); break;
+    switch (e->csg_form) {
+        case 2:  sim_launch<2>(P, L); break;
+        case 1:  sim_launch<1>(P, L); break;
+        default: sim_launch<0>(P, L); break;
     }
 }
 
@@ -851,7 +541,7 @@ void gbo_engine_destroy(gbo_engine* e)
     e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->inst_box.release(); e->overlap.release(); e->clear.release(); e->prim.release(); e->solid.release();
     e->node.release(); e->plan.release(); e->itra.release(); e->optical.release();
     e->gs.release(); e->gs_end.release(); e->input.release(); e->photon.release(); e->seq.release();
-    e->hits_unordered.release(); e->hits.release(); e->merged.release(); gbo::merge_scratch_free(e->merge_scratch); e->merge_scratch = nullptr; e->gen_photon.release(); e->gen_rng.release(); e->gen_hint.release(); e->gs_hint.release(); e->bitmap.release(); e->word_prefix.release();
+    e->hits_unordered.release(); e->hits.release(); e->merged.release(); gbo::merge_scratch_free(e->merge_scratch); e->merge_scratch = nullptr; e->gen_photon.release(); e->gen_rng.release(); e->gen_hint.release(); e->wf.release(); e->gs_hint.release(); e->bitmap.release(); e->word_prefix.release();
     e->block_sum.release(); e->block_offset.release(); e->counters.release();
     if (e->host_counters) cudaFreeHost(e->host_counters);
     for (auto& v : e->ev) if (v) cudaEventDestroy(v);
@@ -909,6 +599,8 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
         }
     }
 
+    if (cfg && (cfg->kernel_mode < 0 || cfg->kernel_mode > 3))
+        return fail(GBO_ERR_ARG, "kernel_mode %d not in 0..3", cfg->kernel_mode);
     gbo_engine* e = new gbo_engine();
     e->device = device;
     if (cfg) e->cfg = *cfg; else gbo_config_default(&e->cfg);
@@ -957,15 +649,15 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     TRY(make_texture(&e->icdf_array, &e->icdf_tex, g->icdf, g->icdf_nx, g->icdf_ny, false));
     TRY(e->counters.ensure(4));
     {
-        int sms = 0, b[7] = {0, 0, 0, 0, 0, 0, 0};
+        int sms = 0, b[7] = {0, 0, 0, 0, 0, 0, 0};     // indexed by kernel_form()
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_simulate_pool<0, false, true, false>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_simulate_pool<0, true, true, false>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_simulate_pool<1, false, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_simulate_pool<1, true, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[4], k_simulate_pool<2, false, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[5], k_simulate_pool<2, true, true, true>, SIM_BLOCK, 0) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[6], k_simulate_pool<0, false, true, true>, SIM_BLOCK, 0) != cudaSuccess) {
+            sim_pool_occupancy<0>(false, false, &b[0]) != cudaSuccess ||
+            sim_pool_occupancy<0>(true, false, &b[1]) != cudaSuccess ||
+            sim_pool_occupancy<1>(false, true, &b[2]) != cudaSuccess ||
+            sim_pool_occupancy<1>(true, true, &b[3]) != cudaSuccess ||
+            sim_pool_occupancy<2>(false, true, &b[4]) != cudaSuccess ||
+            sim_pool_occupancy<2>(true, true, &b[5]) != cudaSuccess ||
+            sim_pool_occupancy<0>(false, true, &b[6]) != cudaSuccess) {
             gbo_engine_destroy(e);
             return fail(GBO_ERR_CUDA, "occupancy query failed");
         }
@@ -1051,11 +743,13 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     if (keep_photon) { if (at.photon_base == 0 && (rc = e->photon.ensure(at.capacity))) return rc; }
     else { if ((rc = e->hits_unordered.ensure(num_photon))) return rc; }
     if (keep_seq && at.photon_base == 0) { if ((rc = e->seq.ensure(at.capacity))) return rc; }
-    if (e->cfg.kernel_mode == 2) {
+    if (e->cfg.kernel_mode >= 2) {
         if ((rc = e->gen_photon.ensure(num_photon))) return rc;
         if ((rc = e->gen_rng.ensure(num_photon))) return rc;
         if ((rc = e->gen_hint.ensure(num_photon))) return rc;
     }
+    Wavefront wf{};
+    if (e->cfg.kernel_mode == 3 && (rc = e->wf.ensure(num_photon, e->cfg.max_bounce, wf))) return rc;
     if (num_gs > 0 && (rc = e->gs_hint.ensure(num_gs))) return rc;
 
     Params P = make_params(e);
@@ -1077,7 +771,7 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     int launches = prior_launches;
     const bool pool = e->cfg.kernel_mode != 1;
     if (pool && num_photon > 0) CU(cudaMemsetAsync(e->bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
-    if (e->cfg.kernel_mode == 2 && num_photon > 0) {
+    if (e->cfg.kernel_mode >= 2 && num_photon > 0) {
         P.gen_photon = e->gen_photon.ptr;
         P.gen_rng = e->gen_rng.ptr;
         P.gen_hint = e->gen_hint.ptr;
@@ -1090,9 +784,10 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     }
     CU(cudaEventRecord(e->ev[1], s));
     if (num_photon > 0) {
-        launch_simulate(e, P, num_photon, e->counters.ptr + 2, s, P.gen_photon ? e->ev[4] : nullptr);
+        launch_simulate(e, P, num_photon, e->counters.ptr + 2, s, P.gen_photon ? e->ev[4] : nullptr,
+                        e->cfg.kernel_mode == 3 ? &wf : nullptr);
         CU(cudaGetLastError());
-        launches++;
+        launches += simulate_kernels(e, num_photon);
     }
     CU(cudaEventRecord(e->ev[2], s));
     if (num_photon > 0) {
@@ -1371,6 +1066,10 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         for (const Cand& c : std::vector<Cand>{{1, 32, 1, 0, 1, 1}, {0, 4, 1, 0, 1, 1}, {0, 4, 4, 0, 1, 1},
                                                {2, 1, 1, 0, 1, 1}, {2, 4, 1, 0, 1, 1}})
             cands.push_back(c);
+    if (!e->cfg.precision) {                                                 // the wavefront form
+        cands.push_back({3, 4, 1, 0, 1, 0});
+        if (e->csg_form == 0) cands.push_back({3, 4, 1, 0, 1, 1});
+    }
     const int form = 2 * e->csg_form + (e->cfg.precision ? 1 : 0);
     for (int b = 1; b < e->pool_occ[form] && cands.size() < 32; b++) {       // fewer resident blocks than fit
         cands.push_back({2, 4, 1, b, 1, 0});
@@ -1477,20 +1176,16 @@ int gbo_trace_rays(gbo_engine* e, const float* pos, const float* dir, int32_t n,
     std::memcpy(in.data(), pos, (size_t)n * 12);
     std::memcpy(in.data() + (size_t)n * 3, dir, (size_t)n * 12);
     std::vector<float> out((size_t)n * 2);
-    const int form = 2 * e->csg_form + (e->cfg.precision ? 1 : 0);
+    const bool polish = e->cfg.precision != 0;
     int rc = with_scratch(in.size() * 4, in.data(), out.size() * 4, out.data(), [&](void* d_in, void* d_out) {
         const float3* dp = (const float3*)d_in;
         const float3* dd = (const float3*)((float*)d_in + (size_t)n * 3);
         float* dt = (float*)d_out;
         unsigned* db = (unsigned*)((float*)d_out + n);
-        const unsigned g = (unsigned)((n + 127) / 128);
-        switch (form) {
-            case 0: k_trace_rays<0, false><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
-            case 1: k_trace_rays<0, true><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
-            case 2: k_trace_rays<1, false><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
-            case 3: k_trace_rays<1, true><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
-            case 4: k_trace_rays<2, false><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
-            default: k_trace_rays<2, true><<<g, 128>>>(P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+        switch (e->csg_form) {
+            case 2:  trace_rays_launch<2>(polish, P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            case 1:  trace_rays_launch<1>(polish, P.acc, dp, dd, n, tmin, tmax, dt, db); break;
+            default: trace_rays_launch<0>(polish, P.acc, dp, dd, n, tmin, tmax, dt, db); break;
         }
     });
     if (rc) return rc;
@@ -1545,45 +1240,6 @@ static_assert(NA_OFF_BITMAP % 256 == 0 && NA_OFF_PREFIX % 256 == 0 && NA_OFF_BLO
               NA_OFF_BLOCK_OFF % 256 == 0 && NA_OFF_STAGING % 256 == 0, "scratch sections stay 256-byte aligned");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
-
-// The one-thread-per-photon program with a bounded hit append: hits beyond the staging capacity are counted
-// but not stored, and the host reports the overflow.
-template <int TREE>
-__global__ void __launch_bounds__(SIM_BLOCK) k_simulate_bounded(const __grid_constant__ Params P, long long cap)
-{
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    Photon p;
-    bool is_hit = false;
-    if (idx < P.num_photon) {
-        RngT<(TREE >= 1)> rng;
-        int hint;
-        generate(P, idx, p, rng, hint);
-        int bounce = 0;
-        while (bounce < P.max_bounce && p.time < P.max_time) {
-            const float tmin = (p.orient_boundary_flag & P.eps0_mask) ? P.tmin0 : P.tmin;
-            Hit h;
-            trace<TREE>(P.acc, p.pos, p.mom, tmin, P.tmax, hint, h);
-            if ((h.prim_boundary & 0xffffu) == 0xffffu) break;
-            hint = (int)(h.iindex_identity >> 16);
-            h.normal = normalize(h.normal);
-            const int command = propagate(P.tab, p, h, rng);
-            bounce++;
-            if (command == CMD_BREAK) break;
-        }
-        is_hit = (p.flagmask & P.hitmask) == P.hitmask;
-    }
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned mask = __ballot_sync(0xffffffffu, is_hit);
-    const long long word = idx >> 5;
-    if (lane == 0 && word * 32 < P.num_photon) P.bitmap[word] = mask;
-    if (mask) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(P.hit_count, (unsigned long long)__popc(mask));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        const unsigned long long slot = base + __popc(mask & ((1u << lane) - 1u));
-        if (is_hit && slot < (unsigned long long)cap) store_photon(P.hit_unordered + slot, p);
-    }
-}
 
 }  // namespace gbo
 
@@ -1679,9 +1335,9 @@ int gbo_simulate_noalloc(gbo_engine* e, int32_t event_id, const void* d_gs, int6
     const long long nblk = (words + SCAN_WORDS - 1) / SCAN_WORDS;
     if (total > 0) {
         const long long blocks = ((long long)total + SIM_BLOCK - 1) / SIM_BLOCK;
-        if (e->csg_form == 2) k_simulate_bounded<2><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P, NA_MAX_HIT);
-        else if (e->csg_form == 1) k_simulate_bounded<1><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P, NA_MAX_HIT);
-        else k_simulate_bounded<0><<<(unsigned)blocks, SIM_BLOCK, 0, s>>>(P, NA_MAX_HIT);
+        if (e->csg_form == 2) sim_launch_bounded<2>(P, NA_MAX_HIT, (unsigned)blocks, s);
+        else if (e->csg_form == 1) sim_launch_bounded<1>(P, NA_MAX_HIT, (unsigned)blocks, s);
+        else sim_launch_bounded<0>(P, NA_MAX_HIT, (unsigned)blocks, s);
         CU(cudaGetLastError());
         k_word_prefix<<<(unsigned)nblk, SCAN_WORDS, 0, s>>>(bitmap, words, word_prefix, block_sum);
         k_block_offsets<<<1, 1024, 0, s>>>(block_sum, nblk, block_offset, counters + 1);

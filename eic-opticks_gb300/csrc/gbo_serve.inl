@@ -87,9 +87,11 @@ struct Slot {
     DBuf<unsigned long long> gs_end, ev_photon_begin, ev_pos0, ev_photon_offset, block_offset, counters, hit_gidx, ev_hit;
     DBuf<int> ev_gs_begin;
     DBuf<gbo_sphoton> input, hits_unordered, hits;
-    DBuf<gbo_sphoton> gen_photon;       // kernel mode 2: the batch's pregenerated photons
+    DBuf<gbo_sphoton> gen_photon;       // kernel modes 2 and 3: the batch's pregenerated photons
     DBuf<ulonglong2> gen_rng;
     DBuf<int> gen_hint, gs_hint;        // start instance per pregenerated photon / per genstep
+    WavefrontBufs wf;                   // kernel mode 3
+    Wavefront wf_dev{};
     DBuf<uint32_t> bitmap, word_prefix, block_sum;
     HBuf<gbo_quad6> h_gs;
     HBuf<unsigned long long> h_gs_end, h_ev_photon_begin, h_ev_pos0, h_ev_photon_offset, h_ev_hit, h_counters;
@@ -103,6 +105,7 @@ struct Slot {
         gs.release(); gs_end.release(); ev_photon_begin.release(); ev_pos0.release(); ev_photon_offset.release();
         block_offset.release(); counters.release(); hit_gidx.release(); ev_hit.release(); ev_gs_begin.release();
         input.release(); hits_unordered.release(); hits.release(); gen_photon.release(); gen_rng.release(); gen_hint.release(); gs_hint.release();
+        wf.release();
         bitmap.release(); word_prefix.release();
         block_sum.release(); h_gs.release(); h_gs_end.release(); h_ev_photon_begin.release(); h_ev_pos0.release();
         h_ev_photon_offset.release(); h_ev_hit.release(); h_counters.release(); h_ev_gs_begin.release();
@@ -128,9 +131,11 @@ std::atomic<int>& big_counter(int device) { return g_big_in_flight[device >= 0 &
 constexpr size_t SERVE_DIRECT_HIT_BYTES = 64ull << 20;
 
 // device bytes per photon slot of a batch: bitmap + prefix bits, unordered + ordered hit capacity, hit index;
-// kernel mode 2 adds the pregenerated photon and its random-stream place
+// kernel modes 2 and 3 add the pregenerated photon, its random-stream place and start instance; kernel mode 3 adds
+// the hit record and three list entries
 constexpr double SERVE_BYTES_PER_PHOTON = 0.25 + 64.0 + 64.0 + 8.0;
 constexpr double SERVE_BYTES_PER_PHOTON_GEN = 64.0 + 16.0 + 4.0;
+constexpr double SERVE_BYTES_PER_PHOTON_WF = 32.0 + 12.0;
 
 }  // namespace
 
@@ -185,7 +190,7 @@ int enqueue_batch(gbo_engine* e, Slot& sl, int n_ev, long long n_gs, bool has_in
     P.ev_pos0 = sl.ev_pos0.ptr;
     P.ev_photon_offset = sl.ev_photon_offset.ptr;
     P.hit_gidx = sl.hit_gidx.ptr;
-    if (e->cfg.kernel_mode == 2) {
+    if (e->cfg.kernel_mode >= 2) {
         P.gen_photon = sl.gen_photon.ptr;
         P.gen_rng = sl.gen_rng.ptr;
         P.gen_hint = sl.gen_hint.ptr;
@@ -194,7 +199,7 @@ int enqueue_batch(gbo_engine* e, Slot& sl, int n_ev, long long n_gs, bool has_in
         if (e->cfg.kernel_mode != 1) CU(cudaMemsetAsync(sl.bitmap.ptr, 0, (size_t)words * sizeof(uint32_t), s));
         k_genstep_hint<<<(unsigned)((n_gs + 127) / 128), 128, 0, s>>>(P.acc, P.gs, (int)n_gs, sl.gs_hint.ptr);
         P.gs_hint = sl.gs_hint.ptr;
-        launch_simulate(e, P, N, sl.counters.ptr + 2, s);
+        launch_simulate(e, P, N, sl.counters.ptr + 2, s, nullptr, e->cfg.kernel_mode == 3 ? &sl.wf_dev : nullptr);
         CU(cudaGetLastError());
         k_word_prefix<<<(unsigned)nblk, SCAN_WORDS, 0, s>>>(sl.bitmap.ptr, words, sl.word_prefix.ptr, sl.block_sum.ptr);
         k_block_offsets<<<1, 1024, 0, s>>>(sl.block_sum.ptr, nblk, sl.block_offset.ptr, sl.counters.ptr + 1);
@@ -256,8 +261,9 @@ int launch_batch(gbo_server* sv, Slot& sl)
         (rc = sl.block_sum.ensure(nblk)) || (rc = sl.block_offset.ensure(nblk)) || (rc = sl.hits_unordered.ensure(N)) ||
         (rc = sl.hit_gidx.ensure(N)) || (rc = sl.hits.ensure(N)) || (has_input && (rc = sl.input.ensure(N))) ||
         (rc = sl.gs_hint.ensure(n_gs > 0 ? n_gs : 1)) ||
-        (e->cfg.kernel_mode == 2 &&
-         ((rc = sl.gen_photon.ensure(N)) || (rc = sl.gen_rng.ensure(N)) || (rc = sl.gen_hint.ensure(N)))))
+        (e->cfg.kernel_mode >= 2 &&
+         ((rc = sl.gen_photon.ensure(N)) || (rc = sl.gen_rng.ensure(N)) || (rc = sl.gen_hint.ensure(N)))) ||
+        (e->cfg.kernel_mode == 3 && (rc = sl.wf.ensure(N, e->cfg.max_bounce, sl.wf_dev))))
         return rc;
     // input photons go up straight from each event's own copy, one copy per piece at the piece's launch position
     // (outside any graph: the source is pageable host memory)
@@ -411,26 +417,35 @@ void serve_loop(gbo_server* sv)
         // enough photons wait to fill the GPU (min_batch_photon), so that batches do not degenerate to single events.
         // A big event (at least target_batch_photon photons, enough to fill the GPU alone) never starts beside
         // another big one's kernels, where the two would share the SMs and each take twice as long (it may start
-        // while the other's hits download); small events may pass a waiting big one into the free slot.
+        // while the other's hits download), and never joins a batch of small events, whose latency would become its
+        // own; small events may pass a waiting big one into the free slot unless big_exclusive keeps the GPU for
+        // the big one's kernels.
         for (Slot& sl : sv->slots) {
             if (sl.phase != 0) continue;
             int in_flight = 0;
             bool big_in_flight = false;
             for (Slot& x : sv->slots) in_flight += x.phase != 0;
             big_in_flight = big_counter(sv->e->device).load() > 0;
+            if (big_in_flight && sv->cfg.big_exclusive) continue;
             {
                 std::lock_guard<std::mutex> lock(sv->mu);
                 auto admissible = [&](const ServerEvent& ev) {
                     return !big_in_flight || ev.num_photon - ev.next_photon < sv->cfg.target_batch_photon;
                 };
                 if (in_flight > 0) {
+                    // small events wait for company while the GPU is busy, but not longer than max_wait_us: a chain
+                    // of big launches would otherwise hold them until it ends
                     long long waiting = 0;
+                    Clock::time_point oldest = Clock::time_point::max();
                     for (auto& ev : sv->pending) {
                         if (!admissible(*ev)) continue;
                         waiting += ev->num_photon - ev->next_photon;
+                        if (ev->t_submit < oldest) oldest = ev->t_submit;
                         if (waiting >= sv->cfg.min_batch_photon) break;
                     }
-                    if (waiting < sv->cfg.min_batch_photon) continue;
+                    const bool overdue = waiting > 0 && sv->cfg.max_wait_us > 0 &&
+                                         Clock::now() - oldest >= std::chrono::microseconds(sv->cfg.max_wait_us);
+                    if (waiting < sv->cfg.min_batch_photon && !overdue) continue;
                 }
                 long long photons = 0;
                 sl.big = false;
@@ -438,6 +453,7 @@ void serve_loop(gbo_server* sv)
                     std::shared_ptr<ServerEvent> ev = *it;
                     const long long rest = ev->num_photon - ev->next_photon;
                     if (!admissible(*ev)) { ++it; continue; }
+                    if (!sl.pieces.empty() && rest >= sv->cfg.target_batch_photon) { ++it; continue; }
                     if (!sl.pieces.empty() && (photons + rest > sv->max_batch_photon ||
                                                photons >= sv->cfg.target_batch_photon ||
                                                (int)sl.pieces.size() >= sv->cfg.max_batch_events))
@@ -503,6 +519,7 @@ int gbo_server_config_default(gbo_server_config* c)
     c->min_batch_photon = 2ll << 20;
     c->use_graph = 1;
     c->target_batch_photon = 4ll << 20;
+    c->max_wait_us = 1000;
     return GBO_OK;
 }
 
@@ -519,7 +536,8 @@ int gbo_server_create(gbo_engine* e, const gbo_server_config* cfg, gbo_server** 
     auto* sv = new gbo_server();
     sv->e = e;
     sv->cfg = c;
-    const double per_photon = SERVE_BYTES_PER_PHOTON + (e->cfg.kernel_mode == 2 ? SERVE_BYTES_PER_PHOTON_GEN : 0.0);
+    const double per_photon = SERVE_BYTES_PER_PHOTON + (e->cfg.kernel_mode >= 2 ? SERVE_BYTES_PER_PHOTON_GEN : 0.0) +
+                              (e->cfg.kernel_mode == 3 ? SERVE_BYTES_PER_PHOTON_WF : 0.0);
     const long long by_budget = (long long)((double)c.hbm_budget_bytes / (per_photon * c.slots));
     sv->max_batch_photon = c.max_batch_photon > 0 && c.max_batch_photon < by_budget ? c.max_batch_photon : by_budget;
     if (sv->max_batch_photon < 1) { delete sv; return fail(GBO_ERR_CAPACITY, "gbo_server_create: HBM budget below one photon per slot"); }

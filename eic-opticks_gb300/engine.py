@@ -280,7 +280,7 @@ class Engine:
 class ServerConfig(C.Structure):
     _fields_ = [("slots", C.c_int32), ("max_batch_events", C.c_int32), ("max_batch_photon", C.c_int64),
                 ("hbm_budget_bytes", C.c_int64), ("min_batch_photon", C.c_int64), ("use_graph", C.c_int32),
-                ("reserved", C.c_int32), ("target_batch_photon", C.c_int64)]
+                ("big_exclusive", C.c_int32), ("target_batch_photon", C.c_int64), ("max_wait_us", C.c_int64)]
 
 
 class ServerStats(C.Structure):

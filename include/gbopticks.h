@@ -78,8 +78,11 @@ typedef struct gbo_config {
     int64_t  max_photon;            /* capacity limit per event (0: no limit beyond device memory) */
     int32_t  kernel_mode;           /* 0: persistent photon-pool kernel generating its photons, 1: one thread per
                                        photon, 2 (default): photon pool over photons generated up front by a
-                                       separate kernel (84 more device bytes per photon; gbo_simulate_noalloc runs
-                                       its own one-thread kernel) */
+                                       separate kernel (84 more device bytes per photon), 3: wavefront, every step
+                                       of every live photon as three passes (query to the instance-tree walk, the
+                                       queued walks, physics) over photons generated up front (128 more device bytes
+                                       per photon; binary32 only, the precision mode runs mode 2).
+                                       gbo_simulate_noalloc runs its own one-thread kernel */
     int32_t  refill_min;            /* pool kernel: idle lanes a warp waits for before refilling (1..32, 4) */
     int32_t  blocks_per_sm;         /* pool kernel: resident blocks per SM (0: occupancy maximum) */
     int32_t  refill_period;         /* pool kernel: steps between refill checks (compaction period, >= 1) */
@@ -201,9 +204,13 @@ typedef struct gbo_server_config {
     int64_t min_batch_photon;       /* while a launch is in flight, start another only once this many photons wait (2M) */
     int32_t use_graph;              /* 1: each batch's copies and kernels go out as one CUDA graph, captured from the
                                        stream and applied to the slot's executable graph by update (1) */
-    int32_t reserved;
+    int32_t big_exclusive;          /* 1: while a big batch's kernels run (an event of at least target_batch_photon),
+                                       no other batch starts, so the big event keeps the whole GPU; 0: small batches
+                                       may start beside it once min_batch_photon photons wait */
     int64_t target_batch_photon;    /* a batch stops taking events once it holds this many photons (4M): enough to
                                        fill the GPU, small enough that small events do not wait on a long launch */
+    int64_t max_wait_us;            /* while a launch is in flight, waiting events start anyway once the oldest has
+                                       waited this long, even below min_batch_photon (1000 us; 0: no limit) */
 } gbo_server_config;
 typedef struct gbo_server_stats {
     int64_t events_submitted, events_done, batches, photons, max_batch_photon;

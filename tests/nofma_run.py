@@ -20,9 +20,9 @@ _spec = importlib.util.spec_from_file_location("make_device_golden",
 mdg = importlib.util.module_from_spec(_spec)
 _spec.loader.exec_module(mdg)
 
-# (kernel mode, Philox blocks by call): the three kernel modes, and the two main ones with Philox by call (a
-# separate kernel form for geometries without CSG trees)
-FORMS = ((2, 0), (1, 0), (0, 0), (2, 1), (1, 1))
+# (kernel mode, Philox blocks by call): the four kernel modes, and three of them with Philox by call (a separate
+# kernel form for geometries without CSG trees)
+FORMS = ((2, 0), (1, 0), (0, 0), (3, 0), (2, 1), (1, 1), (3, 1))
 
 
 def form_key(mode, rng_call):

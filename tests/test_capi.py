@@ -77,7 +77,8 @@ def test_ctypes_mirrors_match_the_header(tmp_path):
     import subprocess
     from eic_opticks_gb300 import engine as E
     pairs = [("gbo_config", E.Config), ("gbo_tune_result", E.TuneResult), ("gbo_stats", E.Stats),
-             ("gbo_geometry_desc", E.GeometryDesc)]
+             ("gbo_geometry_desc", E.GeometryDesc), ("gbo_server_config", E.ServerConfig),
+             ("gbo_server_stats", E.ServerStats)]
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbopticks.h"', "int main(void) {"]
     for cname, py in pairs:
         lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))

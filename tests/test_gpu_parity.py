@@ -210,9 +210,9 @@ def nofma_digests(E, tmp_path_factory):
 def test_arithmetic_bit_exact_with_reference_device(nofma_digests, name):
     """The strict gate: without multiply-add contraction on either side, the engine's photons (record and flag
     history) equal the reference's bit for bit, in every kernel form (pool over pregenerated photons, one thread
-    per photon, pool generating its photons; Philox inlined or by call)."""
+    per photon, pool generating its photons, wavefront; Philox inlined or by call)."""
     want = _device_golden(name, "nofma")["digest"]
-    for form in ("mode2", "mode1", "mode0", "mode2_call", "mode1_call"):
+    for form in ("mode2", "mode1", "mode0", "mode3", "mode2_call", "mode1_call", "mode3_call"):
         got = nofma_digests["%s_%s" % (name, form)]
         assert len(got) == len(want)
         exact = float((got == want).mean()) if len(want) else 1.0

@@ -30,7 +30,8 @@ def make_events(rng, n, geom_kind, wc=None):
     return events
 
 
-@pytest.mark.parametrize("kind,use_graph,mode", [("crystal", 1, 0), ("water", 1, 0), ("crystal", 0, 0), ("crystal", 1, 2)])
+@pytest.mark.parametrize("kind,use_graph,mode", [("crystal", 1, 0), ("water", 1, 0), ("crystal", 0, 0), ("crystal", 1, 2),
+                                                 ("crystal", 1, 3), ("water", 0, 3)])
 def test_served_events_equal_alone(E, kind, use_graph, mode):
     from eic_opticks_gb300 import geometry as G
     geom = G.crystal_array() if kind == "crystal" else G.water_cube()
