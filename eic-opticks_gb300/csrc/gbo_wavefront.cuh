@@ -27,6 +27,17 @@
 
 namespace gbo {
 
+// Register budgets of the passes, measured on the 100M-photon, 20,000-sensor event: 128 for the query passes (4 blocks
+// of 128 per SM, a few spills) beat 168 without spills by 10 %; 80 for the physics pass (6 blocks per SM) beat
+// ptxas' own choice (72, 20 B of spills) by 2 %.  A persistent walk pass (lanes whose walk ended taking the next
+// queued query, one traversal round at a time) ran 17-23 % slower than these one-query-per-lane passes.
+#ifndef GBO_WF_TRACE_BOUNDS
+#define GBO_WF_TRACE_BOUNDS __maxnreg__(128)
+#endif
+#ifndef GBO_WF_STEP_BOUNDS
+#define GBO_WF_STEP_BOUNDS __maxnreg__(80)
+#endif
+
 GBO_DEV void wf_store_hit(float4* q, const Hit& h)
 {
     __stcg(q, make_float4(h.normal.x, h.normal.y, h.normal.z, h.t));
@@ -83,7 +94,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_wf_start(const __grid_constant__ 
 
 // The query of each photon of step s up to the instance-tree walk (WALK false), or the queued queries in full.
 template <int TREE, bool WALK>
-__global__ void __launch_bounds__(SIM_BLOCK) k_wf_trace(const __grid_constant__ Params P, Wavefront W, int s)
+__global__ void GBO_WF_TRACE_BOUNDS k_wf_trace(const __grid_constant__ Params P, Wavefront W, int s)
 {
     const unsigned lane = threadIdx.x & 31u;
     const long long n = (long long)W.count[2 * s + (WALK ? 1 : 0)];
@@ -114,7 +125,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_wf_trace(const __grid_constant__ 
 
 // The physics of step s: bounce s + 1 of every photon of the step's list.
 template <int TREE, bool RCALL>
-__global__ void __launch_bounds__(SIM_BLOCK) k_wf_step(const __grid_constant__ Params P, Wavefront W, int s)
+__global__ void GBO_WF_STEP_BOUNDS k_wf_step(const __grid_constant__ Params P, Wavefront W, int s)
 {
     const unsigned lane = threadIdx.x & 31u;
     const long long n = (long long)W.count[2 * s];

@@ -89,21 +89,42 @@ def test_event_above_photon_limit_is_refused(E):
 
 @pytest.mark.parametrize("n_photon", [1, 31, 33, 1000, 4097])
 def test_pregenerated_pool_small_events_equal_one_thread(E, n_photon):
-    """The pregenerated photon pool hands photons out in warp chunks of 32: events smaller than one chunk, than the
-    grid, and with ragged last chunks give the same photons and hits as the one-thread-per-photon kernel."""
+    """The pregenerated photon pool hands photons out in warp chunks of 32, the wavefront appends them to its step
+    lists a warp at a time: events smaller than one chunk, than the grid, and with ragged last chunks give the same
+    photons and hits as the one-thread-per-photon kernel."""
     from eic_opticks_gb300 import geometry as G, gensteps as GS
     arrays = G.crystal_array().arrays()
     gs = GS.crystal_scint_gensteps(1, n_photon, seed=n_photon, poisson=False)
     out = []
-    for mode in (1, 2):
+    for mode in (1, 2, 3):
         eng = E.Engine(arrays, record_photon=1, record_seq=1, kernel_mode=mode, refill_min=1)
         eng.simulate(5, gs)
         out.append((eng.photons(), eng.seq(), eng.hits()))
         eng.close()
-    (p1, s1, h1), (p2, s2, h2) = out
-    assert len(p1) == len(p2) == n_photon
-    assert np.array_equal(s1.view(np.uint64), s2.view(np.uint64))
-    assert np.array_equal(p1["index"], p2["index"]) and np.array_equal(h1["index"], h2["index"])
+    p1, s1, h1 = out[0]
+    for p2, s2, h2 in out[1:]:
+        assert len(p1) == len(p2) == n_photon
+        assert np.array_equal(s1.view(np.uint64), s2.view(np.uint64))
+        assert np.array_equal(p1["index"], p2["index"]) and np.array_equal(h1["index"], h2["index"])
+
+
+@pytest.mark.parametrize("max_bounce", [0, 1, 2, 5])
+def test_wavefront_bounce_limit(E, max_bounce):
+    """The wavefront runs max_bounce steps; photons still alive after the last one end there, as the bounce loop of
+    the other forms ends them: same flag histories, photons and hits for every limit, including none."""
+    from eic_opticks_gb300 import geometry as G, gensteps as GS
+    arrays = G.crystal_array().arrays()
+    gs = GS.crystal_scint_gensteps(4, 500, seed=3, poisson=False)
+    out = []
+    for mode in (1, 3):
+        eng = E.Engine(arrays, record_photon=1, record_seq=1, kernel_mode=mode, max_bounce=max_bounce)
+        eng.simulate(2, gs)
+        out.append((eng.photons(), eng.seq(), eng.hits()))
+        eng.close()
+    (p1, s1, h1), (p3, s3, h3) = out
+    assert np.array_equal(s1.view(np.uint64), s3.view(np.uint64))
+    assert np.array_equal(p1["flagmask"], p3["flagmask"]) and np.array_equal(h1["index"], h3["index"])
+    assert np.allclose(p1["pos"], p3["pos"], atol=1e-3)
 
 
 def test_genstep_hint_outside_every_instance(E):
