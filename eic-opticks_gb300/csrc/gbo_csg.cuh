@@ -431,8 +431,12 @@ GBO_COLD bool leaf_phicut(float4& is, float4 q0, float t_min, float3 o, float3 d
 
 // csg_intersect_leaf.h:174-325
 // rd_inv (optional): the correctly rounded reciprocals of rd's components, reused by an untransformed box3
+// whole_prim: the leaf is a prim by itself, whose hit OptiX accepts only inside the ray's [tmin, tmax] interval.  Of
+// the leaves only a convex polyhedron reports a valid hit below t_min (t = 0 when both its planes lie at or below
+// t_min: csg_intersect_leaf_convexpolyhedron.h:87-104 writes no t), so the check sits on its out-of-line path.
 GBO_DEV bool intersect_leaf(float4& is, const gbo_csgnode* node, const float4* plan, const gbo_qat4* itra,
-                            float t_min, float3 ro, float3 rd, bool polish = false, const float3* rd_inv = nullptr)
+                            float t_min, float3 ro, float3 rd, bool polish = false, const float3* rd_inv = nullptr,
+                            bool whole_prim = false)
 {
     is = make_float4(0.f, 0.f, 0.f, 0.f);
     const NodeView nd = load_node(node);
@@ -458,7 +462,11 @@ GBO_DEV bool intersect_leaf(float4& is, const gbo_csgnode* node, const float4* p
         // the out-of-line leaves write a copy: `is` itself never has its address taken, so it stays in registers
         // on the other paths
         case GBO_CSG_CONE:             { float4 c = is; valid = leaf_cone(c, nd.q0, t_min, origin, direction); is = c; } break;
-        case GBO_CSG_CONVEXPOLYHEDRON: { float4 c = is; valid = leaf_convexpolyhedron(c, nd.q0, plan, t_min, origin, direction); is = c; } break;
+        case GBO_CSG_CONVEXPOLYHEDRON: {
+            float4 c = is;
+            valid = leaf_convexpolyhedron(c, nd.q0, plan, t_min, origin, direction) && (!whole_prim || c.w >= t_min);
+            is = c;
+        } break;
         case GBO_CSG_HYPERBOLOID:      { float4 c = is; valid = leaf_hyperboloid(c, nd.q0, t_min, origin, direction); is = c; } break;
         case GBO_CSG_PHICUT:           { float4 c = is; valid = leaf_phicut(c, nd.q0, t_min, origin, direction); is = c; } break;
         case GBO_CSG_HALFSPACE:        { float4 c = is; valid = leaf_halfspace(c, nd.q0, t_min, origin, direction); is = c; } break;

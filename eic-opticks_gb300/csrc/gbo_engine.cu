@@ -1061,7 +1061,8 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
     for (int r : {1, 2, 4, 8, 16, 32})
         for (int p : {1, 4}) cands.push_back({0, r, p, 0, 1, 0});
     for (int r : {1, 2, 4, 8, 16}) cands.push_back({2, r, 1, 0, 1, 0});
-    for (int w : {16, 24, 32}) cands.push_back({2, 4, 1, 0, w, 0});
+    if (e->csg_form >= 1)                                                    // gathered walks: CSG-tree forms
+        for (int w : {16, 24, 32}) cands.push_back({2, 4, 1, 0, w, 0});
     if (e->csg_form == 0 && !e->cfg.precision)
         for (const Cand& c : std::vector<Cand>{{1, 32, 1, 0, 1, 1}, {0, 4, 1, 0, 1, 1}, {0, 4, 4, 0, 1, 1},
                                                {2, 1, 1, 0, 1, 1}, {2, 4, 1, 0, 1, 1}})

@@ -307,10 +307,15 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
             if (!pool_open) break;
             continue;
         }
-        // gathered TLAS walks: parked lanes walk once enough of them wait, or when no live lane is left to step
-        const unsigned parked_mask = __ballot_sync(0xffffffffu, parked);
-        const bool walk_now = parked_mask != 0u &&
-                              (__popc(parked_mask) >= P.walk_min || parked_mask == __ballot_sync(0xffffffffu, live));
+        // gathered TLAS walks (CSG-tree forms): parked lanes walk once enough of them wait, or when no live lane is
+        // left to step.  The single-leaf forms compile none of it: their walks are short, and the two ballots per
+        // step cost 2 % on the crystal event.
+        bool walk_now = false;
+        if constexpr (TREE >= 1) {
+            const unsigned parked_mask = __ballot_sync(0xffffffffu, parked);
+            walk_now = parked_mask != 0u &&
+                       (__popc(parked_mask) >= P.walk_min || parked_mask == __ballot_sync(0xffffffffu, live));
+        }
         bool done = false;
         if (live) {
             if (parked || (bounce < P.max_bounce && p.time < P.max_time)) {
@@ -321,7 +326,8 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
                 trace_begin(b, P.tmax);
                 int r = TRACE_WALK;
                 if (!parked || walk_now)
-                    r = trace_items<TREE, PRECISE>(P.acc, p.pos, p.mom, tmin, hint, !parked && P.walk_min > 1, b);
+                    r = trace_items<TREE, PRECISE>(P.acc, p.pos, p.mom, tmin, hint,
+                                                   TREE >= 1 && !parked && P.walk_min > 1, b);
                 parked = r == TRACE_WALK;
                 if (!parked) {
                     Hit h;

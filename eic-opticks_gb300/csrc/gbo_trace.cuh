@@ -131,7 +131,8 @@ GBO_DEV bool prim_hit(float4& is, const Accel& a, int node_word, float t_min, fl
         }
         return intersect_prim<(TREE >= 2)>(is, root, a.plan, a.itra, t_min, o, d, POLISH);
     }
-    if (node_typecode(root) >= GBO_CSG_LEAF) return intersect_leaf(is, root, a.plan, a.itra, t_min, o, d, POLISH, d_inv);
+    if (node_typecode(root) >= GBO_CSG_LEAF)
+        return intersect_leaf(is, root, a.plan, a.itra, t_min, o, d, POLISH, d_inv, true);
     is = make_float4(0.f, 0.f, 0.f, 0.f);
     return false;
 }
@@ -167,8 +168,8 @@ GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float
         if (!prim_hit<TREE, POLISH>(is, a, __float_as_int(pb0.w), tmin, po, pd, POLISH ? nullptr : &oinv)) continue;
         // OptiX accepts a reported hit only inside the ray's [tmin, tmax] interval: a convex polyhedron behind the
         // ray reports a valid t of 0 (csg_intersect_leaf_convexpolyhedron.h:87-104 writes no t when both planes
-        // lie at or below t_min)
-        if (!(is.w >= tmin)) continue;
+        // lie at or below t_min), also inside a tree or list (single-leaf prims check it in intersect_leaf)
+        if (TREE && !(is.w >= tmin)) continue;
         const unsigned key = ((unsigned)ii << 16) | (unsigned)k2;
         if (is.w < b.t || (is.w == b.t && b.key != 0xffffffffu && key < b.key)) {
             b.t = is.w; b.key = key; b.is = is; b.inst = ii; b.pb = __float_as_uint(pb1.w);

@@ -90,9 +90,9 @@ typedef struct gbo_config {
     int32_t  precision;             /* 0: binary32 as the reference (default); 1: binary64 Newton polish of every
                                        accepted sphere / zsphere / cylinder root and binary64 position/time
                                        accumulators */
-    int32_t  walk_min;              /* pool kernels: a lane whose step needs a walk of the instance tree parks until
-                                       this many lanes of its warp need one (or no other lane can step), so the walks
-                                       run together; 1: no parking (1) */
+    int32_t  walk_min;              /* pool kernels of geometries with CSG trees: a lane whose step needs a walk of
+                                       the instance tree parks until this many lanes of its warp need one (or no other
+                                       lane can step), so the walks run together; 1: no parking (1) */
     int32_t  rng_call;              /* kernels of geometries without CSG trees, binary32: 0 (default) inlines the
                                        Philox rounds at every draw site, 1 computes each block of four draws by an
                                        out-of-line call (smaller code; the CSG-tree kernels always do).  Same numbers
