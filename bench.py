@@ -37,15 +37,20 @@ METRIC = "propagated photons/s, batched vs plain per-event launch on 1 GB300; p9
 UNIT = "photons/s"
 WORKLOAD = "crystal_array_8x8_CsI_scint_2000gs_poisson5000"
 L2_FLUSH_BYTES = 256 << 20
-# ncu DRAM bytes (read + write) per photon of the simulate kernels on the crystal event, scaled to the benchmark
-# event by its photon count (all of it grows with the photons): one thread per photon (k_simulate, 1M-photon event:
-# gensteps in, hits and hit bitmap out), and the pregenerated pool (k_generate + k_simulate_pool, 2.5M-photon event:
-# 0.22 + 182.10 MB and 210.98 + 2.46 MB, larger than L2)
+# ncu DRAM bytes (read + write) per photon of the simulate kernels, scaled to the benchmark event by its photon count
+# (all of it grows with the photons), each with the build it was captured on: one thread per photon on the crystal
+# event (k_simulate, 1M photons: gensteps in, hits and hit bitmap out), the pregenerated pool on the crystal event
+# (k_generate + k_simulate_pool, 2.5M photons: 0.21 + 182.05 MB and 210.78 + 2.20 MB, larger than L2) and the
+# wavefront on the 20,000-sensor sphere (k_generate + k_wf_start + 31 x 3 passes, 5M photons: 8655 MB)
 TRAFFIC_B_PER_PHOTON = {("crystal_array", 1): (443392.0 + 840192.0) / 998319,
-                        ("crystal_array", 2): (0.22e6 + 182.10e6 + 210.98e6 + 2.46e6) / 2499792}
-TRAFFIC_SOURCE = {("crystal_array", 1): "ncu DRAM bytes of k_simulate on a 1M-photon crystal event, scaled by photons",
+                        ("crystal_array", 2): (0.21e6 + 182.05e6 + 210.78e6 + 2.20e6) / 2499792,
+                        ("large_sphere", 3): 8654.99e6 / 5000000}
+TRAFFIC_SOURCE = {("crystal_array", 1): "ncu DRAM bytes of k_simulate on a 1M-photon crystal event (an earlier "
+                                        "build of that kernel), scaled by photons",
                   ("crystal_array", 2): "ncu DRAM bytes of k_generate + k_simulate_pool on a 2.5M-photon crystal "
-                                        "event, scaled by photons"}
+                                        "event (commit a69d80e), scaled by photons",
+                  ("large_sphere", 3): "ncu DRAM bytes of k_generate + the wavefront passes on a 5M-photon event of "
+                                       "the 20,000-sensor sphere (commit a69d80e), scaled by photons"}
 
 
 def pinned_photons(n):
