@@ -300,18 +300,23 @@ struct WavefrontBufs {
     DBuf<float4> hit;
     DBuf<int> list;
     DBuf<unsigned long long> count;
-    void release() { hit.release(); list.release(); count.release(); }
+    DBuf<unsigned> bins;
+    void release() { hit.release(); list.release(); count.release(); bins.release(); }
     int ensure(long long n, int max_bounce, Wavefront& w)
     {
         int rc;
-        if ((rc = hit.ensure(2 * (size_t)n)) || (rc = list.ensure(3 * (size_t)n)) ||
-            (rc = count.ensure(2 * (size_t)(max_bounce + 1))))
+        if ((rc = hit.ensure(2 * (size_t)n)) || (rc = list.ensure(5 * (size_t)n)) ||
+            (rc = count.ensure(2 * (size_t)(max_bounce + 1))) ||
+            (rc = bins.ensure((size_t)(max_bounce > 0 ? max_bounce : 1) * WF_CELLS)))
             return rc;
         w.hit = hit.ptr;
         w.list[0] = list.ptr;
         w.list[1] = list.ptr + n;
         w.walk = list.ptr + 2 * n;
+        w.walk_key = list.ptr + 3 * n;
+        w.walk_sorted = list.ptr + 4 * n;
         w.count = count.ptr;
+        w.bins = bins.ptr;
         return 0;
     }
 };
@@ -407,10 +412,10 @@ struct gbo_engine {
 };
 
 // Simulation kernels one launch_simulate issues over n photons (the generation kernel counted by the caller): one,
-// or in kernel mode 3 the wavefront's start pass and three passes per step.
+// or in kernel mode 3 the wavefront's start pass and six kernels per step (three passes, the walk queue's sort).
 static int simulate_kernels(const gbo_engine* e, long long n)
 {
-    if (e->cfg.kernel_mode == 3 && !e->cfg.precision && n < 0x7fffffffll) return 1 + 3 * e->cfg.max_bounce;
+    if (e->cfg.kernel_mode == 3 && !e->cfg.precision && n < 0x7fffffffll) return 1 + 6 * e->cfg.max_bounce;
     return 1;
 }
 

@@ -132,10 +132,10 @@ constexpr size_t SERVE_DIRECT_HIT_BYTES = 64ull << 20;
 
 // device bytes per photon slot of a batch: bitmap + prefix bits, unordered + ordered hit capacity, hit index;
 // kernel modes 2 and 3 add the pregenerated photon, its random-stream place and start instance; kernel mode 3 adds
-// the hit record and three list entries
+// the hit record and five list entries (two step lists, the walk queue, its keys, the sorted queue)
 constexpr double SERVE_BYTES_PER_PHOTON = 0.25 + 64.0 + 64.0 + 8.0;
 constexpr double SERVE_BYTES_PER_PHOTON_GEN = 64.0 + 16.0 + 4.0;
-constexpr double SERVE_BYTES_PER_PHOTON_WF = 32.0 + 12.0;
+constexpr double SERVE_BYTES_PER_PHOTON_WF = 32.0 + 20.0;
 
 }  // namespace
 

@@ -409,10 +409,18 @@ __global__ void k_trace_rays(Accel acc, const float3* pos, const float3* dir, in
 // ---- per-form host launchers (defined in gbo_sim_forms.inl, one translation unit per TREE value) ---------------
 
 // the wavefront form's device state (gbo_wavefront.cuh), besides the pregenerated-photon buffers
+// the walk queue's sort grid (gbo_wavefront.cuh): 32 x 32 x 32 cells over the TLAS root box
+constexpr int WF_CELL_BITS = 5;
+constexpr int WF_CELLS = 1 << (3 * WF_CELL_BITS);
+constexpr long long WF_SORT_MIN = 65536;        // walk queues shorter than this are walked unsorted
+
 struct Wavefront {
     float4* hit;                    // 2 per photon: (normal, t), (lposz, iindex_identity, prim_boundary, 0)
     int* list[2];                   // live photons of even / odd steps
     int* walk;                      // photons of the current step whose query walks the instance tree
+    int* walk_key;                  // their cells (the walk queue's sort key), at the same positions
+    int* walk_sorted;               // the walk queue ordered by cell
+    unsigned* bins;                 // per step, WF_CELLS cell counts turned into offsets (max_bounce x WF_CELLS)
     unsigned long long* count;      // [2 s]: photons alive at step s; [2 s + 1]: of them queued for a walk;
                                     // 2 (max_bounce + 1) counters, zeroed by the launch
 };

@@ -48,6 +48,7 @@ static void wavefront_launch(const Params& P, const SimLaunch& L)
 {
     const Wavefront& W = L.wf;
     cudaMemsetAsync(W.count, 0, 2 * (size_t)(P.max_bounce + 1) * sizeof(unsigned long long), L.stream);
+    cudaMemsetAsync(W.bins, 0, (size_t)P.max_bounce * WF_CELLS * sizeof(unsigned), L.stream);
     const long long full = (L.n + SIM_BLOCK - 1) / SIM_BLOCK;
     auto grid = [&](int occ) {
         const long long g = (long long)L.sms * occ;
@@ -57,8 +58,12 @@ static void wavefront_launch(const Params& P, const SimLaunch& L)
     const unsigned g_near = grid(resident_blocks<k_wf_trace<TREE, false>>());
     const unsigned g_walk = grid(resident_blocks<k_wf_trace<TREE, true>>());
     const unsigned g_step = grid(resident_blocks<k_wf_step<TREE, RCALL>>());
+    const unsigned g_cells = (unsigned)L.sms * 8u;
     for (int s = 0; s < P.max_bounce; s++) {
         k_wf_trace<TREE, false><<<g_near, SIM_BLOCK, 0, L.stream>>>(P, W, s);
+        k_wf_cells_count<TREE><<<g_cells, SIM_BLOCK, 0, L.stream>>>(W, s);
+        k_wf_cells_scan<TREE><<<1, WF_SCAN_THREADS, 0, L.stream>>>(W, s);
+        k_wf_cells_scatter<TREE><<<g_cells, SIM_BLOCK, 0, L.stream>>>(W, s);
         k_wf_trace<TREE, true><<<g_walk, SIM_BLOCK, 0, L.stream>>>(P, W, s);
         k_wf_step<TREE, RCALL><<<g_step, SIM_BLOCK, 0, L.stream>>>(P, W, s);
     }

@@ -80,7 +80,7 @@ typedef struct gbo_config {
                                        photon, 2 (default): photon pool over photons generated up front by a
                                        separate kernel (84 more device bytes per photon), 3: wavefront, every step
                                        of every live photon as three passes (query to the instance-tree walk, the
-                                       queued walks, physics) over photons generated up front (128 more device bytes
+                                       queued walks, physics) over photons generated up front (136 more device bytes
                                        per photon; binary32 only, the precision mode runs mode 2).
                                        gbo_simulate_noalloc runs its own one-thread kernel */
     int32_t  refill_min;            /* pool kernel: idle lanes a warp waits for before refilling (1..32, 4) */
