@@ -41,16 +41,17 @@ L2_FLUSH_BYTES = 256 << 20
 # (all of it grows with the photons), each with the build it was captured on: one thread per photon on the crystal
 # event (k_simulate, 1M photons: gensteps in, hits and hit bitmap out), the pregenerated pool on the crystal event
 # (k_generate + k_simulate_pool, 2.5M photons: 0.21 + 182.05 MB and 210.78 + 2.20 MB, larger than L2) and the
-# wavefront on the 20,000-sensor sphere (k_generate + k_wf_start + 31 x 3 passes, 5M photons: 8655 MB)
+# wavefront on the 20,000-sensor sphere (k_generate + k_wf_start + 31 x (3 passes + the walk-queue sort), 5M
+# photons: 8877 MB)
 TRAFFIC_B_PER_PHOTON = {("crystal_array", 1): (443392.0 + 840192.0) / 998319,
                         ("crystal_array", 2): (0.21e6 + 182.05e6 + 210.78e6 + 2.20e6) / 2499792,
-                        ("large_sphere", 3): 8654.99e6 / 5000000}
+                        ("large_sphere", 3): 8877.07e6 / 5000000}
 TRAFFIC_SOURCE = {("crystal_array", 1): "ncu DRAM bytes of k_simulate on a 1M-photon crystal event (an earlier "
                                         "build of that kernel), scaled by photons",
                   ("crystal_array", 2): "ncu DRAM bytes of k_generate + k_simulate_pool on a 2.5M-photon crystal "
                                         "event (commit a69d80e), scaled by photons",
                   ("large_sphere", 3): "ncu DRAM bytes of k_generate + the wavefront passes on a 5M-photon event of "
-                                       "the 20,000-sensor sphere (commit a69d80e), scaled by photons"}
+                                       "the 20,000-sensor sphere (commit db3b43a), scaled by photons"}
 
 
 def pinned_photons(n):
@@ -517,7 +518,7 @@ def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=N
 
     # ---- end to end through the C ABI with host buffers (e2e) ----
     hits_host = None
-    e2e_ms = []
+    e2e_ms, e2e_sim_ms, e2e_hits_ms = [], [], []
     h2d = gs.nbytes + (inp.nbytes if inp is not None else 0)
     nh = 0
     for k in range(warmup + steps):
@@ -525,12 +526,16 @@ def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=N
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         nh = eng.simulate(2000 + k, gs, inp)
+        t1 = time.perf_counter()
         if hits_host is None or len(hits_host) < nh:
             hits_host = pinned_photons(max(nh, 1) * 2)
+        t2 = time.perf_counter()
         eng.hits(out=hits_host[:nh])
-        dt = time.perf_counter() - t0
-        if k >= warmup:
-            e2e_ms.append(dt * 1e3)
+        t3 = time.perf_counter()
+        if k >= warmup:             # the timed step: the call, then the hit download (a first-step buffer
+            e2e_ms.append((t1 - t0 + t3 - t2) * 1e3)        # allocation between them is setup, not timed)
+            e2e_sim_ms.append((t1 - t0) * 1e3)
+            e2e_hits_ms.append((t3 - t2) * 1e3)
     d2h = nh * 64 + 32      # ordered hits + the counters read that sizes them
     e2e_total = sum(e2e_ms)
     if dist:
@@ -554,7 +559,8 @@ def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=N
                               "walk_min": tune.get("walk_min", 1), "rng_call": tune.get("rng_call", 0),
                               "chosen_by": "--form" if form else "autotuner on 10% sample"},
                    "max_bounce": 31},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "simulate_ms": float(np.mean(e2e_sim_ms)), "hit_download_ms": float(np.mean(e2e_hits_ms))},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": (TRAFFIC_B_PER_PHOTON[traffic_key] * n_photon

@@ -301,14 +301,17 @@ struct WavefrontBufs {
     DBuf<int> list;
     DBuf<unsigned long long> count;
     DBuf<unsigned> bins;
-    void release() { hit.release(); list.release(); count.release(); bins.release(); }
-    int ensure(long long n, int max_bounce, Wavefront& w)
+    DBuf<Acc64> acc;
+    void release() { hit.release(); list.release(); count.release(); bins.release(); acc.release(); }
+    int ensure(long long n, int max_bounce, bool precise, Wavefront& w)
     {
         int rc;
         if ((rc = hit.ensure(2 * (size_t)n)) || (rc = list.ensure(5 * (size_t)n)) ||
             (rc = count.ensure(2 * (size_t)(max_bounce + 1))) ||
-            (rc = bins.ensure((size_t)(max_bounce > 0 ? max_bounce : 1) * WF_CELLS)))
+            (rc = bins.ensure((size_t)(max_bounce > 0 ? max_bounce : 1) * WF_CELLS)) ||
+            (precise && (rc = acc.ensure((size_t)n))))
             return rc;
+        w.acc = precise ? acc.ptr : nullptr;
         w.hit = hit.ptr;
         w.list[0] = list.ptr;
         w.list[1] = list.ptr + n;
@@ -415,7 +418,7 @@ struct gbo_engine {
 // or in kernel mode 3 the wavefront's start pass and six kernels per step (three passes, the walk queue's sort).
 static int simulate_kernels(const gbo_engine* e, long long n)
 {
-    if (e->cfg.kernel_mode == 3 && !e->cfg.precision && n < 0x7fffffffll) return 1 + 6 * e->cfg.max_bounce;
+    if (e->cfg.kernel_mode == 3 && n < 0x7fffffffll) return 1 + 6 * e->cfg.max_bounce;
     return 1;
 }
 
@@ -754,7 +757,8 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
         if ((rc = e->gen_hint.ensure(num_photon))) return rc;
     }
     Wavefront wf{};
-    if (e->cfg.kernel_mode == 3 && (rc = e->wf.ensure(num_photon, e->cfg.max_bounce, wf))) return rc;
+    if (e->cfg.kernel_mode == 3 && (rc = e->wf.ensure(num_photon, e->cfg.max_bounce, e->cfg.precision != 0, wf)))
+        return rc;
     if (num_gs > 0 && (rc = e->gs_hint.ensure(num_gs))) return rc;
 
     Params P = make_params(e);
@@ -1072,10 +1076,8 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         for (const Cand& c : std::vector<Cand>{{1, 32, 1, 0, 1, 1}, {0, 4, 1, 0, 1, 1}, {0, 4, 4, 0, 1, 1},
                                                {2, 1, 1, 0, 1, 1}, {2, 4, 1, 0, 1, 1}})
             cands.push_back(c);
-    if (!e->cfg.precision) {                                                 // the wavefront form
-        cands.push_back({3, 4, 1, 0, 1, 0});
-        if (e->csg_form == 0) cands.push_back({3, 4, 1, 0, 1, 1});
-    }
+    cands.push_back({3, 4, 1, 0, 1, 0});                                     // the wavefront form
+    if (e->csg_form == 0 && !e->cfg.precision) cands.push_back({3, 4, 1, 0, 1, 1});
     const int form = 2 * e->csg_form + (e->cfg.precision ? 1 : 0);
     for (int b = 1; b < e->pool_occ[form] && cands.size() < 32; b++) {       // fewer resident blocks than fit
         cands.push_back({2, 4, 1, b, 1, 0});

@@ -263,7 +263,7 @@ int launch_batch(gbo_server* sv, Slot& sl)
         (rc = sl.gs_hint.ensure(n_gs > 0 ? n_gs : 1)) ||
         (e->cfg.kernel_mode >= 2 &&
          ((rc = sl.gen_photon.ensure(N)) || (rc = sl.gen_rng.ensure(N)) || (rc = sl.gen_hint.ensure(N)))) ||
-        (e->cfg.kernel_mode == 3 && (rc = sl.wf.ensure(N, e->cfg.max_bounce, sl.wf_dev))))
+        (e->cfg.kernel_mode == 3 && (rc = sl.wf.ensure(N, e->cfg.max_bounce, e->cfg.precision != 0, sl.wf_dev))))
         return rc;
     // input photons go up straight from each event's own copy, one copy per piece at the piece's launch position
     // (outside any graph: the source is pageable host memory)
@@ -537,7 +537,8 @@ int gbo_server_create(gbo_engine* e, const gbo_server_config* cfg, gbo_server** 
     sv->e = e;
     sv->cfg = c;
     const double per_photon = SERVE_BYTES_PER_PHOTON + (e->cfg.kernel_mode >= 2 ? SERVE_BYTES_PER_PHOTON_GEN : 0.0) +
-                              (e->cfg.kernel_mode == 3 ? SERVE_BYTES_PER_PHOTON_WF : 0.0);
+                              (e->cfg.kernel_mode == 3 ? SERVE_BYTES_PER_PHOTON_WF : 0.0) +
+                              (e->cfg.kernel_mode == 3 && e->cfg.precision ? (double)sizeof(Acc64) : 0.0);
     const long long by_budget = (long long)((double)c.hbm_budget_bytes / (per_photon * c.slots));
     sv->max_batch_photon = c.max_batch_photon > 0 && c.max_batch_photon < by_budget ? c.max_batch_photon : by_budget;
     if (sv->max_batch_photon < 1) { delete sv; return fail(GBO_ERR_CAPACITY, "gbo_server_create: HBM budget below one photon per slot"); }

@@ -421,6 +421,7 @@ struct Wavefront {
     int* walk_key;                  // their cells (the walk queue's sort key), at the same positions
     int* walk_sorted;               // the walk queue ordered by cell
     unsigned* bins;                 // per step, WF_CELLS cell counts turned into offsets (max_bounce x WF_CELLS)
+    Acc64* acc;                     // precision mode: each photon's binary64 position / time accumulators
     unsigned long long* count;      // [2 s]: photons alive at step s; [2 s + 1]: of them queued for a walk;
                                     // 2 (max_bounce + 1) counters, zeroed by the launch
 };
@@ -430,8 +431,7 @@ struct SimLaunch {
     unsigned long long* pool;       // photon-pool counter, zeroed by the caller
     cudaStream_t stream;
     int kernel_mode;                // 0: pool generating its photons, 1: one thread per photon, 2: pool over
-                                    // pregenerated photons (P.gen_photon set), 3: wavefront (P.gen_photon set;
-                                    // binary32 only, the precision mode runs mode 2)
+                                    // pregenerated photons (P.gen_photon set), 3: wavefront (P.gen_photon set)
     bool precise;                   // precision-mode kernels
     bool rng_call;                  // single-leaf binary32 kernels: Philox blocks by call (the CSG-tree forms
                                     // always call)

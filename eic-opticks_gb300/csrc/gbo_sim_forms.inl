@@ -43,7 +43,7 @@ static int resident_blocks()
 // Kernel mode 3: the start pass, then max_bounce steps of three passes each, all on the launch's stream (the
 // passes of a step read their list's length on the device, so the host never waits between them; steps whose list
 // is empty return at once).
-template <int TREE, bool RCALL>
+template <int TREE, bool RCALL, bool PRECISE>
 static void wavefront_launch(const Params& P, const SimLaunch& L)
 {
     const Wavefront& W = L.wf;
@@ -54,18 +54,18 @@ static void wavefront_launch(const Params& P, const SimLaunch& L)
         const long long g = (long long)L.sms * occ;
         return (unsigned)(g < full ? g : full);
     };
-    k_wf_start<TREE><<<grid(resident_blocks<k_wf_start<TREE>>()), SIM_BLOCK, 0, L.stream>>>(P, W);
-    const unsigned g_near = grid(resident_blocks<k_wf_trace<TREE, false>>());
-    const unsigned g_walk = grid(resident_blocks<k_wf_trace<TREE, true>>());
-    const unsigned g_step = grid(resident_blocks<k_wf_step<TREE, RCALL>>());
+    k_wf_start<TREE, PRECISE><<<grid(resident_blocks<k_wf_start<TREE, PRECISE>>()), SIM_BLOCK, 0, L.stream>>>(P, W);
+    const unsigned g_near = grid(resident_blocks<k_wf_trace<TREE, false, PRECISE>>());
+    const unsigned g_walk = grid(resident_blocks<k_wf_trace<TREE, true, PRECISE>>());
+    const unsigned g_step = grid(resident_blocks<k_wf_step<TREE, RCALL, PRECISE>>());
     const unsigned g_cells = (unsigned)L.sms * 8u;
     for (int s = 0; s < P.max_bounce; s++) {
-        k_wf_trace<TREE, false><<<g_near, SIM_BLOCK, 0, L.stream>>>(P, W, s);
+        k_wf_trace<TREE, false, PRECISE><<<g_near, SIM_BLOCK, 0, L.stream>>>(P, W, s);
         k_wf_cells_count<TREE><<<g_cells, SIM_BLOCK, 0, L.stream>>>(W, s);
         k_wf_cells_scan<TREE><<<1, WF_SCAN_THREADS, 0, L.stream>>>(W, s);
         k_wf_cells_scatter<TREE><<<g_cells, SIM_BLOCK, 0, L.stream>>>(W, s);
-        k_wf_trace<TREE, true><<<g_walk, SIM_BLOCK, 0, L.stream>>>(P, W, s);
-        k_wf_step<TREE, RCALL><<<g_step, SIM_BLOCK, 0, L.stream>>>(P, W, s);
+        k_wf_trace<TREE, true, PRECISE><<<g_walk, SIM_BLOCK, 0, L.stream>>>(P, W, s);
+        k_wf_step<TREE, RCALL, PRECISE><<<g_step, SIM_BLOCK, 0, L.stream>>>(P, W, s);
     }
 }
 
@@ -74,12 +74,17 @@ static void wavefront_launch(const Params& P, const SimLaunch& L)
 template <int TREE>
 void sim_launch(const Params& P, const SimLaunch& L)
 {
-    // the wavefront form keeps photon indices in 32-bit lists and has no binary64 accumulators: larger launches and
-    // the precision mode run the pool over pregenerated photons instead
-    if (L.kernel_mode == 3 && !L.precise && P.gen_photon && L.wf.count && L.n < 0x7fffffffll) {
-        if constexpr (TREE >= 1) wavefront_launch<TREE, true>(P, L);
-        else if (L.rng_call) wavefront_launch<0, true>(P, L);
-        else wavefront_launch<0, false>(P, L);
+    // the wavefront form keeps photon indices in 32-bit lists: larger launches run the pool over pregenerated photons
+    // instead (and so does a precision-mode launch without accumulator buffers)
+    if (L.kernel_mode == 3 && P.gen_photon && L.wf.count && L.n < 0x7fffffffll && (!L.precise || L.wf.acc)) {
+        if constexpr (TREE >= 1) {
+            if (L.precise) wavefront_launch<TREE, true, true>(P, L);
+            else wavefront_launch<TREE, true, false>(P, L);
+        } else {
+            if (L.precise) wavefront_launch<0, false, true>(P, L);
+            else if (L.rng_call) wavefront_launch<0, true, false>(P, L);
+            else wavefront_launch<0, false, false>(P, L);
+        }
         return;
     }
     if constexpr (TREE >= 1) {

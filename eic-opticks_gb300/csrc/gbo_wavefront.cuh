@@ -17,7 +17,8 @@
 // Each kernel is a fraction of the whole photon program's code, so the instruction cache holds the kernel that is
 // running, and every warp works on live photons only.  Between passes a photon lives in the pregenerated-photon
 // buffers of kernel mode 2 (record, random-stream place, start instance) plus a 32-byte hit record and its list
-// entries; one step moves about 250 bytes per live photon through HBM.  Every live photon takes exactly one step per pass, so a photon of the
+// entries (in the precision mode also its binary64 position / time accumulators, 32 bytes); one step moves about
+// 250 bytes per live photon through HBM.  Every live photon takes exactly one step per pass, so a photon of the
 // list of step s has bounced s times.
 //
 // A photon's arithmetic is the same as in the other forms (same functions, same order), so photons, flag histories
@@ -111,7 +112,7 @@ GBO_DEV int wf_cell(const Accel& a, float3 pos, float3 dir, float t)
          base += (long long)gridDim.x * blockDim.x)
 
 // Start: every photon of the launch as generated by k_generate; those that may step join the list of step 0.
-template <int TREE>
+template <int TREE, bool PRECISE>
 __global__ void __launch_bounds__(SIM_BLOCK) k_wf_start(const __grid_constant__ Params P, Wavefront W)
 {
     const unsigned lane = threadIdx.x & 31u;
@@ -124,6 +125,11 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_wf_start(const __grid_constant__ 
             load_photon_streamed(p, P.gen_photon + idx);
             if (P.seq_out) seq_start(P.seq_out + idx, flag_of(p), boundary_of(p));
             go = 0 < P.max_bounce && p.time < P.max_time;
+            if (PRECISE && go) {
+                Acc64 acc;
+                acc_init(acc, p);
+                W.acc[idx] = acc;
+            }
         }
         wf_append(W.list[0], W.count, go, (int)idx);
         finish_photons(P, valid && !go, idx, p);
@@ -131,7 +137,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_wf_start(const __grid_constant__ 
 }
 
 // The query of each photon of step s up to the instance-tree walk (WALK false), or the queued queries in full.
-template <int TREE, bool WALK>
+template <int TREE, bool WALK, bool PRECISE>
 __global__ void GBO_WF_TRACE_BOUNDS k_wf_trace(const __grid_constant__ Params P, Wavefront W, int s)
 {
     const unsigned lane = threadIdx.x & 31u;
@@ -150,7 +156,7 @@ __global__ void GBO_WF_TRACE_BOUNDS k_wf_trace(const __grid_constant__ Params P,
             const float tmin = (obf & P.eps0_mask) ? P.tmin0 : P.tmin;
             Best bb;
             trace_begin(bb, P.tmax);
-            walk = trace_items<TREE, false>(P.acc, pos, mom, tmin, __ldcg(P.gen_hint + idx), !WALK, bb) == TRACE_WALK;
+            walk = trace_items<TREE, PRECISE>(P.acc, pos, mom, tmin, __ldcg(P.gen_hint + idx), !WALK, bb) == TRACE_WALK;
             if (!walk) {
                 Hit h;
                 trace_finish(P.acc, pos, mom, bb, h);
@@ -237,7 +243,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_wf_cells_scatter(Wavefront W, int
 }
 
 // The physics of step s: bounce s + 1 of every photon of the step's list.
-template <int TREE, bool RCALL>
+template <int TREE, bool RCALL, bool PRECISE>
 __global__ void GBO_WF_STEP_BOUNDS k_wf_step(const __grid_constant__ Params P, Wavefront W, int s)
 {
     const unsigned lane = threadIdx.x & 31u;
@@ -262,7 +268,9 @@ __global__ void GBO_WF_STEP_BOUNDS k_wf_step(const __grid_constant__ Params P, W
                 rng_init(rng, P.seed, r.y, r.x);
                 const int hint = (int)(h.iindex_identity >> 16);
                 h.normal = normalize(h.normal);
-                const int command = propagate(P.tab, p, h, rng);
+                Acc64 acc;
+                if (PRECISE) acc = W.acc[idx];
+                const int command = propagate(P.tab, p, h, rng, PRECISE ? &acc : nullptr);
                 const int bounce = s + 1;
                 if (P.seq_out) seq_add(P.seq_out + idx, (unsigned)bounce, flag_of(p), boundary_of(p));
                 done = command == CMD_BREAK || !(bounce < P.max_bounce && p.time < P.max_time);
@@ -270,6 +278,7 @@ __global__ void GBO_WF_STEP_BOUNDS k_wf_step(const __grid_constant__ Params P, W
                     store_photon(P.gen_photon + idx, p);
                     P.gen_rng[idx].x = rng.pos;
                     P.gen_hint[idx] = hint;
+                    if (PRECISE) W.acc[idx] = acc;
                 }
             }
         }

@@ -81,7 +81,7 @@ typedef struct gbo_config {
                                        separate kernel (84 more device bytes per photon), 3: wavefront, every step
                                        of every live photon as three passes (query to the instance-tree walk, the
                                        queued walks, physics) over photons generated up front (136 more device bytes
-                                       per photon; binary32 only, the precision mode runs mode 2).
+                                       per photon, 168 in the precision mode).
                                        gbo_simulate_noalloc runs its own one-thread kernel */
     int32_t  refill_min;            /* pool kernel: idle lanes a warp waits for before refilling (1..32, 4) */
     int32_t  blocks_per_sm;         /* pool kernel: resident blocks per SM (0: occupancy maximum) */

@@ -84,3 +84,28 @@ def test_fp64_intersection_error_other_geometries(oracle, name):
               % (name, precision, ok.mean(), q[0], q[1], q[2], err.max(), (err / ulp).max()))
     assert out[0][0] > 0.999 and out[1][0] > 0.999
     assert out[1][1] <= out[0][1] * 1.0001 + 1e-9
+
+
+@pytest.mark.parametrize("fixture", ["sim_crystal_array.npz", "sim_large_sphere_small.npz"])
+def test_precision_mode_kernel_forms_agree(fixture):
+    """The precision mode in every kernel form (one thread per photon, photon pool over pregenerated photons,
+    wavefront carrying each photon's binary64 accumulators between its passes): the same flag histories, flags,
+    indices and hits; float words within the kernel-form bounds, or, on the mirrored small sphere whose paths grow
+    last-bit differences between separately compiled kernels, within 1e-3 mm / 1e-3 ns for at least as many photons
+    as the reference's own builds agree on."""
+    import __graft_entry__ as ge
+    ge.build()
+    from conftest import assert_forms_agree, golden_arrays, load_golden
+    from eic_opticks_gb300 import engine as E
+    z = load_golden(fixture)
+    arrays = golden_arrays(z)
+    out = {}
+    for mode in (1, 2, 3):
+        eng = E.Engine(arrays, precision=1, record_photon=1, record_seq=1, kernel_mode=mode)
+        eng.simulate(int(z["event_index"]), z["gs"])
+        out[mode] = (eng.photons(), eng.seq(), eng.hits())
+        eng.close()
+    for mode in (2, 3):
+        assert np.array_equal(out[mode][1].view(np.uint64), out[1][1].view(np.uint64))
+        assert np.array_equal(out[mode][2]["index"], out[1][2]["index"])
+        assert_forms_agree(out[mode][0], out[1][0], fixture)
