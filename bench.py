@@ -55,19 +55,25 @@ TRAFFIC_SOURCE = {("crystal_array", 1): "ncu DRAM bytes of k_simulate on a 1M-ph
 
 
 def pinned_photons(n):
-    """A host array of n photon records in page-locked memory (the destination of the end-to-end hit download);
-    pageable memory if the allocator cannot pin it."""
+    """A host array of at least n photon records in page-locked memory (the destination of the end-to-end hit
+    download), one buffer for the whole run that grows when a larger event needs it (page-locked memory is a limited
+    resource: a buffer per configuration had left the later, larger ones pageable); pageable memory if the allocator
+    cannot pin it.  pinned_photons.pinned tells which."""
     import torch
     from eic_opticks_gb300 import engine as E
-    try:
-        buf = torch.empty(n * E.L.PHOTON.itemsize, dtype=torch.uint8, pin_memory=True)
-    except RuntimeError:
-        return np.zeros(n, dtype=E.L.PHOTON)
-    pinned_photons.keep.append(buf)             # the tensor owns the memory: keep it alive with the array
-    return buf.numpy().view(E.L.PHOTON)
+    if pinned_photons.buf is None or pinned_photons.buf.numel() < n * E.L.PHOTON.itemsize:
+        pinned_photons.buf = None               # release the smaller buffer before pinning the larger one
+        try:
+            pinned_photons.buf = torch.empty(n * E.L.PHOTON.itemsize, dtype=torch.uint8, pin_memory=True)
+            pinned_photons.pinned = bool(pinned_photons.buf.is_pinned())
+        except RuntimeError:
+            pinned_photons.pinned = False
+            return np.zeros(n, dtype=E.L.PHOTON)
+    return pinned_photons.buf.numpy().view(E.L.PHOTON)
 
 
-pinned_photons.keep = []
+pinned_photons.buf = None
+pinned_photons.pinned = False
 
 
 def peaks():
@@ -560,7 +566,8 @@ def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=N
                               "chosen_by": "--form" if form else "autotuner on 10% sample"},
                    "max_bounce": 31},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "simulate_ms": float(np.mean(e2e_sim_ms)), "hit_download_ms": float(np.mean(e2e_hits_ms))},
+                "simulate_ms": float(np.mean(e2e_sim_ms)), "hit_download_ms": float(np.mean(e2e_hits_ms)),
+                "hit_buffer": "page-locked" if pinned_photons.pinned else "pageable"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": (TRAFFIC_B_PER_PHOTON[traffic_key] * n_photon

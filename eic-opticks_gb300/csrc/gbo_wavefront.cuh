@@ -2,7 +2,7 @@
 //
 // The photon program of CSGOptiX/CSGOptiX7.cu:405-503 runs one photon per thread from generation to its last
 // bounce.  The persistent pool forms keep that shape; this form cuts it at every step instead.  Step s of every live
-// photon runs as three passes over the list of photons alive at step s, each pass a kernel of its own:
+// photon runs as kernels over the list of photons alive at step s: three passes, and a sort between the first two:
 //
 //   k_wf_trace<TREE, false>  the query's first part: the photon's previous instance, then that instance's overlap
 //                            list or its clear ball (trace_items stopped before the instance-tree walk).  Queries
@@ -30,8 +30,8 @@
 namespace gbo {
 
 // Register budgets of the passes, measured on the 100M-photon, 20,000-sensor event: 128 for the query passes (4 blocks
-// of 128 per SM, a few spills) beat 168 without spills by 10 %; 80 for the physics pass (6 blocks per SM) beat
-// ptxas' own choice (72, 20 B of spills) by 2 %.  A persistent walk pass (lanes whose walk ended taking the next
+// of 128 per SM, a few spills) beat 168 without spills by 10 %; a budget of 80 for the physics pass (ptxas then uses
+// 72 without spills: 7 blocks per SM) beat ptxas' unbounded choice (72 with 20 B of spills) by 2 %.  A persistent walk pass (lanes whose walk ended taking the next
 // queued query, one traversal round at a time) ran 17-23 % slower than these one-query-per-lane passes.
 #ifndef GBO_WF_TRACE_BOUNDS
 #define GBO_WF_TRACE_BOUNDS __maxnreg__(128)
@@ -91,7 +91,9 @@ GBO_DEV unsigned wf_spread(unsigned v)          // 5 bits -> every third bit
 GBO_DEV int wf_cell(const Accel& a, float3 pos, float3 dir, float t)
 {
     const float4* root = reinterpret_cast<const float4*>(a.tlas);
-    const float4 l0 = __ldg(root), h0 = __ldg(root + 1), l1 = __ldg(root + 2), h1 = __ldg(root + 3);
+    const float4 l0 = __ldg(root), h0 = __ldg(root + 1);
+    float4 l1 = __ldg(root + 2), h1 = __ldg(root + 3);
+    if (__float_as_int(h1.w) < 0) { l1 = l0; h1 = h0; }        // a root with one child
     const float3 lo = f3(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z));
     const float3 hi = f3(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z));
     const float3 ext = hi - lo;
