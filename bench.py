@@ -282,7 +282,7 @@ def pct(v, q):
     return float(np.percentile(np.asarray(v), q)) if len(v) else None
 
 
-def serving_bench(num_events=160, submitters=16, load=0.8, lo=3.0, hi=7.0):
+def serving_bench(num_events=400, submitters=16, load=0.8, lo=3.0, hi=7.0):
     """Plain one-launch-per-event path vs the continuous-batching server on the mixed serving workload.
 
     * plain capacity: events processed one synchronous gbo_simulate call at a time (the reference's way);
@@ -716,7 +716,7 @@ def main():
         "e2e": m["e2e"], "gpu_launches": m["gpu_launches"], "roofline": m["roofline"], "clocks": m["clocks"],
     }
     if not args.no_serving and world == 1:
-        line["serving"] = serving_bench()                                   # the 1e3-1e7 serving stream
+        line["serving"] = serving_bench(num_events=400)                     # the 1e3-1e7 serving stream
         line["serving_small_events"] = serving_bench(num_events=1500, lo=3.0, hi=5.0)
     n_batch = args.batch_events if args.batch_events is not None else (
         {"nested_boxes": 64, "water_cube": 16, "crystal_array": 8, "large_sphere": 2}[args.workload])
