@@ -35,18 +35,30 @@ namespace gbo {
 
 constexpr int SCAN_WORDS = 256;     // words per block in k_word_prefix
 
-// every photon of the launch generated up front, converged, so that the pool kernel's refills are plain loads
+// Every photon of the launch generated up front, converged, so that the pool kernel's refills are plain loads.  A
+// warp generates GEN_PER_LANE x 32 consecutive photons, 32 at a time: the photons of a genstep are consecutive, so
+// after one binary search a lane finds its next photon's genstep by stepping forward (usually not at all) instead of
+// searching again (the search's chain of dependent loads had bound the kernel).
+constexpr int GEN_PER_LANE = 8;
+
 __global__ void __launch_bounds__(SIM_BLOCK) k_generate(const __grid_constant__ Params P)
 {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= P.num_photon) return;
-    Photon p;
-    RngT<false> rng;
-    int hint;
-    generate(P, idx, p, rng, hint);
-    store_photon(P.gen_photon + idx, p);
-    P.gen_rng[idx] = make_ulonglong2(rng.pos, ((unsigned long long)rng.sub_hi << 32) | rng.sub_lo);
-    P.gen_hint[idx] = hint;
+    const unsigned lane = threadIdx.x & 31u;
+    const long long first = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (32ll * GEN_PER_LANE);
+    int gi = -1;
+    for (int j = 0; j < GEN_PER_LANE; j++) {
+        const long long idx = first + 32ll * j + lane;
+        if (idx >= P.num_photon) return;
+        if (gi < 0) gi = genstep_of(P, idx);
+        else while (__ldg(P.gs_end + gi) <= (unsigned long long)idx) gi++;
+        Photon p;
+        RngT<false> rng;
+        int hint;
+        generate_at(P, idx, gi, p, rng, hint);
+        store_photon(P.gen_photon + idx, p);
+        P.gen_rng[idx] = make_ulonglong2(rng.pos, ((unsigned long long)rng.sub_hi << 32) | rng.sub_lo);
+        P.gen_hint[idx] = hint;
+    }
 }
 
 // Start instance of each genstep's photons: of the instances whose padded world box holds the genstep position
@@ -449,7 +461,8 @@ static void launch_simulate(const gbo_engine* e, const Params& P, long long n, u
     if (wf) L.wf = *wf;
     if (L.kernel_mode != 1) {
         if (P.gen_photon && n > 0) {
-            k_generate<<<(unsigned)((n + SIM_BLOCK - 1) / SIM_BLOCK), SIM_BLOCK, 0, s>>>(P);
+            const long long per_block = (long long)SIM_BLOCK * GEN_PER_LANE;
+            k_generate<<<(unsigned)((n + per_block - 1) / per_block), SIM_BLOCK, 0, s>>>(P);
             if (after_gen) cudaEventRecord(after_gen, s);
         }
         const int form = kernel_form(e);

@@ -135,15 +135,22 @@ k_simulate(const __grid_constant__ Params P)
 
 // ---- persistent form: lanes refill from a photon pool so a warp never idles behind its longest photon --------
 
-// `hint` receives the start instance found for the photon's genstep (-1 when none was computed)
-template <class R>
-GBO_GEN void generate(const Params& P, long long idx, Photon& p, R& rng, int& hint)
+// the genstep holding launch photon idx: the first whose inclusive numphoton prefix exceeds idx
+GBO_DEV int genstep_of(const Params& P, long long idx)
 {
     int lo = 0, hi = P.num_gs - 1;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         if (__ldg(P.gs_end + mid) > (unsigned long long)idx) hi = mid; else lo = mid + 1;
     }
+    return lo;
+}
+
+// Photon idx of genstep lo, as generate_photon makes it; `hint` receives the start instance found for the genstep
+// (-1 when none was computed)
+template <class R>
+GBO_DEV void generate_in(const Params& P, long long idx, int lo, Photon& p, R& rng, int& hint)
+{
     hint = P.gs_hint ? __ldg(P.gs_hint + lo) : -1;
     const float4* g = P.gs + 6 * (size_t)lo;
     float4 gq[6];
@@ -179,6 +186,19 @@ GBO_GEN void generate(const Params& P, long long idx, Photon& p, R& rng, int& hi
         default: break;
     }
     set_index(p, photon_idx);
+}
+
+template <class R>
+GBO_GEN void generate(const Params& P, long long idx, Photon& p, R& rng, int& hint)
+{
+    generate_in(P, idx, genstep_of(P, idx), p, rng, hint);
+}
+
+// the same for a caller that knows the photon's genstep
+template <class R>
+GBO_GEN void generate_at(const Params& P, long long idx, int lo, Photon& p, R& rng, int& hint)
+{
+    generate_in(P, idx, lo, p, rng, hint);
 }
 
 constexpr int POOL_CHUNK = 32;      // pregenerated photons a warp claims at once (kernel mode 2)
