@@ -259,7 +259,18 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
         }
         d.solid = s;
         d.identity = (uint32_t)q.q2.i[3];
-        d.is_identity = ident ? 1 : 0;
+        // 2: the inverse's rotation block is exactly 1 on the diagonal and +0 elsewhere (a pure translation)
+        bool shift = true;
+        for (int j = 0; j < 3; j++) {
+            const float* c = j == 0 ? d.c0 : (j == 1 ? d.c1 : d.c2);
+            for (int k = 0; k < 3; k++) {
+                uint32_t bits;
+                std::memcpy(&bits, c + k, 4);
+                shift = shift && bits == (k == j ? 0x3f800000u : 0u);
+            }
+            shift = shift && std::isfinite(c[3]);
+        }
+        d.is_identity = ident ? 1 : (shift ? 2 : 0);
         d.iindex = (uint32_t)i;
         const Box& sb = solid_box[s];
         Box wb;

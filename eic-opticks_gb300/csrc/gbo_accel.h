@@ -53,7 +53,7 @@ struct InstDev {
     float c0[4], c1[4], c2[4];     // columns of the inverse (object <- world) 3x4 transform: xyz rows + translation
     int32_t solid;
     uint32_t identity;             // sensor_identifier + 1, 0 : not a sensor
-    int32_t is_identity;
+    int32_t is_identity;           // 1: identity, 2: pure translation (rotation block exactly 1 and +0), 0: other
     uint32_t iindex;
 };
 static_assert(sizeof(InstDev) == 64, "InstDev is 64 bytes");

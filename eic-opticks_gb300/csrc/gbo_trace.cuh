@@ -7,7 +7,8 @@
 //   * the closest t wins; equal t resolve to the lowest (instance, prim) so that the result does not depend on
 //     traversal order or on the instance hint;
 //   * the object-frame normal goes to the world frame through the inverse-transpose
-//     (optixTransformNormalFromObjectToWorldSpace); identity instances skip both transforms;
+//     (optixTransformNormalFromObjectToWorldSpace); identity instances skip both transforms, and in the single-leaf
+//     forms translated instances take the ray by one addition when that gives the transform's result bit for bit;
 //   * iindex|identity and globalPrimIdx|boundary packed in 16-bit halves (CSGOptiX7.cu:753, :929);
 //   * a miss returns boundary 0xffff (__miss__ms).
 // Traversal: the instance the photon last hit (the hint) is intersected first, since photons mostly stay inside
@@ -145,17 +146,49 @@ struct Best {
     unsigned pb;
 };
 
+GBO_DEV bool no_zero(float3 v) { return v.x != 0.f && v.y != 0.f && v.z != 0.f; }
+
+// Single-leaf forms share the world-frame reciprocal direction between the instance tests and the box tests of a
+// query, and take translated instances by the shortcut below.  In the CSG-tree forms both cost more registers than
+// they save (the wavefront walk pass ran 4 % slower on the 20,000-sensor sphere, whose sensors are rotated).
+template <int TREE> struct InvShare { static constexpr bool on = TREE == 0; };
+
+// the world-frame reciprocal direction `inv`, computed once per query by the first test that needs it
+template <int TREE>
+GBO_DEV void need_inv(float3& inv, bool& inv_ok, float3 dir)
+{
+    if (!InvShare<TREE>::on || !inv_ok) { inv = safe_inv(dir); inv_ok = true; }
+}
+
 template <int TREE, bool POLISH>
-GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float tmin, Best& b)
+GBO_DEV void test_instance(const Accel& a, int ii, float3 pos, float3 dir, float tmin, Best& b, float3& inv,
+                           bool& inv_ok)
 {
     const InstDev d = load_inst(a.inst + ii);
-    const float3 oo = d.is_identity ? pos : inst_point(d, pos);
-    const float3 od = d.is_identity ? dir : inst_vector(d, dir);
-    const float3 oinv = safe_inv(od);
+    // an inverse that is a pure translation (rotation block 1 on the diagonal, +0 elsewhere; is_identity 2) maps a
+    // ray with no zero coordinate to exactly pos + t and dir: the general transform's products by 1 and +0 are exact
+    // and its sums of them add nothing, so this local ray and its reciprocal direction equal the general ones bit
+    // for bit
+    const bool shift = InvShare<TREE>::on && !POLISH && d.is_identity == 2 && no_zero(pos) && no_zero(dir);
+    float3 oo, od, oinv;
+    if (d.is_identity == 1 || shift) {
+        oo = shift ? f3(pos.x + d.c0[3], pos.y + d.c1[3], pos.z + d.c2[3]) : pos;
+        od = dir;
+        if (InvShare<TREE>::on) {
+            need_inv<TREE>(inv, inv_ok, dir);
+            oinv = inv;
+        } else {
+            oinv = safe_inv(od);
+        }
+    } else {
+        oo = inst_point(d, pos);
+        od = inst_vector(d, dir);
+        oinv = safe_inv(od);
+    }
     // precision mode: the ray handed to the prims is transformed in binary64, once per instance and only when a
     // prim box is hit (the box test keeps the binary32 ray: boxes are padded far beyond its error)
     float3 po = oo, pd = od;
-    bool have64 = !POLISH || d.is_identity;
+    bool have64 = !POLISH || d.is_identity == 1;
     const int2 so = __ldg(reinterpret_cast<const int2*>(a.solid + d.solid));
     for (int k2 = 0; k2 < so.y; k2++) {
         const float4* pq = reinterpret_cast<const float4*>(a.prim + so.x + k2);
@@ -213,12 +246,14 @@ GBO_DEV int trace_items(const Accel& a, float3 pos, float3 dir, float tmin, int 
     int item = 0;
     int ov_first = 0;
     bool root_next = false;         // the TLAS root waits under the hint item (kept out of the local-memory stack)
+    bool inv_ok = false;
     if (hint >= 0) {
         root_next = true;
         item = leaf_item(HINT_FIRST, 1);
     } else {
         if (stop_at_root) return TRACE_WALK;
         inv = safe_inv(dir);
+        inv_ok = true;
     }
     // while-while traversal (Aila & Laine 2009): every lane first descends inner nodes until it holds a leaf, then
     // the lanes process their leaves together, so the expensive instance / CSG work runs with the warp converged;
@@ -262,7 +297,7 @@ GBO_DEV int trace_items(const Accel& a, float3 pos, float3 dir, float tmin, int 
                     float tn;
                     if (!slab(wlo, whi, pos, inv, tmin, b.t, tn)) continue;
                 }
-                test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b);
+                test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b, inv, inv_ok);
             }
             if (first == HINT_FIRST) {
                 // when the previous instance's closest hit keeps the whole segment inside its box, only the instances
@@ -275,7 +310,10 @@ GBO_DEV int trace_items(const Accel& a, float3 pos, float3 dir, float tmin, int 
                     sp = 0;
                     root_next = false;
                     item = NONE;
-                    if (ocount > 0) { item = leaf_item(OVERLAP_FIRST, ocount); inv = safe_inv(dir); }
+                    if (ocount > 0) {
+                        item = leaf_item(OVERLAP_FIRST, ocount);
+                        need_inv<TREE>(inv, inv_ok, dir);
+                    }
                     continue;
                 }
                 // a container (long overlap list): a segment inside its clear ball meets no other instance
@@ -289,7 +327,7 @@ GBO_DEV int trace_items(const Accel& a, float3 pos, float3 dir, float tmin, int 
                     }
                 }
                 if (stop_at_root) return TRACE_WALK;      // the TLAS walk, deferred by the caller
-                inv = safe_inv(dir);                // the TLAS walk follows
+                need_inv<TREE>(inv, inv_ok, dir);     // the TLAS walk follows
             }
             item = pop_item(stack, sp, root_next);
         }
@@ -317,7 +355,7 @@ GBO_DEV void trace_finish(const Accel& a, float3 pos, float3 dir, const Best& b,
     const InstDev d = load_inst(a.inst + b.inst);
     float3 n = f3(b.is.x, b.is.y, b.is.z);
     float lz;
-    if (d.is_identity) {
+    if (d.is_identity == 1) {
         lz = pos.z + b.is.w * dir.z;
     } else {
         n = inst_normal(d, n);
@@ -345,6 +383,7 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
     int item = 0;
     int ov_first = 0;
     bool root_next = false;         // the TLAS root waits under the hint item (kept out of the local-memory stack)
+    bool inv_ok = hint < 0;
     if (hint >= 0) { root_next = true; item = leaf_item(HINT_FIRST, 1); }
     else inv = safe_inv(dir);
     // while-while traversal (Aila & Laine 2009): every lane first descends inner nodes until it holds a leaf, then
@@ -389,7 +428,7 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
                     float tn;
                     if (!slab(wlo, whi, pos, inv, tmin, b.t, tn)) continue;
                 }
-                test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b);
+                test_instance<TREE, POLISH>(a, ii, pos, dir, tmin, b, inv, inv_ok);
             }
             if (first == HINT_FIRST) {
                 // when the previous instance's closest hit keeps the whole segment inside its box, only the instances
@@ -402,7 +441,10 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
                     sp = 0;
                     root_next = false;
                     item = NONE;
-                    if (ocount > 0) { item = leaf_item(OVERLAP_FIRST, ocount); inv = safe_inv(dir); }
+                    if (ocount > 0) {
+                        item = leaf_item(OVERLAP_FIRST, ocount);
+                        need_inv<TREE>(inv, inv_ok, dir);
+                    }
                     continue;
                 }
                 // a container (long overlap list): a segment inside its clear ball meets no other instance
@@ -415,7 +457,7 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
                         continue;
                     }
                 }
-                inv = safe_inv(dir);                // the TLAS walk follows
+                need_inv<TREE>(inv, inv_ok, dir);     // the TLAS walk follows
             }
             item = pop_item(stack, sp, root_next);
         }
@@ -432,7 +474,7 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
     const InstDev d = load_inst(a.inst + b.inst);
     float3 n = f3(b.is.x, b.is.y, b.is.z);
     float lz;
-    if (d.is_identity) {
+    if (d.is_identity == 1) {
         lz = pos.z + b.is.w * dir.z;
     } else {
         n = inst_normal(d, n);

@@ -7,10 +7,16 @@
 //     child (when other instances exist);
 //   * every overlap-list entry is another instance whose world box meets the listing instance's box;
 //   * no other instance's world box enters a clear ball;
-//   * the deepest leaf fits the traversal stack (one entry per inner node on a path).
+//   * the deepest leaf fits the traversal stack (one entry per inner node on a path);
+//   * is_identity is 1 exactly for identity instances and 2 exactly for inverses whose rotation block is 1 on the
+//     diagonal and +0 elsewhere, and for those the single-leaf traversal's shortcut (pos + translation, dir
+//     unchanged, for rays with no zero coordinate) equals the general transform bit for bit on seeded rays.
 // Prints one summary line; exits non-zero on the first violation.
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
+#include <cstring>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -166,7 +172,46 @@ int main(int argc, char** argv)
             CHECK(d2 >= (double)c[3], "instance %d's box enters the clear ball of %d", j, i);
         }
     }
-    std::printf("instances %d nodes %zu depth %d root leaves %d containers %d listed %d full %d balls %d\n", n,
-                A.tlas2.size(), A.max_depth, leaves_at_root, containers, listed, full, balls);
+    // instance classes and the translated-instance shortcut (binary32, no contraction: the operation order of the
+    // device's general transform, inst_point / inst_vector)
+    int shifted = 0;
+    std::mt19937 gen(7);
+    std::uniform_real_distribution<float> u(-1.f, 1.f);
+    for (int i = 0; i < n; i++) {
+        const InstDev& q = A.inst[i];
+        const gbo_qat4& f = inst[i];
+        const bool ident = f.q0.f[0] == 1.f && f.q0.f[1] == 0.f && f.q0.f[2] == 0.f && f.q1.f[0] == 0.f &&
+                           f.q1.f[1] == 1.f && f.q1.f[2] == 0.f && f.q2.f[0] == 0.f && f.q2.f[1] == 0.f &&
+                           f.q2.f[2] == 1.f && f.q3.f[0] == 0.f && f.q3.f[1] == 0.f && f.q3.f[2] == 0.f;
+        const float* col[3] = {q.c0, q.c1, q.c2};
+        bool unit = true;
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++) {
+                uint32_t bits;
+                std::memcpy(&bits, col[j] + k, 4);
+                unit = unit && bits == (j == k ? 0x3f800000u : 0u);
+            }
+        CHECK(q.is_identity == (ident ? 1 : (unit ? 2 : 0)), "instance %d classed %d", i, q.is_identity);
+        if (q.is_identity != 2) continue;
+        shifted++;
+        for (int r = 0; r < 64; r++) {
+            float p[3], v[3];
+            for (int k = 0; k < 3; k++) {
+                p[k] = 1000.f * u(gen);
+                v[k] = u(gen);
+            }
+            for (int j = 0; j < 3; j++) {
+                const float* c = col[j];
+                const volatile float pj = ((c[0] * p[0] + c[1] * p[1]) + c[2] * p[2]) + c[3] * 1.f;
+                const volatile float vj = ((c[0] * v[0] + c[1] * v[1]) + c[2] * v[2]) + c[3] * 0.f;
+                const float ps = p[j] + c[3];
+                CHECK(std::memcmp((const void*)&pj, &ps, 4) == 0 && std::memcmp((const void*)&vj, &v[j], 4) == 0,
+                      "instance %d: translated shortcut differs from the transform", i);
+            }
+        }
+    }
+    std::printf("instances %d nodes %zu depth %d root leaves %d containers %d listed %d full %d balls %d "
+                "translated %d\n", n, A.tlas2.size(), A.max_depth, leaves_at_root, containers, listed, full, balls,
+                shifted);
     return 0;
 }
