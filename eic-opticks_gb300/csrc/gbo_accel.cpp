@@ -342,6 +342,7 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
             }
         }
         out.inst_box.resize(num_inst);
+        out.inner_box.resize(num_inst);
         for (int i = 0; i < num_inst; i++) {
             InstBox& ib = out.inst_box[i];
             for (int k = 0; k < 3; k++) {
@@ -356,6 +357,22 @@ int build_accel(const gbo_csgnode* node, int num_node, const gbo_csgprim* prim, 
             std::sort(ov[i].begin(), ov[i].end());
             ib.overlap_first = (int32_t)out.overlap.size();
             ib.overlap_count = full[i] ? -1 : (int32_t)ov[i].size();
+            InstBox& in = out.inner_box[i];
+            bool empty = false;
+            for (int k = 0; k < 3; k++) {
+                const double lo = ib.lo[k], hi = ib.hi[k];
+                const double m = 2e-6 * (std::max(std::fabs(lo), std::fabs(hi)) + std::fabs(lo) + std::fabs(hi)) + 1e-5;
+                float ilo = (float)(lo + m), ihi = (float)(hi - m);
+                if ((double)ilo < lo + m) ilo = std::nextafter(ilo, INFINITY);
+                if ((double)ihi > hi - m) ihi = std::nextafter(ihi, -INFINITY);
+                in.lo[k] = ilo;
+                in.hi[k] = ihi;
+                empty = empty || !(ilo < ihi);
+            }
+            if (empty)
+                for (int k = 0; k < 3; k++) { in.lo[k] = INFINITY; in.hi[k] = -INFINITY; }
+            in.overlap_first = ib.overlap_first;
+            in.overlap_count = ib.overlap_count;
             if (!full[i]) out.overlap.insert(out.overlap.end(), ov[i].begin(), ov[i].end());
         }
         if (out.overlap.empty()) out.overlap.push_back(0);

@@ -91,6 +91,10 @@ struct AccelHost {
     std::vector<PrimDev> prim;
     std::vector<SolidDev> solid;
     std::vector<InstBox> inst_box;
+    // per instance: inst_box shrunk on each axis by 2e-6 (max(|lo|, |hi|) + |lo| + |hi|) + 1e-5, rounded inward, with
+    // the same overlap list fields: a point strictly inside it lies inside inst_box by more than the rounding of a
+    // photon's position and of its segment's end (an empty box where the shrink consumes it)
+    std::vector<InstBox> inner_box;
     std::vector<int32_t> overlap;
     // per instance (cx, cy, cz, r^2): a ball no other instance's box enters, for instances whose overlap list is
     // too long (r^2 = 0: none)

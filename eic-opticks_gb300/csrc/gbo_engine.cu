@@ -381,6 +381,7 @@ struct gbo_engine {
     DBuf<InstDev> inst;
     DBuf<double> inst64;                   // precision mode only
     DBuf<InstBox> inst_box;
+    DBuf<InstBox> inner_box;
     DBuf<int32_t> overlap;
     DBuf<float> clear;
     DBuf<PrimDev> prim;
@@ -559,7 +560,7 @@ void gbo_engine_destroy(gbo_engine* e)
     if (e->icdf_tex) cudaDestroyTextureObject(e->icdf_tex);
     if (e->bnd_array) cudaFreeArray(e->bnd_array);
     if (e->icdf_array) cudaFreeArray(e->icdf_array);
-    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->inst_box.release(); e->overlap.release(); e->clear.release(); e->prim.release(); e->solid.release();
+    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->inst_box.release(); e->inner_box.release(); e->overlap.release(); e->clear.release(); e->prim.release(); e->solid.release();
     e->node.release(); e->plan.release(); e->itra.release(); e->optical.release();
     e->gs.release(); e->gs_end.release(); e->input.release(); e->photon.release(); e->seq.release();
     e->hits_unordered.release(); e->hits.release(); e->merged.release(); gbo::merge_scratch_free(e->merge_scratch); e->merge_scratch = nullptr; e->gen_photon.release(); e->gen_rng.release(); e->gen_hint.release(); e->wf.release(); e->gs_hint.release(); e->bitmap.release(); e->word_prefix.release();
@@ -649,6 +650,7 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     TRY(upload(e->inst, acc.inst.data(), acc.inst.size(), e->stream));
     if (e->cfg.precision) TRY(upload(e->inst64, acc.inst64.data(), acc.inst64.size(), e->stream));
     TRY(upload(e->inst_box, acc.inst_box.data(), acc.inst_box.size(), e->stream));
+    TRY(upload(e->inner_box, acc.inner_box.data(), acc.inner_box.size(), e->stream));
     TRY(upload(e->overlap, acc.overlap.data(), acc.overlap.size(), e->stream));
     TRY(upload(e->clear, acc.clear.data(), acc.clear.size(), e->stream));
     TRY(upload(e->prim, acc.prim.data(), acc.prim.size(), e->stream));
@@ -703,6 +705,7 @@ static Params make_params(gbo_engine* e)
     P.acc.inst = e->inst.ptr;
     P.acc.inst64 = e->inst64.ptr;
     P.acc.inst_box = reinterpret_cast<const float4*>(e->inst_box.ptr);
+    P.acc.inner_box = reinterpret_cast<const float4*>(e->inner_box.ptr);
     P.acc.overlap = e->overlap.ptr;
     P.acc.clear = reinterpret_cast<const float4*>(e->clear.ptr);
     P.acc.prim = e->prim.ptr;

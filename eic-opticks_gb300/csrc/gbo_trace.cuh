@@ -36,6 +36,7 @@ struct Accel {
     const gbo_qat4* itra;
     const double* inst64;       // binary64 inverse columns, 12 per instance (precision mode only)
     const float4* inst_box;     // InstBox per instance (2 x float4): world box, overlap list range
+    const float4* inner_box;    // InstBox per instance: the world box shrunk by the inside test's margin
     const int* overlap;         // overlap lists
     const float4* clear;        // per instance: ball (centre, r^2) that no other instance's box enters
 };
@@ -47,16 +48,13 @@ GBO_DEV bool inside_ball(float4 c, float3 p)
     return dx * dx + dy * dy + dz * dz < c.w * 0.9999f;
 }
 
-// p inside the box by a margin of ~30 binary32 ulp of the coordinates involved: far above the rounding of p and of
-// pos + t dir, far below the boxes' padding (1e-5 x extent + 1e-3 mm), so photons sitting on a face of their
-// instance's solid still pass
+// p inside an instance's box by a margin of ~30 binary32 ulp of the coordinates involved: far above the rounding of
+// p and of pos + t dir, far below the boxes' padding (1e-5 x extent + 1e-3 mm), so photons sitting on a face of
+// their instance's solid still pass.  The margin is folded into the instance's inner box on the host (its largest
+// value over the box), so the test is six compares.
 GBO_DEV bool inside_box(float4 lo, float4 hi, float3 p)
 {
-    const float mx = 2e-6f * (fabsf(p.x) + fabsf(lo.x) + fabsf(hi.x)) + 1e-5f;
-    const float my = 2e-6f * (fabsf(p.y) + fabsf(lo.y) + fabsf(hi.y)) + 1e-5f;
-    const float mz = 2e-6f * (fabsf(p.z) + fabsf(lo.z) + fabsf(hi.z)) + 1e-5f;
-    return p.x > lo.x + mx && p.x < hi.x - mx && p.y > lo.y + my && p.y < hi.y - my && p.z > lo.z + mz &&
-           p.z < hi.z - mz;
+    return p.x > lo.x && p.x < hi.x && p.y > lo.y && p.y < hi.y && p.z > lo.z && p.z < hi.z;
 }
 
 GBO_DEV bool slab(float4 bmin, float4 bmax, float3 o, float3 inv, float tmin, float tmax, float& tnear)
@@ -302,7 +300,7 @@ GBO_DEV int trace_items(const Accel& a, float3 pos, float3 dir, float tmin, int 
             if (first == HINT_FIRST) {
                 // when the previous instance's closest hit keeps the whole segment inside its box, only the instances
                 // whose boxes overlap that box can hold a closer hit: their short list replaces the TLAS
-                const float4 blo = __ldg(a.inst_box + 2 * hint), bhi = __ldg(a.inst_box + 2 * hint + 1);
+                const float4 blo = __ldg(a.inner_box + 2 * hint), bhi = __ldg(a.inner_box + 2 * hint + 1);
                 const int ocount = __float_as_int(bhi.w);
                 const float3 e = pos + b.t * dir;
                 if (ocount >= 0 && inside_box(blo, bhi, pos) && inside_box(blo, bhi, e)) {
@@ -433,7 +431,7 @@ GBO_DEV void trace(const Accel& a, float3 pos, float3 dir, float tmin, float tma
             if (first == HINT_FIRST) {
                 // when the previous instance's closest hit keeps the whole segment inside its box, only the instances
                 // whose boxes overlap that box can hold a closer hit: their short list replaces the TLAS
-                const float4 blo = __ldg(a.inst_box + 2 * hint), bhi = __ldg(a.inst_box + 2 * hint + 1);
+                const float4 blo = __ldg(a.inner_box + 2 * hint), bhi = __ldg(a.inner_box + 2 * hint + 1);
                 const int ocount = __float_as_int(bhi.w);
                 const float3 e = pos + b.t * dir;
                 if (ocount >= 0 && inside_box(blo, bhi, pos) && inside_box(blo, bhi, e)) {

@@ -8,6 +8,8 @@
 //   * every overlap-list entry is another instance whose world box meets the listing instance's box;
 //   * no other instance's world box enters a clear ball;
 //   * the deepest leaf fits the traversal stack (one entry per inner node on a path);
+//   * each inner box lies inside its instance's box by the inside test's largest margin (or is empty) and carries
+//     the same overlap list;
 //   * is_identity is 1 exactly for identity instances and 2 exactly for inverses whose rotation block is 1 on the
 //     diagonal and +0 elsewhere, and for those the single-leaf traversal's shortcut (pos + translation, dir
 //     unchanged, for rays with no zero coordinate) equals the general transform bit for bit on seeded rays.
@@ -172,6 +174,19 @@ int main(int argc, char** argv)
             CHECK(d2 >= (double)c[3], "instance %d's box enters the clear ball of %d", j, i);
         }
     }
+    CHECK(A.inner_box.size() == A.inst_box.size(), "inner box count");
+    for (int i = 0; i < n; i++) {
+        const InstBox &b = A.inst_box[i], &in = A.inner_box[i];
+        CHECK(in.overlap_first == b.overlap_first && in.overlap_count == b.overlap_count, "inner box %d list", i);
+        const bool empty = in.lo[0] == INFINITY;
+        for (int k = 0; k < 3; k++) {
+            const double lo = b.lo[k], hi = b.hi[k];
+            const double m = 2e-6 * (std::fmax(std::fabs(lo), std::fabs(hi)) + std::fabs(lo) + std::fabs(hi)) + 1e-5;
+            CHECK(empty ? (in.lo[k] == INFINITY && in.hi[k] == -INFINITY) : ((double)in.lo[k] >= lo + m &&
+                  (double)in.hi[k] <= hi - m && in.lo[k] < in.hi[k]), "inner box %d axis %d", i, k);
+        }
+    }
+
     // instance classes and the translated-instance shortcut (binary32, no contraction: the operation order of the
     // device's general transform, inst_point / inst_vector)
     int shifted = 0;
