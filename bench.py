@@ -7,8 +7,9 @@ from seeded numpy generators (Geant4 is not part of the path).
 
 * ``value``  photons/s with the gensteps already resident in device memory (gbo_simulate_device), timed with
   CUDA events around each event; L2 is flushed (256 MB write) between timed events.
-* ``e2e``    photons/s through the reference-facing C ABI (gbo_simulate with host gensteps, then gbo_copy_hits
-  into pinned host memory), host<->device copies inside the timed region.
+* ``e2e``    photons/s through the reference-facing C ABI (gbo_simulate_to_host: host gensteps in, the event's hits
+  out into page-locked host memory), host<->device copies inside the timed region; ``e2e.two_calls`` is the same
+  through gbo_simulate followed by gbo_copy_hits.
 * ``roofline`` the simulate kernel's algorithmic HBM bytes per photon (genstep share + 4 B seed + 64 B photon
   write + 64 B compaction read + 64 B x hit fraction, the reference's traffic for the same event) over its
   CUDA-event time, against the measured copy bandwidth.
@@ -523,32 +524,46 @@ def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=N
     value = world * n_photon * steps / (total_ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers (e2e) ----
-    hits_host = None
-    e2e_ms, e2e_sim_ms, e2e_hits_ms = [], [], []
+    # one page-locked destination for the whole run, sized from the device-resident events' hit count (events of
+    # other ids differ by a few hits); allocated before the timed steps
+    hits_host = pinned_photons(int(hits * 1.25) + 4096)
     h2d = gs.nbytes + (inp.nbytes if inp is not None else 0)
-    nh = 0
-    for k in range(warmup + steps):
-        flush.zero_()
-        torch.cuda.synchronize()
+
+    def e2e_steps(run):
+        out_ms, nh = [], 0
+        for k in range(warmup + steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            nh = run(k)
+            t1 = time.perf_counter()
+            if k >= warmup:
+                out_ms.append((t1 - t0) * 1e3)
+        total = sum(out_ms)
+        if dist:
+            t = torch.tensor([total], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total = float(t[0])
+        return world * n_photon * steps / (total * 1e-3), out_ms, nh
+
+    # gbo_simulate_to_host: the call a user makes, hits landing in host memory when it returns
+    e2e_value, e2e_ms, nh = e2e_steps(lambda k: eng.simulate_to_host(2000 + k, gs, hits_host, inp))
+    launches_e2e = eng.stats()["simulate_launches"]
+    # gbo_simulate, then gbo_copy_hits (timed apart)
+    sim_part, hit_part = [], []
+
+    def two_calls(k):
         t0 = time.perf_counter()
-        nh = eng.simulate(2000 + k, gs, inp)
+        n = eng.simulate(4000 + k, gs, inp)
         t1 = time.perf_counter()
-        if hits_host is None or len(hits_host) < nh:
-            hits_host = pinned_photons(max(nh, 1) * 2)
-        t2 = time.perf_counter()
-        eng.hits(out=hits_host[:nh])
-        t3 = time.perf_counter()
-        if k >= warmup:             # the timed step: the call, then the hit download (a first-step buffer
-            e2e_ms.append((t1 - t0 + t3 - t2) * 1e3)        # allocation between them is setup, not timed)
-            e2e_sim_ms.append((t1 - t0) * 1e3)
-            e2e_hits_ms.append((t3 - t2) * 1e3)
+        if n > len(hits_host):
+            raise RuntimeError("%d hits for a buffer of %d" % (n, len(hits_host)))
+        eng.hits(out=hits_host[:n])
+        sim_part.append((time.perf_counter() - t1, t1 - t0))
+        return n
+    two_value, _, _ = e2e_steps(two_calls)
+    sim_part = sim_part[warmup:]
     d2h = nh * 64 + 32      # ordered hits + the counters read that sizes them
-    e2e_total = sum(e2e_ms)
-    if dist:
-        t = torch.tensor([e2e_total], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t[0])
-    e2e_value = world * n_photon * steps / (e2e_total * 1e-3)
 
     hbm, peak_kind = peaks()
     f_hit = hits / n_photon
@@ -566,8 +581,11 @@ def measure_workload(kind, args, dist, rank, world, local, steps, warmup, form=N
                               "chosen_by": "--form" if form else "autotuner on 10% sample"},
                    "max_bounce": 31},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "simulate_ms": float(np.mean(e2e_sim_ms)), "hit_download_ms": float(np.mean(e2e_hits_ms)),
-                "hit_buffer": "page-locked" if pinned_photons.pinned else "pageable"},
+                "call": "gbo_simulate_to_host", "ms_per_step": float(np.mean(e2e_ms)), "launches": launches_e2e,
+                "hit_buffer": "page-locked" if pinned_photons.pinned else "pageable",
+                "two_calls": {"value": two_value, "call": "gbo_simulate + gbo_copy_hits",
+                              "simulate_ms": float(np.mean([b for _, b in sim_part])),
+                              "hit_download_ms": float(np.mean([a for a, _ in sim_part]))}},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": (TRAFFIC_B_PER_PHOTON[traffic_key] * n_photon

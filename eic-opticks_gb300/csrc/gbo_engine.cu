@@ -17,6 +17,7 @@
 //   k_gather_*         hits written in photon order (the order thrust::copy_if gives the reference)
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -24,6 +25,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/gbopticks.h"
@@ -375,6 +377,7 @@ struct gbo_engine {
     int device = 0;
     gbo_config cfg{};
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;     // hit downloads that overlap the next launch (gbo_simulate_to_host)
     // geometry
     DBuf<BvhNode2> tlas;
     DBuf<int32_t> tlas_index;
@@ -568,6 +571,7 @@ void gbo_engine_destroy(gbo_engine* e)
     if (e->host_counters) cudaFreeHost(e->host_counters);
     for (auto& v : e->ev) if (v) cudaEventDestroy(v);
     if (e->stream) cudaStreamDestroy(e->stream);
+    if (e->copy_stream) cudaStreamDestroy(e->copy_stream);
     delete e;
 }
 
@@ -628,7 +632,8 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     if (cfg) e->cfg = *cfg; else gbo_config_default(&e->cfg);
     int rc = 0;
 #define TRY(x) do { rc = (x); if (rc) { gbo_engine_destroy(e); return rc; } } while (0)
-    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
         gbo_engine_destroy(e);
         return fail(GBO_ERR_CUDA, "cudaStreamCreate failed");
     }
@@ -745,9 +750,10 @@ struct LaunchPlace {
 };
 
 // runs one launch whose gensteps (and input photons) are already on the device
-static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int64_t num_gs,
-                     const gbo_sphoton* d_input, int64_t num_input, long long num_photon, cudaStream_t s,
-                     int prior_launches, LaunchPlace at = LaunchPlace())
+// (d_gs_end: the launch's inclusive photon-count prefix of its gensteps)
+static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, const unsigned long long* d_gs_end,
+                     int64_t num_gs, const gbo_sphoton* d_input, int64_t num_input, long long num_photon,
+                     cudaStream_t s, int prior_launches, LaunchPlace at = LaunchPlace())
 {
     const bool keep_photon = e->cfg.record_photon != 0;
     const bool keep_seq = e->cfg.record_seq != 0;
@@ -781,7 +787,7 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     const uint64_t skip = e->cfg.event_skipahead * (uint64_t)(event_id < 0 ? 0 : event_id);
     P.position0 = e->cfg.rng_offset + skip;
     P.gs = reinterpret_cast<const float4*>(d_gs);
-    P.gs_end = e->gs_end.ptr;
+    P.gs_end = d_gs_end;
     P.num_gs = (int)num_gs;
     P.num_photon = num_photon;
     P.photon_offset = at.photon_offset;
@@ -852,59 +858,98 @@ static int run_event(gbo_engine* e, int32_t event_id, const gbo_quad6* d_gs, int
     return GBO_OK;
 }
 
-int gbo_simulate(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs, const gbo_sphoton* input_photon,
-                 int64_t num_input_photon)
+// Where gbo_simulate_to_host puts an event's hits: the caller's host buffer of `capacity` hits.
+struct HitSink {
+    gbo_sphoton* host;
+    int64_t capacity;
+};
+
+// Host-side checks shared by the host-genstep entry points; the event's photon count into *total.
+static int check_host_event(const char* fn, const gbo_quad6* gs, int64_t num_gs, const gbo_sphoton* input_photon,
+                            int64_t num_input_photon, unsigned long long* total)
 {
-    if (!e) return fail(GBO_ERR_ARG, "gbo_simulate: null engine");
-    if (num_gs < 0 || (num_gs > 0 && !gs)) return fail(GBO_ERR_ARG, "gbo_simulate: bad gensteps");
-    if (num_gs > 0x7fffffff) return fail(GBO_ERR_CAPACITY, "gbo_simulate: %lld gensteps", (long long)num_gs);
-    if (num_input_photon < 0 || (num_input_photon > 0 && !input_photon)) return fail(GBO_ERR_ARG, "gbo_simulate: bad input photons");
-    CU(cudaSetDevice(e->device));
-    std::vector<unsigned long long> end((size_t)num_gs);
-    unsigned long long total = 0;
+    if (num_gs < 0 || (num_gs > 0 && !gs)) return fail(GBO_ERR_ARG, "%s: bad gensteps", fn);
+    if (num_gs > 0x7fffffff) return fail(GBO_ERR_CAPACITY, "%s: %lld gensteps", fn, (long long)num_gs);
+    if (num_input_photon < 0 || (num_input_photon > 0 && !input_photon)) return fail(GBO_ERR_ARG, "%s: bad input photons", fn);
+    unsigned long long n = 0;
     bool has_input_gs = false;
     for (int64_t i = 0; i < num_gs; i++) {
-        total += gs[i].q[0].u[3];
-        end[(size_t)i] = total;
+        n += gs[i].q[0].u[3];
         if (gs[i].q[0].i[0] == GBO_GS_INPUT_PHOTON) has_input_gs = true;
     }
-    if (has_input_gs && (long long)num_input_photon < (long long)total)
-        return fail(GBO_ERR_ARG, "gbo_simulate: INPUT_PHOTON gensteps need %llu photons, %lld given", total,
-                    (long long)num_input_photon);
-    cudaStream_t s = e->stream;
-    const long long max_slot = e->cfg.max_slot;
-    if (max_slot <= 0 || (long long)total <= max_slot) {
-        CU(cudaEventRecord(e->ev[0], s));
-        int rc;
-        if ((rc = upload(e->gs, gs, (size_t)num_gs, s))) return rc;
-        if ((rc = upload(e->gs_end, end.data(), end.size(), s))) return rc;
-        if (num_input_photon > 0) { if ((rc = upload(e->input, input_photon, (size_t)num_input_photon, s))) return rc; }
-        return run_event(e, event_id, e->gs.ptr, num_gs, num_input_photon > 0 ? e->input.ptr : nullptr, num_input_photon,
-                         (long long)total, s, 0);
+    if (has_input_gs && (long long)num_input_photon < (long long)n)
+        return fail(GBO_ERR_ARG, "%s: INPUT_PHOTON gensteps need %llu photons, %lld given", fn, n, (long long)num_input_photon);
+    *total = n;
+    return GBO_OK;
+}
+
+// Genstep ranges [g0, g1) of the launches of one event: launches of at most max_slot photons at genstep
+// granularity (SGenstep::GetGenstepSlices, qudarap/QSim.cc:481-529) when max_slot is set, else one launch.
+static std::vector<std::pair<int64_t, int64_t>> launch_ranges(const gbo_quad6* gs, int64_t num_gs, long long max_slot)
+{
+    std::vector<std::pair<int64_t, int64_t>> r;
+    if (max_slot > 0) {
+        int64_t g0 = 0;
+        while (g0 < num_gs) {
+            int64_t g1 = g0;
+            unsigned long long n = 0;
+            while (g1 < num_gs && (g1 == g0 || (long long)(n + gs[g1].q[0].u[3]) <= max_slot)) n += gs[g1++].q[0].u[3];
+            r.push_back({g0, g1});
+            g0 = g1;
+        }
+        return r;
     }
-    // Device-memory-bounded slicing of one event into launches of at most max_slot photons, at genstep
-    // granularity (SGenstep::GetGenstepSlices, qudarap/QSim.cc:481-529); every photon keeps its event-level index
-    // (photon_slot_offset + idx, CSGOptiX7.cu:415) so the event's results do not depend on the slicing.
+    r.push_back({0, num_gs});
+    return r;
+}
+
+// One event from host gensteps as the launches `ranges`.  Every photon keeps its event-level index
+// (photon_slot_offset + idx, CSGOptiX7.cu:415), so the event's results do not depend on the launches.  With a
+// sink, each launch's ordered hits go to the host buffer on the copy stream as soon as the launch ends, as the
+// reference gathers each genstep slice's hits to the host in turn; the call returns when the last copy has landed.
+// (On a GB300 with NVLink-C2C host memory, CUDA-event probes showed the next launch's first command on the
+// simulation stream completing only when such a copy ended: the copies do not overlap the launches there.)
+static int simulate_ranges(gbo_engine* e, int32_t event_id, const gbo_quad6* gs,
+                           const std::vector<std::pair<int64_t, int64_t>>& ranges, const gbo_sphoton* input_photon,
+                           int64_t num_input_photon, unsigned long long total, const HitSink* sink)
+{
+    cudaStream_t s = e->stream;
+    const int64_t num_gs = ranges.empty() ? 0 : ranges.back().second;
+    // every launch's gensteps and photon-count prefixes (from each launch's first genstep) go to the device before
+    // the first launch: a host copy issued between launches queues behind the previous launch's hit download.  Input
+    // photons still go up per launch, so that max_slot bounds their device memory too
+    std::vector<unsigned long long> part((size_t)num_gs);
+    for (const auto& gr : ranges) {
+        unsigned long long c = 0;
+        for (int64_t i = gr.first; i < gr.second; i++) { c += gs[i].q[0].u[3]; part[(size_t)i] = c; }
+    }
+    const bool inp = num_input_photon > 0;
+    CU(cudaEventRecord(e->ev[0], s));
+    int rc;
+    if ((rc = upload(e->gs, gs, (size_t)num_gs, s))) return rc;
+    if ((rc = upload(e->gs_end, part.data(), part.size(), s))) return rc;
     LaunchPlace at;
     at.capacity = (long long)total;
     gbo_stats acc{};
-    int64_t g0 = 0;
-    while (g0 < num_gs) {
-        int64_t g1 = g0;
-        unsigned long long n = 0;
-        while (g1 < num_gs && (g1 == g0 || (long long)(n + gs[g1].q[0].u[3]) <= max_slot)) n += gs[g1++].q[0].u[3];
-        std::vector<unsigned long long> part((size_t)(g1 - g0));
-        unsigned long long c = 0;
-        for (int64_t i = g0; i < g1; i++) { c += gs[i].q[0].u[3]; part[(size_t)(i - g0)] = c; }
-        CU(cudaEventRecord(e->ev[0], s));
-        int rc;
-        if ((rc = upload(e->gs, gs + g0, (size_t)(g1 - g0), s))) return rc;
-        if ((rc = upload(e->gs_end, part.data(), part.size(), s))) return rc;
-        const bool inp = num_input_photon > 0;
-        if (inp && n > 0) { if ((rc = upload(e->input, input_photon + at.photon_offset, (size_t)n, s))) return rc; }
-        if ((rc = run_event(e, event_id, e->gs.ptr, g1 - g0, inp ? e->input.ptr : nullptr, inp ? (int64_t)n : 0,
-                            (long long)n, s, 0, at)))
-            return rc;
+    for (const auto& gr : ranges) {
+        const int64_t g0 = gr.first, g1 = gr.second;
+        const unsigned long long n = g1 > g0 ? part[(size_t)(g1 - 1)] : 0ull;
+        if (g0 > 0) CU(cudaEventRecord(e->ev[0], s));
+        if (inp && n > 0 && (rc = upload(e->input, input_photon + at.photon_offset, (size_t)n, s))) break;
+        if ((rc = run_event(e, event_id, e->gs.ptr + g0, e->gs_end.ptr + g0, g1 - g0, inp ? e->input.ptr : nullptr,
+                            inp ? (int64_t)n : 0, (long long)n, s, 0, at)))
+            break;
+        if (sink) {
+            // run_event returned after its stream finished: this launch's hits [hit_base, num_hit) are final and
+            // the launches that follow write beyond them
+            const long long lo = std::min<long long>(at.hit_base, sink->capacity);
+            const long long hi = std::min<long long>(e->num_hit, sink->capacity);
+            if (hi > lo) {
+                const cudaError_t ce = cudaMemcpyAsync(sink->host + lo, e->hits.ptr + lo, (size_t)(hi - lo) * sizeof(gbo_sphoton),
+                                                       cudaMemcpyDeviceToHost, e->copy_stream);
+                if (ce != cudaSuccess) { rc = fail(GBO_ERR_CUDA, "hit download: %s", cudaGetErrorString(ce)); break; }
+            }
+        }
         acc.ms_upload += e->stats.ms_upload;
         acc.ms_simulate += e->stats.ms_simulate;
         acc.ms_compact += e->stats.ms_compact;
@@ -914,11 +959,47 @@ int gbo_simulate(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         at.photon_offset += n;
         at.photon_base += (long long)n;
         at.hit_base = e->num_hit;
-        g0 = g1;
     }
+    if (sink) {
+        const cudaError_t ce = cudaStreamSynchronize(e->copy_stream);
+        if (rc == GBO_OK && ce != cudaSuccess) rc = fail(GBO_ERR_CUDA, "hit download: %s", cudaGetErrorString(ce));
+    }
+    if (rc) return rc;
     acc.num_photon = e->num_photon;
     acc.num_hit = e->num_hit;
     e->stats = acc;
+    return GBO_OK;
+}
+
+int gbo_simulate(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs, const gbo_sphoton* input_photon,
+                 int64_t num_input_photon)
+{
+    if (!e) return fail(GBO_ERR_ARG, "gbo_simulate: null engine");
+    unsigned long long total = 0;
+    int rc;
+    if ((rc = check_host_event("gbo_simulate", gs, num_gs, input_photon, num_input_photon, &total))) return rc;
+    CU(cudaSetDevice(e->device));
+    return simulate_ranges(e, event_id, gs, launch_ranges(gs, num_gs, e->cfg.max_slot), input_photon,
+                           num_input_photon, total, nullptr);
+}
+
+int gbo_simulate_to_host(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs,
+                         const gbo_sphoton* input_photon, int64_t num_input_photon, gbo_sphoton* hits,
+                         int64_t hit_capacity, int64_t* num_hit)
+{
+    if (!e || !num_hit) return fail(GBO_ERR_ARG, "gbo_simulate_to_host: null argument");
+    if (hit_capacity < 0 || (hit_capacity > 0 && !hits)) return fail(GBO_ERR_ARG, "gbo_simulate_to_host: bad hit buffer");
+    unsigned long long total = 0;
+    int rc;
+    if ((rc = check_host_event("gbo_simulate_to_host", gs, num_gs, input_photon, num_input_photon, &total))) return rc;
+    CU(cudaSetDevice(e->device));
+    const HitSink sink{hits, hit_capacity};
+    if ((rc = simulate_ranges(e, event_id, gs, launch_ranges(gs, num_gs, e->cfg.max_slot), input_photon,
+                              num_input_photon, total, &sink)))
+        return rc;
+    *num_hit = e->num_hit;
+    if (e->num_hit > hit_capacity)
+        return fail(GBO_ERR_CAPACITY, "gbo_simulate_to_host: %lld hits for a buffer of %lld", e->num_hit, (long long)hit_capacity);
     return GBO_OK;
 }
 
@@ -949,7 +1030,7 @@ int gbo_simulate_slice(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int
     if (num_input_photon > 0) { if ((rc = upload(e->input, input_photon, (size_t)num_input_photon, s))) return rc; }
     LaunchPlace at;
     at.photon_offset = photon_offset;
-    return run_event(e, event_id, e->gs.ptr, num_gs, num_input_photon > 0 ? e->input.ptr : nullptr, num_input_photon,
+    return run_event(e, event_id, e->gs.ptr, e->gs_end.ptr, num_gs, num_input_photon > 0 ? e->input.ptr : nullptr, num_input_photon,
                      (long long)total, s, 0, at);
 }
 
@@ -978,7 +1059,7 @@ int gbo_simulate_device(gbo_engine* e, int32_t event_id, const void* d_gs, int64
             return fail(GBO_ERR_ARG, "gbo_simulate_device: INPUT_PHOTON gensteps need %llu photons, %lld given", total,
                         (long long)num_input);
     }
-    return run_event(e, event_id, (const gbo_quad6*)d_gs, num_gs, (const gbo_sphoton*)d_input, num_input,
+    return run_event(e, event_id, (const gbo_quad6*)d_gs, e->gs_end.ptr, num_gs, (const gbo_sphoton*)d_input, num_input,
                      (long long)total, s, num_gs > 0 ? 1 : 0);
 }
 

@@ -87,6 +87,8 @@ def load(path=None):
     lib.gbo_simulate.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
     lib.gbo_simulate_device.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
     lib.gbo_simulate_slice.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_uint64]
+    lib.gbo_simulate_to_host.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                                         C.c_int64, C.POINTER(C.c_int64)]
     lib.gbo_num_hit.argtypes = [C.c_void_p]
     lib.gbo_num_photon.argtypes = [C.c_void_p]
     lib.gbo_device_hits.argtypes = [C.c_void_p]
@@ -175,6 +177,20 @@ class Engine:
                                      inp.ctypes.data_as(C.c_void_p) if inp is not None else None,
                                      len(inp) if inp is not None else 0), "gbo_simulate")
         return self.num_hit()
+
+    def simulate_to_host(self, event_id, gensteps, out, input_photon=None):
+        """gbo_simulate_to_host: simulate and write the hits into `out` (a PHOTON array, page-locked for overlap);
+        returns the hit count.  A count above len(out) raises after the first len(out) hits were stored."""
+        gs = np.ascontiguousarray(gensteps, dtype=np.float32)
+        inp = np.ascontiguousarray(input_photon) if input_photon is not None else None
+        if out.dtype != L.PHOTON or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous photon array")
+        n = C.c_int64()
+        _check(self.lib.gbo_simulate_to_host(self.handle, int(event_id), gs.ctypes.data_as(C.c_void_p), len(gs),
+                                             inp.ctypes.data_as(C.c_void_p) if inp is not None else None,
+                                             len(inp) if inp is not None else 0, out.ctypes.data_as(C.c_void_p),
+                                             len(out), C.byref(n)), "gbo_simulate_to_host")
+        return int(n.value)
 
     def simulate_slice(self, event_id, gensteps, photon_offset, input_photon=None):
         """One launch of the event photons photon_offset.. (gbo_simulate_slice)."""

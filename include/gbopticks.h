@@ -15,6 +15,9 @@
  *   gbo_simulate         G4CXOpticks::simulate(int eventID, bool reset=false) (g4cx/G4CXOpticks.hh:95,
  *                        .cc:466-486) with gensteps that SEvt::AddGenstep collected (sysrap/SEvt.hh:487) and the
  *                        input photons of SEvt::SetInputPhoton; synchronous, hits gathered when it returns
+ *   gbo_simulate_to_host G4CXOpticks::simulate followed by the gather of the event's hits into host memory
+ *                        (QSim::simulate gathers each genstep slice's hits in turn, qudarap/QSim.cc:481-529), in one
+ *                        call
  *   gbo_num_hit          SEvt::GetNumHit(0) (sysrap/SEvt.cc:2050)
  *   gbo_copy_hits        SEvt::getHit(sphoton&, unsigned idx) (sysrap/SEvt.cc:4991), in bulk
  *   gbo_reset            G4CXOpticks::reset(int eventID) (g4cx/G4CXOpticks.hh:96, .cc:499-518)
@@ -132,6 +135,15 @@ int         gbo_engine_create(const gbo_geometry_desc* geom, const gbo_config* c
 void        gbo_engine_destroy(gbo_engine* e);
 int         gbo_simulate(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs,
                          const gbo_sphoton* input_photon, int64_t num_input_photon);
+/* gbo_simulate_to_host : gbo_simulate, then the event's hits (photon order, as gbo_copy_hits gives them) written into
+ * `hits`, room for hit_capacity hits (page-locked memory for full copy speed).  With max_slot set the event runs as
+ * max_slot slices and each slice's hits are copied out as soon as it ends, on a stream of their own.  Results equal
+ * gbo_simulate's for the same event id.  *num_hit receives the hit count; above hit_capacity the call stores the
+ * first hit_capacity hits and returns GBO_ERR_CAPACITY.  The event's hits also stay on the device as after
+ * gbo_simulate. */
+int         gbo_simulate_to_host(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t num_gs,
+                                 const gbo_sphoton* input_photon, int64_t num_input_photon, gbo_sphoton* hits,
+                                 int64_t hit_capacity, int64_t* num_hit);
 int         gbo_simulate_device(gbo_engine* e, int32_t event_id, const void* d_gs, int64_t num_gs,
                                 const void* d_input_photon, int64_t num_input_photon, void* cuda_stream);
 /* gbo_simulate_slice : one launch of a slice of an event, the photons of `gs` being event photons

@@ -310,6 +310,34 @@ def test_sliced_event_equals_whole(E, max_slot):
     sliced.close()
 
 
+@pytest.mark.parametrize("kernel_mode", [2, 3])
+def test_simulate_to_host_equals_simulate_and_copy(E, kernel_mode):
+    """gbo_simulate_to_host: the hits of gbo_simulate + gbo_copy_hits, for events of one launch and a max_slot-sliced
+    event (each slice's hits copied out as it ends); a buffer smaller than the hit count keeps the first hits and the
+    call reports the full count."""
+    from eic_opticks_gb300 import geometry as G, gensteps as GS
+    arrays = G.crystal_array().arrays()
+    small = GS.crystal_scint_gensteps(60, 900, seed=21)
+    big = GS.crystal_scint_gensteps(400, 5000, seed=22)
+    for gs, cfg in ((small, {}), (big, {}), (small, {"max_slot": 9000})):
+        eng = E.Engine(arrays, kernel_mode=kernel_mode, **cfg)
+        n0 = eng.simulate(5, gs)
+        h0 = eng.hits()
+        out = np.zeros(n0 + 3, dtype=E.L.PHOTON)
+        n1 = eng.simulate_to_host(5, gs, out)
+        st = eng.stats()
+        assert n1 == n0 and np.array_equal(out[:n1].view(np.uint32), h0.view(np.uint32))
+        assert np.array_equal(eng.hits().view(np.uint32), h0.view(np.uint32))
+        if cfg:
+            assert st["simulate_launches"] > 1
+        short = np.zeros(n0 // 2, dtype=E.L.PHOTON)
+        with pytest.raises(E.GBOError, match=r"code 4"):
+            eng.simulate_to_host(5, gs, short)
+        assert eng.num_hit() == n0
+        assert np.array_equal(short.view(np.uint32), h0[:len(short)].view(np.uint32))
+        eng.close()
+
+
 def test_shards_on_separate_launches_equal_whole(E):
     """Event shards simulated as separate launches (as on separate GPUs) concatenate to the whole event's hits."""
     from eic_opticks_gb300 import geometry as G, gensteps as GS, shard
