@@ -15,11 +15,13 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdlib>
 #include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
+#include "gbo_gensteps.hh"
 #include "gbopticks.h"
 
 namespace gbo {
@@ -45,6 +47,17 @@ public:
         g.q[0].i[0] = GBO_GS_INPUT_PHOTON;
         g.q[0].u[3] = (uint32_t)n;
         gensteps().push_back(g);
+    }
+    // the gensteps collected for the next simulate (SEvt::GetNumGenstepFromGenstep / GetGenstep, in a copy)
+    static int64_t GetNumGenstepFromGenstep(int /*eidx*/)
+    {
+        std::lock_guard<std::mutex> lock(mutex());
+        return (int64_t)gensteps().size();
+    }
+    static std::vector<gbo_quad6> GetGenstep(int /*eidx*/)
+    {
+        std::lock_guard<std::mutex> lock(mutex());
+        return gensteps();
     }
     static int64_t GetNumHit(int /*eidx*/)
     {
@@ -133,6 +146,29 @@ private:
     }
     static G4CXOpticks*& instance() { static G4CXOpticks* p = nullptr; return p; }
     gbo_engine* engine_ = nullptr;
+};
+
+// U4::CollectGenstep_* (u4/U4.cc:159-185, :278-311): make the genstep from the step's values and add it to the
+// event, honouring the reference's environment switches: U4__CollectGenstep_<name>_DISABLE collects nothing,
+// U4__CollectGenstep_<name>_ZEROPHO collects the genstep with zero photons.
+struct U4 {
+    static void CollectGenstep_DsG4Scintillation_r4695(const TrackInfo& t, const StepPoints& s, uint32_t matline,
+                                                       int32_t numPhotons, int32_t scnt, double ScintillationTime)
+    {
+        if (std::getenv("U4__CollectGenstep_DsG4Scintillation_r4695_DISABLE")) return;
+        if (std::getenv("U4__CollectGenstep_DsG4Scintillation_r4695_ZEROPHO")) numPhotons = 0;
+        SEvt::AddGenstep(MakeGenstep_DsG4Scintillation_r4695(t, s, matline, numPhotons, scnt, ScintillationTime));
+    }
+    static void CollectGenstep_G4Cerenkov_modified(const TrackInfo& t, const StepPoints& s, uint32_t matline,
+                                                   int32_t numPhotons, double betaInverse, double pmin_eV,
+                                                   double pmax_eV, double maxCos, double maxSin2,
+                                                   double meanNumberOfPhotons1, double meanNumberOfPhotons2)
+    {
+        if (std::getenv("U4__CollectGenstep_G4Cerenkov_modified_DISABLE")) return;
+        if (std::getenv("U4__CollectGenstep_G4Cerenkov_modified_ZEROPHO")) numPhotons = 0;
+        SEvt::AddGenstep(MakeGenstep_G4Cerenkov_modified(t, s, matline, numPhotons, betaInverse, pmin_eV, pmax_eV,
+                                                         maxCos, maxSin2, meanNumberOfPhotons1, meanNumberOfPhotons2));
+    }
 };
 
 }  // namespace gbo

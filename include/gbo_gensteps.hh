@@ -36,6 +36,8 @@ struct StepPoint {
 
 struct StepPoints {
     StepPoint pre, post;
+    double step_length = -1.0;  // G4Step::GetStepLength (mm): the true path length, which exceeds the chord |post - pre|
+                                // for steps bent by a field or by multiple scattering; < 0 takes the chord
 };
 
 struct TrackInfo {
@@ -46,6 +48,15 @@ struct TrackInfo {
 };
 
 constexpr double HC_EVNM = 1239.8418754200;       // h c in eV nm (sysrap/smath.h)
+
+// Geant4's internal units and the two constants u4/U4.cc uses for Wmin / Wmax (h_Planck * c_light / p / nm, p in MeV):
+// the SI 2019 definitions in CLHEP's units (mm, ns, MeV), each built in the order CLHEP's headers build it.
+namespace clhep {
+constexpr double MeV = 1.0, eV = 1.e-6 * MeV, e_SI = 1.602176634e-19, joule = eV / e_SI;
+constexpr double ns = 1.0, s = 1.e+9 * ns, mm = 1.0, m = 1000. * mm, nm = 1.e-9 * m;
+constexpr double h_Planck = 6.62607015e-34 * joule * s;
+constexpr double c_light = 2.99792458e+8 * m / s;
+}  // namespace clhep
 
 namespace detail {
 inline void put_f(gbo_quad6& g, int q, int c, double v) { g.q[q].f[c] = (float)v; }
@@ -68,7 +79,7 @@ inline void common(gbo_quad6& g, uint32_t gentype, const TrackInfo& t, const Ste
         put_f(g, 2, k, d);
         len2 += d * d;
     }
-    put_f(g, 2, 3, std::sqrt(len2));                         // step_length
+    put_f(g, 2, 3, s.step_length >= 0.0 ? s.step_length : std::sqrt(len2));      // G4Step::GetStepLength
     put_i(g, 3, 0, t.pdg_code);
     put_f(g, 3, 1, t.charge);
     put_f(g, 3, 2, t.weight);
@@ -88,7 +99,8 @@ inline gbo_quad6 MakeGenstep_DsG4Scintillation_r4695(const TrackInfo& t, const S
 }
 
 // scerenkov layout: q3.w preVelocity, q4 (BetaInverse, Wmin, Wmax, maxCos), q5 (maxSin2, MeanNumberOfPhotons1,
-// MeanNumberOfPhotons2, postVelocity); Wmin/Wmax in nm from the photon energy range pmin/pmax in eV (u4/U4.cc:200-260)
+// MeanNumberOfPhotons2, postVelocity); Wmin/Wmax in nm from the photon energy range pmin/pmax in eV, converted as
+// u4/U4.cc:200-260 converts Geant4's MeV values (h_Planck * c_light / p / nm)
 inline gbo_quad6 MakeGenstep_G4Cerenkov_modified(const TrackInfo& t, const StepPoints& s, uint32_t matline,
                                                   int32_t numPhotons, double betaInverse, double pmin_eV,
                                                   double pmax_eV, double maxCos, double maxSin2,
@@ -98,8 +110,8 @@ inline gbo_quad6 MakeGenstep_G4Cerenkov_modified(const TrackInfo& t, const StepP
     detail::common(g, GBO_GS_G4Cerenkov_modified, t, s, matline, numPhotons);
     detail::put_f(g, 3, 3, s.pre.velocity);
     detail::put_f(g, 4, 0, betaInverse);
-    detail::put_f(g, 4, 1, HC_EVNM / pmax_eV);
-    detail::put_f(g, 4, 2, HC_EVNM / pmin_eV);
+    detail::put_f(g, 4, 1, clhep::h_Planck * clhep::c_light / (pmax_eV * clhep::eV) / clhep::nm);
+    detail::put_f(g, 4, 2, clhep::h_Planck * clhep::c_light / (pmin_eV * clhep::eV) / clhep::nm);
     detail::put_f(g, 4, 3, maxCos);
     detail::put_f(g, 5, 0, maxSin2);
     detail::put_f(g, 5, 1, meanNumberOfPhotons1);
@@ -154,7 +166,7 @@ inline gbo_quad6 MakeGenstep_Cerenkov_FromTable(const TrackInfo& t, const StepPo
     const double maxCos = bi / nmax;
     double len2 = 0.0;
     for (int k = 0; k < 3; k++) len2 += (s.post.pos[k] - s.pre.pos[k]) * (s.post.pos[k] - s.pre.pos[k]);
-    const double step = std::sqrt(len2);
+    const double step = s.step_length >= 0.0 ? s.step_length : std::sqrt(len2);
     const double m1 = CerenkovMeanPhotonsPerMM(t.charge, beta_pre, energy_eV, rindex, n) * step;
     const double m2 = CerenkovMeanPhotonsPerMM(t.charge, beta_post, energy_eV, rindex, n) * step;
     return MakeGenstep_G4Cerenkov_modified(t, s, matline, numPhotons, bi, energy_eV[0], energy_eV[n - 1], maxCos,
