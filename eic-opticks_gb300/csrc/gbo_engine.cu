@@ -393,6 +393,7 @@ struct gbo_engine {
     DBuf<float4> plan;
     DBuf<gbo_qat4> itra;
     DBuf<uint4> optical;
+    DBuf<float> bnd_y;
     cudaArray_t bnd_array = nullptr, icdf_array = nullptr;
     cudaTextureObject_t bnd_tex = 0, icdf_tex = 0;
     int bnd_nx = 0, bnd_ny = 0, hd_factor = 0;
@@ -563,7 +564,7 @@ void gbo_engine_destroy(gbo_engine* e)
     if (e->icdf_tex) cudaDestroyTextureObject(e->icdf_tex);
     if (e->bnd_array) cudaFreeArray(e->bnd_array);
     if (e->icdf_array) cudaFreeArray(e->icdf_array);
-    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->inst_box.release(); e->inner_box.release(); e->overlap.release(); e->clear.release(); e->prim.release(); e->solid.release();
+    e->tlas.release(); e->tlas_index.release(); e->inst.release(); e->inst64.release(); e->inst_box.release(); e->bnd_y.release(); e->inner_box.release(); e->overlap.release(); e->clear.release(); e->prim.release(); e->solid.release();
     e->node.release(); e->plan.release(); e->itra.release(); e->optical.release();
     e->gs.release(); e->gs_end.release(); e->input.release(); e->photon.release(); e->seq.release();
     e->hits_unordered.release(); e->hits.release(); e->merged.release(); gbo::merge_scratch_free(e->merge_scratch); e->merge_scratch = nullptr; e->gen_photon.release(); e->gen_rng.release(); e->gen_hint.release(); e->wf.release(); e->gs_hint.release(); e->bitmap.release(); e->word_prefix.release();
@@ -674,6 +675,13 @@ int gbo_engine_create(const gbo_geometry_desc* g, const gbo_config* cfg, int dev
     e->nms = g->bnd_domain_step;
     e->hd_factor = g->hd_factor;
     TRY(make_texture(&e->bnd_array, &e->bnd_tex, g->bnd, e->bnd_nx, e->bnd_ny, true));
+    {
+        // each boundary-texture row's normalized y, the binary32 quotient the lookups would otherwise divide out
+        std::vector<float> y((size_t)e->bnd_ny);
+        const float rows = (float)e->bnd_ny;
+        for (int iy = 0; iy < e->bnd_ny; iy++) y[(size_t)iy] = ((float)iy + 0.5f) / rows;
+        TRY(upload(e->bnd_y, y.data(), y.size(), e->stream));
+    }
     TRY(make_texture(&e->icdf_array, &e->icdf_tex, g->icdf, g->icdf_nx, g->icdf_ny, false));
     TRY(e->counters.ensure(4));
     {
@@ -719,6 +727,7 @@ static Params make_params(gbo_engine* e)
     P.acc.plan = e->plan.ptr;
     P.acc.itra = e->itra.ptr;
     P.tab.bnd_tex = e->bnd_tex;
+    P.tab.bnd_y = e->bnd_y.ptr;
     P.tab.bnd_nx = (float)e->bnd_nx;
     P.tab.bnd_ny = (float)e->bnd_ny;
     P.tab.nm0 = e->nm0;

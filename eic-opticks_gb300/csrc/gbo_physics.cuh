@@ -23,6 +23,7 @@ constexpr int LOOP_CAP = 100000;
 struct Tables {
     cudaTextureObject_t bnd_tex;     // float4 (761, num_bnd*8), linear, normalized, wrap
     float bnd_nx, bnd_ny, nm0, nms;
+    const float* bnd_y;              // per texture row iy: (iy + 0.5f) / bnd_ny, the row's normalized y, in binary32
     const uint4* optical;            // (num_bnd*4)
     cudaTextureObject_t icdf_tex;    // float (4096, 3)
     int hd_factor;
@@ -85,7 +86,7 @@ GBO_DEV float4 boundary_lookup(const Tables& t, float nm, unsigned line, unsigne
     const float fx = (nm - t.nm0) / t.nms;
     const float x = (fx + 0.5f) / t.bnd_nx;
     const unsigned iy = 2u * line + k;
-    const float y = ((float)iy + 0.5f) / t.bnd_ny;
+    const float y = __ldg(t.bnd_y + iy);              // ((float)iy + 0.5f) / t.bnd_ny, divided once on the host
     return tex2D<float4>(t.bnd_tex, x, y);
 }
 
