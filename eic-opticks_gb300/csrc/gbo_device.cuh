@@ -12,6 +12,9 @@
 #include "../../include/gbo_types.h"
 
 #define GBO_DEV __device__ __forceinline__
+// a branch taken by few photons of any workload (reemission, Rayleigh scattering, diffuse reflection): the compiler
+// lays its code out of the straight path of a step
+#define GBO_UNLIKELY(c) __builtin_expect(!!(c), 0)
 
 namespace gbo {
 

@@ -369,7 +369,7 @@ GBO_DEV int propagate_to_boundary(const Tables& t, Photon& p, const State& s, fl
         if (absorption_distance <= distance_to_boundary) {
             advance(p, absorption_distance, group_velocity, acc);
             const float u_reemit = reemission_prob == 0.f ? 2.f : uniform(rng);
-            if (u_reemit < reemission_prob) {
+            if (GBO_UNLIKELY(u_reemit < reemission_prob)) {
                 const float u_re_wavelength = uniform(rng);
                 const float u_re_mom_ph = uniform(rng);
                 const float u_re_mom_ct = uniform(rng);
@@ -384,7 +384,7 @@ GBO_DEV int propagate_to_boundary(const Tables& t, Photon& p, const State& s, fl
             flag = GBO_BULK_ABSORB;
             return CMD_BREAK;
         }
-    } else if (scattering_distance <= distance_to_boundary) {
+    } else if (GBO_UNLIKELY(scattering_distance <= distance_to_boundary)) {
         advance(p, scattering_distance, group_velocity, acc);
         rayleigh_scatter(p, rng);
         flag = GBO_BULK_SCATTER;
@@ -469,7 +469,7 @@ GBO_DEV int propagate_at_surface(const Tables& t, Photon& p, const State& s, flo
     const int action = u_surface < absorb + detect ? CMD_BREAK : CMD_CONTINUE;
     if (action == CMD_BREAK) {
         flag = u_surface < absorb ? GBO_SURFACE_ABSORB : GBO_SURFACE_DETECT;
-    } else if (u_surface < absorb + detect + reflect_diffuse_) {
+    } else if (GBO_UNLIKELY(u_surface < absorb + detect + reflect_diffuse_)) {
         flag = GBO_SURFACE_DREFLECT;
         const float3 old_mom = p.mom;
         const float orient = dot(old_mom, normal) > 0.f ? -1.f : 1.f;
@@ -516,7 +516,7 @@ GBO_DEV int propagate(const Tables& t, Photon& p, const Hit& h, R& rng, Acc64* a
         // call site, so its code is inlined once)
         if (ems == GBO_EMS_NOSURFACE) command = propagate_at_boundary(t, p, s, h.normal, rng, flag);
         else if (ems == GBO_EMS_SURFACE || h.lposz < 0.f) command = propagate_at_surface(t, p, s, h.normal, rng, flag);
-        else if (ems == GBO_EMS_ZPLUS_SENSOR_A) {
+        else if (GBO_UNLIKELY(ems == GBO_EMS_ZPLUS_SENSOR_A)) {
             skip(rng, 1);
             flag = GBO_SURFACE_DETECT;
             command = CMD_BREAK;
