@@ -1173,9 +1173,11 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
     // lanes gathered per TLAS walk (1: none), Philox blocks by call in the single-leaf binary32 form)
     struct Cand { int mode, refill, period, blocks, walk, rcall; };
     std::vector<Cand> cands = {{1, 32, 1, 0, 1, 0}};
-    for (int r : {1, 2, 4, 8, 16, 32})
+    for (int r : {1, 4, 16})
         for (int p : {1, 4}) cands.push_back({0, r, p, 0, 1, 0});
     for (int r : {1, 2, 4, 8, 16}) cands.push_back({2, r, 1, 0, 1, 0});
+    for (int r : {2, 4})                                                     // refill (compaction) every 2 or 4 steps
+        for (int p : {2, 4}) cands.push_back({2, r, p, 0, 1, 0});
     if (e->csg_form >= 1)                                                    // gathered walks: CSG-tree forms
         for (int w : {16, 24, 32}) cands.push_back({2, 4, 1, 0, w, 0});
     if (e->csg_form == 0 && !e->cfg.precision)

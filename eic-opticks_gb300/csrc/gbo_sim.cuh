@@ -285,7 +285,7 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
     long long idx = -1;
     int bounce = 0;
     int hint = -1;
-    int it = 0;
+    int phase = 0;                  // step count modulo `period`, kept by a counter (a modulo by it would divide)
     Photon p;
     RngT<RCALL> rng;
     Acc64 acc;
@@ -293,12 +293,12 @@ __global__ void GBO_POOL_BOUNDS k_simulate_pool(const __grid_constant__ Params P
     long long cbase = 0;
     int cn = 0, cused = 0;
     bool parked = false;            // the photon's step waits for a gathered TLAS walk
-    for (;; it++) {
+    for (;; phase = phase + 1 == period ? 0 : phase + 1) {
         // refill every `period` steps (or when the warp is empty): idle lanes take the next photon indices in lane
         // order; mode 2 claims them POOL_CHUNK at a time (one atomic per chunk) and loads them as generated, the
         // other pool mode claims exactly the idle lanes' count and generates them
         const unsigned idle = __ballot_sync(0xffffffffu, !live);
-        const bool refill = pool_open && (idle == 0xffffffffu || (it % period == 0 && __popc(idle) >= refill_min));
+        const bool refill = pool_open && (idle == 0xffffffffu || (phase == 0 && __popc(idle) >= refill_min));
         if (PREGEN || P.gen_photon) {
             if (refill)
                 refill_pregenerated<PRECISE>(P, pool, idle, lane, lt, live, idx, p, rng, hint, acc, bounce, cbase, cn,
