@@ -1182,7 +1182,8 @@ int gbo_autotune(gbo_engine* e, int32_t event_id, const gbo_quad6* gs, int64_t n
         for (int w : {16, 24, 32}) cands.push_back({2, 4, 1, 0, w, 0});
     if (e->csg_form == 0 && !e->cfg.precision)
         for (const Cand& c : std::vector<Cand>{{1, 32, 1, 0, 1, 1}, {0, 4, 1, 0, 1, 1}, {0, 4, 4, 0, 1, 1},
-                                               {2, 1, 1, 0, 1, 1}, {2, 4, 1, 0, 1, 1}})
+                                               {2, 1, 1, 0, 1, 1}, {2, 4, 1, 0, 1, 1}, {2, 4, 2, 0, 1, 1},
+                                               {2, 2, 4, 0, 1, 1}})
             cands.push_back(c);
     cands.push_back({3, 4, 1, 0, 1, 0});                                     // the wavefront form
     if (e->csg_form == 0 && !e->cfg.precision) cands.push_back({3, 4, 1, 0, 1, 1});
