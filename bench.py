@@ -41,16 +41,16 @@ L2_FLUSH_BYTES = 256 << 20
 # ncu DRAM bytes (read + write) per photon of the simulate kernels, scaled to the benchmark event by its photon count
 # (all of it grows with the photons), each with the build it was captured on: one thread per photon on the crystal
 # event (k_simulate, 1M photons: gensteps in, hits and hit bitmap out), the pregenerated pool on the crystal event
-# (k_generate + k_simulate_pool, 2.5M photons: 0.39 + 197.38 MB and 210.71 + 2.20 MB, larger than L2) and the
+# (k_generate + k_simulate_pool, 2.5M photons: 0.33 + 197.31 MB and 211.36 + 2.20 MB, larger than L2) and the
 # wavefront on the 20,000-sensor sphere (k_generate + k_wf_start + 31 x (3 passes + the walk-queue sort), 5M
 # photons: 8942 MB)
 TRAFFIC_B_PER_PHOTON = {("crystal_array", 1): (443392.0 + 840192.0) / 998319,
-                        ("crystal_array", 2): (0.39e6 + 197.38e6 + 210.71e6 + 2.20e6) / 2499792,
+                        ("crystal_array", 2): (0.33e6 + 197.31e6 + 211.36e6 + 2.20e6) / 2499792,
                         ("large_sphere", 3): 8942.13e6 / 5000000}
 TRAFFIC_SOURCE = {("crystal_array", 1): "ncu DRAM bytes of k_simulate on a 1M-photon crystal event (an earlier "
                                         "build of that kernel), scaled by photons",
                   ("crystal_array", 2): "ncu DRAM bytes of k_generate + k_simulate_pool on a 2.5M-photon crystal "
-                                        "event (commit 41703c6), scaled by photons",
+                                        "event (commit d060c5a), scaled by photons",
                   ("large_sphere", 3): "ncu DRAM bytes of k_generate + the wavefront passes on a 5M-photon event of "
                                        "the 20,000-sensor sphere (commit 246e140), scaled by photons"}
 
