@@ -512,7 +512,7 @@ int gbo_config_default(gbo_config* c)
     c->blocks_per_sm = 0;
     c->refill_period = 1;
     c->walk_min = 1;
-    c->rng_call = 0;
+    c->rng_call = 1;
     c->max_slot = 0;
     long long iv;
     float fv;

@@ -96,10 +96,10 @@ typedef struct gbo_config {
     int32_t  walk_min;              /* pool kernels of geometries with CSG trees: a lane whose step needs a walk of
                                        the instance tree parks until this many lanes of its warp need one (or no other
                                        lane can step), so the walks run together; 1: no parking (1) */
-    int32_t  rng_call;              /* kernels of geometries without CSG trees, binary32: 0 (default) inlines the
-                                       Philox rounds at every draw site, 1 computes each block of four draws by an
-                                       out-of-line call (smaller code; the CSG-tree kernels always do).  Same numbers
-                                       either way */
+    int32_t  rng_call;              /* kernels of geometries without CSG trees, binary32: 1 (default) computes each
+                                       block of four draws by an out-of-line call (smaller code; the CSG-tree kernels
+                                       always do), 0 inlines the Philox rounds at every draw site.  Same numbers either
+                                       way */
     int32_t  reserved;
 } gbo_config;
 
